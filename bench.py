@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark: 1-D Couette flow in argon, the batched (fused, graph-replayed)
+DSMC step on one GB300.
+
+Workload (the scaled Couette configuration): 50,000 uniform cells over
+L = 5e-4 m, 400 particles per cell (2e7 Ar particles), n = 1e23 m^-3,
+T0 = T_wall = 273 K, diffuse walls moving at -/+500 m/s, dt = 0.2 / nu
+(mean_collision_frequency), VHS Ar.  One step = ntc_equal_weight! ->
+convect + wall reflection -> counting sort -> compute_props_sorted! ->
+avg_props! (the averaging phase of simulations/1D/couette_benchmarking.jl).
+Synthetic, seeded initial state sampled on the device.  The particle state
+(2.5 GB) is larger than L2, so no flush is needed between steps.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl merzgpu|reference]
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "merzbild.jl_gb300"))
+
+L_DOMAIN, NDENS, T_WALL, V_WALL = 5e-4, 1e23, 273.0, 500.0
+ALG_BYTES = 112  # per particle-step: every particle read once and written once (7 FP64)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="merzgpu", choices=["merzgpu", "reference"])
+    p.add_argument("--cells", type=int, default=50000)
+    p.add_argument("--ppc", type=int, default=400)
+    p.add_argument("--plain-steps", type=int, default=1)
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--seed", type=int, default=1234)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Barrier:
+    """Host barrier across ranks (gloo); a no-op for one process."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def __call__(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(args):
+    return {"workload": "1D Couette, Ar, diffuse walls 273 K at -/+500 m/s, n=1e23 m^-3, dt=0.2/nu, "
+                        f"{args.cells} cells x {args.ppc} ppc",
+            "cells": args.cells, "ppc": args.ppc, "particles": args.cells * args.ppc,
+            "step": "ntc_equal_weight -> convect -> sort -> compute_props_sorted -> avg_props",
+            "l2": "inputs larger than L2 (particle state %.1f GB)" % (args.cells * args.ppc * 124 / 1e9)}
+
+
+def setup_device(mz, ctx, args, seed):
+    sp = [mz.Species("Ar", mz.AR_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    grid = mz.Grid1DUniform(L_DOMAIN, args.cells)
+    Fnum = grid.dx * NDENS / args.ppc
+    walls = mz.MaxwellWalls1D(sp, T_WALL, T_WALL, -V_WALL, V_WALL, 1.0, 1.0)
+    dt = 0.2 / mz.mean_collision_frequency(inter, sp, 0, NDENS, T_WALL)
+    cap = int(args.cells * args.ppc * 1.05) + 1024
+    dom = mz.Domain(ctx, args.cells, sp, cap, interactions=inter, seed=seed)
+    dom.set_cell_volumes(grid.V)
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], T_WALL, T_WALL, Fnum)
+    dom.set_sigma_g_w_max(0, 0, smax)
+    return sp, inter, grid, Fnum, walls, dt, dom, smax
+
+
+def make_plan(mz, grid, walls, dt, step0, n_avg, graph=True):
+    plan = mz._lib.StepPlan()
+    plan.dims = 1
+    plan.collide = 1
+    plan.equal_weight = 1
+    plan.props = 1
+    plan.avg_start = 1
+    plan.n_avg = n_avg
+    plan.dt = dt
+    plan.dw_tol = 1e-16
+    plan.step0 = step0
+    plan.use_graph = 1 if graph else 0
+    plan.grid = grid.c_struct()
+    plan.walls = walls.c_struct()
+    return plan
+
+
+AR_MASS = 66.3e-27                 # data/particles.toml
+AR_VHS = (4.11e-10, 0.81, 273.0)   # data/vhs.toml: vhs_d, vhs_o, vhs_Tref
+
+
+def cpu_oracle_run(args, steps, time_budget=None, nthreads=None):
+    """The oracle (C++ restatement of the reference path) on the host cores:
+    the same workload, `steps` steps (or until time_budget seconds).  Uses
+    nothing from the GPU package."""
+    import math
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    nthreads = nthreads or os.cpu_count() or 1
+    g = oracle.grid(L_DOMAIN, args.cells)
+    Fnum = g["dx"] * NDENS / args.ppc
+    d, om, tr = AR_VHS
+    # mean_collision_frequency (collisional_props.jl:42-47)
+    nu = 4.0 * d * d * NDENS * math.sqrt(math.pi * 1.380649e-23 * tr / AR_MASS) * (T_WALL / tr) ** (1.0 - om)
+    dt = 0.2 / nu
+    walls = [T_WALL, T_WALL, 0.0, -V_WALL, 0.0, 0.0, V_WALL, 0.0, 1.0, 1.0]
+    V = [g["dx"]] * args.cells
+    o = oracle.Oracle(args.cells, 1, [AR_MASS])
+    o.load_interactions(d, om, tr)
+    o.pv_create(0, int(args.cells * args.ppc * 1.05) + 1024)
+    o.sample_grid_ndens(0, L_DOMAIN, args.cells, NDENS, T_WALL, Fnum, seed=args.seed, step=0)
+    o.cf_set_smax(0, 0, o.estimate_single(0, 0, T_WALL, T_WALL, Fnum))
+    _, nt, _ = o.pia_get()
+    n = int(nt[0])
+    done = 0
+    t0 = time.perf_counter()
+    for t in range(1, steps + 1):
+        o.ntc_cells(0, 0, dt, V, args.seed, t, equal_weight=True, nthreads=nthreads)
+        o.convect(0, L_DOMAIN, args.cells, walls, dt, args.seed, t, nthreads=nthreads)
+        o.sort(0, L=L_DOMAIN, nx=args.cells)
+        o.compute_props(mode=2, nthreads=nthreads)
+        done += 1
+        if time_budget and time.perf_counter() - t0 > time_budget:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done * n / el, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{done} full steps of the same workload ({args.cells} cells, {n} particles), "
+                      "C++ oracle restating the reference path, OpenMP over cells",
+            "seconds": el, "steps": done}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    if args.warmup:
+        cpu_oracle_run(args, 1)
+    r = cpu_oracle_run(args, steps)
+    out = {"impl": "reference", "metric": "particle-steps/s", "value": r["value"], "unit": "particle-steps/s",
+           "n_gpus": 0, "steps": r["steps"], "warmup": args.warmup,
+           "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload(args),
+           "cpu_baseline": {"value": r["value"], "unit": r["unit"], "cores": r["cores"], "kind": r["kind"],
+                            "sample": r["sample"]},
+           "e2e": {"value": r["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0},
+           "note": "reference Julia path unavailable here (no Julia toolchain); timed: the oracle's C++ "
+                   "restatement of the reference algorithm on the host cores"}
+    print(json.dumps(out))
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import numpy as np
+
+    import merzgpu as mz
+    from merzgpu import build as b
+
+    b.build()
+    barrier = Barrier(world)
+    ctx = mz.Context(local)
+    seed = args.seed + 7919 * rank  # independent replicas
+    sp, inter, grid, Fnum, walls, dt, dom, smax = setup_device(mz, ctx, args, seed)
+    dom.sample_grid_ndens(0, grid, NDENS, T_WALL, Fnum, step=0)
+    n = dom.info(0)["n_total"]
+    inst = mz.PhysProps(dom)
+    avg = mz.PhysProps(dom)
+    K, W = args.steps, args.warmup
+    # warm-up
+    dom.step(make_plan(mz, grid, walls, dt, 0, K), W, inst, avg)
+    mz.clear_props(avg)
+    dom.counters(reset=True)
+    plan = make_plan(mz, grid, walls, dt, W, K)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    barrier()
+    ctx.synchronize()
+    ctx.timer_start()
+    dom.step(plan, K, inst, avg)
+    ms = ctx.timer_stop()
+    ctx.synchronize()
+    barrier()
+    launches = ctx.launch_count() - launches0
+    clk = clocks.stop()
+    cnt = dom.counters(reset=True)
+    t_max = barrier.max(ms / 1e3)
+    total_ps = barrier.sum(float(n) * K)
+    value = total_ps / t_max
+    coll = barrier.sum(float(cnt["accepted"])) / t_max
+    cand = barrier.sum(float(cnt["candidates"])) / t_max
+
+    # per-kernel CUDA-event timing (direct launches, same stream) for the roofline
+    ctx.set_kernel_timing(True)
+    kt_steps = max(3, min(K, 6))
+    dom.step(make_plan(mz, grid, walls, dt, W + K, kt_steps, graph=False), kt_steps, inst, avg)
+    timings = ctx.kernel_timings()
+    ctx.set_kernel_timing(False)
+    tot = sum(v[0] for v in timings.values())
+    kname = "step_cell" if "step_cell" in timings else max(timings.items(), key=lambda kv: kv[1][0])[0]
+    kms, klaunch = timings[kname]
+    avg_launch_s = kms / klaunch / 1e3
+    peak, peak_kind = measured_peaks()
+    achieved = ALG_BYTES * n / avg_launch_s / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "step_cell_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("dram_bytes_per_particle")
+        if traffic is not None:
+            traffic = traffic * n
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": ALG_BYTES * n,
+                "kernel_share": {k: v[0] / tot for k, v in sorted(timings.items(), key=lambda kv: -kv[1][0])}}
+
+    # plain form: the reference's call granularity -- one ntc launch per cell,
+    # then convect, sort and props as separate calls
+    plain = None
+    if not args.no_plain and rank == 0:
+        rng = mz.PhiloxRNG(seed, W + K + kt_steps)
+        pp = mz.PhysProps(dom)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.plain_steps):
+            rng.next_step()
+            for c in range(args.cells):
+                mz.ntc_equal_weight(rng, dom, c, 0, dt)
+            mz.convect_particles(rng, grid, walls, dom, 0, dt)
+            mz.sort_particles(dom, 0, grid)
+            mz.compute_props_sorted(dom, pp)
+        ctx.synchronize()
+        el = time.perf_counter() - t0
+        pv = n * args.plain_steps / el
+        plain = {"value": pv, "unit": "particle-steps/s", "steps": args.plain_steps,
+                 "ms_per_step": 1e3 * el / args.plain_steps, "launches_per_step": args.cells + 6,
+                 "batched_over_plain": value / world / pv}
+
+    # end to end through the C ABI with host buffers: upload the initial state,
+    # K steps, read the cell properties back every step
+    e2e = None
+    if not args.no_e2e:
+        w, v, x, cell = dom.download(0)
+        w, v, x = np.ascontiguousarray(w), np.ascontiguousarray(v), np.ascontiguousarray(x)
+        cell = np.ascontiguousarray(cell)
+        ctx.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        dom2 = dom
+        dom2.upload(0, w, v, x, cell)
+        d2h = 0
+        for k in range(K):
+            dom2.step(make_plan(mz, grid, walls, dt, 1000 + k, 1), 1, inst, None)
+            r = inst.fetch()
+            d2h += r["np"].nbytes + r["n"].nbytes + r["v"].nbytes + r["T"].nbytes
+        ctx.synchronize()
+        el = barrier.max(time.perf_counter() - t0)
+        h2d = w.nbytes + v.nbytes + x.nbytes + cell.nbytes
+        e2e = {"value": barrier.sum(float(n) * K) / el, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
+               "note": f"initial state uploaded once ({h2d} B) inside the timed region, amortised over {K} steps; "
+                       "cell properties (np, n, v, T) read back after every step"}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        r = cpu_oracle_run(args, 20, time_budget=15.0)
+        cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+               "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, sampled on the device)",
+               "config": workload(args) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+               "collisions_per_s": coll, "candidates_per_s": cand,
+               "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
+               "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+               "plain": plain}
+        print(json.dumps(out))
+    dom.close()
+    ctx.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,263 @@
+/*
+ * merzgpu -- GB300 (sm_103a) implementation of Merzbild.jl's per-step DSMC hot
+ * path behind a plain C ABI.
+ *
+ * Conventions
+ *   - Every function returns an int status: MZ_OK (0) or an MZ_E_* code.
+ *     mz_last_error() returns the message of the last failure on a context.
+ *   - Indices are 0-based.  Merzbild.jl is 1-based; a Julia binding adds or
+ *     subtracts 1 at the boundary (cells, slots, indexer fields).
+ *   - Host pointers passed in are only read during the call (copied); output
+ *     pointers are written before the call returns.
+ *   - A domain is bound to one context (one device, one stream).  Calls on a
+ *     domain are enqueued on that stream and may return before the device has
+ *     finished; functions that return data to the host synchronize.  Handles
+ *     are not thread-safe: use one host thread per context.
+ *   - Array layouts of property outputs follow Merzbild.jl's Julia
+ *     column-major arrays so a binding can pass its arrays straight through:
+ *     np/n/T are (n_cells, n_species), v is (3, n_cells, n_species), moments is
+ *     (n_moments, n_cells, n_species).
+ *   - Random numbers are counter-based (Philox4x32-10); every call that draws
+ *     takes an explicit `step` and draws from streams keyed on
+ *     (seed, step, cell, particle/candidate), so results do not depend on
+ *     launch shape, batching, or the order of cells.
+ */
+#ifndef MERZGPU_H
+#define MERZGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MZ_ABI_VERSION 1
+#define MZ_MAX_SPECIES 4
+
+enum {
+    MZ_OK = 0,
+    MZ_E_ARG = 1,       /* invalid argument */
+    MZ_E_CUDA = 2,      /* CUDA runtime error */
+    MZ_E_CAPACITY = 3,  /* particle storage full (grow with mz_domain_reserve) */
+    MZ_E_TIMEOUT = 4,   /* a bounded device wait gave up */
+    MZ_E_STATE = 5,     /* device status word reported a failed invariant */
+    MZ_E_NOMEM = 6      /* device allocation failed */
+};
+
+/* flags */
+#define MZ_NTC_EQUAL_WEIGHT 1        /* ntc_equal_weight! semantics (no splitting) */
+#define MZ_CONVECT_COMPUTE_CELL 1    /* convect_particles_and_compute_cell! */
+#define MZ_PROPS_ALL 0               /* compute_props!: group1 and group2 */
+#define MZ_PROPS_MOMENTS 1           /* compute_props_with_total_moments! */
+#define MZ_PROPS_SORTED 2            /* compute_props_sorted!: group1 only */
+
+typedef struct mz_ctx_s mz_ctx;
+typedef struct mz_domain_s mz_domain;
+typedef struct mz_props_s mz_props;
+
+/* Interaction (collision_utils.jl:73-82) */
+typedef struct {
+    double m_r, mu1, mu2, vhs_d, vhs_o, vhs_Tref, vhs_muref, vhs_factor;
+} mz_interaction;
+
+/* ParticleIndexer (particles.jl:56-66), 0-based slots, empty group: start 0, end -1 */
+typedef struct {
+    int64_t n_local, start1, end1, n_group1, start2, end2, n_group2;
+} mz_particle_indexer;
+
+/* CollisionFactors (collision_ntc.jl:18-25) */
+typedef struct {
+    int64_t n1, n2;
+    double sigma_g_w_max;
+    int64_t n_coll, n_coll_performed, n_eq_w_coll_performed;
+} mz_collision_factors;
+
+/* Grid1DUniform (grid_uniform1D.jl:49-86) */
+typedef struct {
+    double L;
+    int64_t n_cells;
+    double dx, inv_dx, min_x, max_x;
+} mz_grid1d;
+
+/* MaxwellWalls1D (boundary_conditions.jl:29-53); wall 0 = left, 1 = right */
+typedef struct {
+    double T[2];
+    double v[2][3];
+    double accommodation[2];
+    double reflection_v_sq[2][MZ_MAX_SPECIES]; /* 2 k_B T_wall / m_species */
+} mz_walls1d;
+
+/* OctreeN2Merge options (merging_octree_N2.jl:235-246) */
+typedef struct {
+    int32_t split;              /* 1 = OctreeBinMidSplit (the only split implemented) */
+    int32_t init_bin_bounds;    /* 1 = MinMaxVel, 2 = MinMaxVelSym, 3 = C */
+    int32_t bin_bounds_compute; /* 1 = Inherit, 2 = Recompute */
+    int32_t max_Nbins;
+    int32_t max_depth;
+} mz_octree_params;
+
+typedef struct {
+    unsigned long long candidates, accepted, splits, merges, wall_hits;
+} mz_counters;
+
+/* Fused multi-step driver: one step = ntc (every species pair, reference
+ * order) -> convect + cell (1D) -> counting sort -> compute_props_sorted! /
+ * compute_props! -> avg_props!.  Mirrors the time loops of
+ * simulations/1D/couette_benchmarking.jl:58-85 and README.md:91-106. */
+typedef struct {
+    int32_t dims;         /* 0: 0D cells (no convection, no sort); 1: 1D grid */
+    int32_t collide;      /* 1: run NTC each step */
+    int32_t equal_weight; /* 1: ntc_equal_weight!; 0: ntc! (requires 0D or no splits in flight) */
+    int32_t props;        /* 1: compute props at the end of every step */
+    int64_t avg_start;    /* 1-based step of this call from which props are averaged; <= 0: never */
+    int64_t n_avg;        /* avg_props! denominator */
+    double dt;
+    double dw_tol;
+    uint64_t step0;       /* RNG step index of the first step */
+    int32_t use_graph;    /* capture the step in a CUDA graph and replay it */
+    int32_t reserved;
+    mz_grid1d grid;
+    mz_walls1d walls;
+} mz_step_plan;
+
+/* ---------------------------------------------------------------- context */
+int mz_version(void);
+int mz_ctx_create(int device, mz_ctx** out);
+int mz_ctx_destroy(mz_ctx* ctx);
+int mz_ctx_synchronize(mz_ctx* ctx);
+int mz_last_error(const mz_ctx* ctx, char* buf, size_t len);
+/* the context's cudaStream_t, for callers that record their own events */
+int mz_ctx_stream(mz_ctx* ctx, void** stream);
+/* event timing on the context stream */
+int mz_timer_start(mz_ctx* ctx);
+int mz_timer_stop(mz_ctx* ctx, double* ms);
+/* write a scratch buffer larger than L2 (cache flush between timed runs) */
+int mz_ctx_flush_l2(mz_ctx* ctx);
+/* per-kernel CUDA-event timing of the library's own launches (0 = off) */
+int mz_ctx_set_kernel_timing(mz_ctx* ctx, int enable);
+/* name, total ms and launch count of timed kernel k (k < *n_kernels) */
+int mz_kernel_timing(mz_ctx* ctx, int k, char* name, size_t len, double* total_ms, int64_t* launches,
+                     int* n_kernels);
+/* number of library kernels launched since context creation */
+int mz_launch_count(mz_ctx* ctx, int64_t* launches);
+
+/* ---------------------------------------------------------------- domain */
+/* ParticleIndexerArray(n_cells, n_species) + ParticleVector(capacity[s]) per
+ * species + the CollisionFactors array of all pairs and cells. */
+int mz_domain_create(mz_ctx* ctx, int64_t n_cells, int32_t n_species, const int64_t* capacity, mz_domain** out);
+int mz_domain_destroy(mz_domain* dom);
+/* grow a species' storage (Base.resize!, particles.jl:269-298) */
+int mz_domain_reserve(mz_domain* dom, int32_t species, int64_t capacity);
+int mz_domain_info(mz_domain* dom, int32_t species, int64_t* capacity, int64_t* n_total, int64_t* high_water);
+/* species masses (load_species_data, particles.jl:580-591) */
+int mz_set_species(mz_domain* dom, const double* mass);
+/* interactions [s1 + n_species * s2] (load_interaction_data, collision_utils.jl:159-202) */
+int mz_set_interactions(mz_domain* dom, const mz_interaction* inter);
+/* cell volumes (Grid1DUniform cells V / 0-D V); NULL resets to 1.0 */
+int mz_set_cell_volumes(mz_domain* dom, const double* V);
+int mz_set_seed(mz_domain* dom, uint64_t seed);
+/* per-cell RNG keys for independent instances sharing one domain: seed,
+ * stream id and step offset per cell; NULL arrays reset to the domain defaults */
+int mz_set_cell_rng(mz_domain* dom, const uint64_t* seed, const uint32_t* rid, const uint32_t* step_offset);
+
+/* ---------------------------------------------------------------- particles */
+/* Load n particles of one species (w[n], v[n][3], x[n][3], cell[n] 0-based).
+ * The layout is sorted by cell (stable in the given order), every cell's
+ * particles in group 1: the state sample_particles_equal_weight! +
+ * sort_particles! leave (distributions_and_sampling.jl:477-509). */
+int mz_upload_particles(mz_domain* dom, int32_t species, int64_t n, const double* w, const double* v, const double* x,
+                        const int32_t* cell);
+/* Load raw slots plus an explicit indexer (n_cells entries, 0-based slots);
+ * slots no indexer entry covers are dead.  Reproduces hand-built
+ * ParticleIndexerArray states of the reference tests. */
+int mz_upload_particles_indexed(mz_domain* dom, int32_t species, int64_t n_slots, const double* w, const double* v,
+                                const double* x, const mz_particle_indexer* indexer);
+/* Particles in logical order (cells ascending, each cell's group1 then
+ * group2: pv[i] over the indexer); *n_out = n_total.  cell may be NULL. */
+int mz_download_particles(mz_domain* dom, int32_t species, int64_t max_n, double* w, double* v, double* x,
+                          int32_t* cell, int64_t* n_out);
+int mz_get_indexer(mz_domain* dom, int32_t species, mz_particle_indexer* out, int64_t* n_total);
+
+/* ---------------------------------------------------------------- collisions */
+int mz_set_collision_factors(mz_domain* dom, int32_t s1, int32_t s2, const double* sigma_g_w_max);
+int mz_get_collision_factors(mz_domain* dom, int32_t s1, int32_t s2, mz_collision_factors* out);
+/* ntc! / ntc_equal_weight! for cells [cell_begin, cell_end) of pair (s1, s2):
+ * single species when s1 == s2 (collision_ntc.jl:338-380, :479-521), two
+ * species otherwise (collision_ntc.jl:412-453, :554-595).  Cell volumes from
+ * mz_set_cell_volumes.  Split particles (dw_tol, collision_ntc.jl:223-270) go
+ * to the cell's group 2. */
+int mz_ntc(mz_domain* dom, int32_t s1, int32_t s2, double dt, int64_t cell_begin, int64_t cell_end, uint64_t step,
+           int32_t flags, double dw_tol);
+
+/* ---------------------------------------------------------------- properties */
+/* PhysProps(n_cells, n_species, moments_list; ndens_not_Np, Tref) (physical_props.jl:24-58) */
+int mz_props_create(mz_domain* dom, int32_t n_moments, const int32_t* moment_powers, double Tref, int32_t ndens_not_Np,
+                    mz_props** out);
+int mz_props_destroy(mz_props* p);
+/* compute_props! / compute_props_with_total_moments! / compute_props_sorted! (MZ_PROPS_*) */
+int mz_compute_props(mz_domain* dom, mz_props* p, int32_t mode);
+/* avg_props! (physical_props.jl:281-299) */
+int mz_avg_props(mz_props* avg, const mz_props* inst, double n_avg_timesteps);
+/* clear_props! (physical_props.jl:256-262) */
+int mz_clear_props(mz_props* p);
+/* copy to host; any pointer may be NULL */
+int mz_props_download(mz_props* p, double* lpa, double* np, double* n, double* v, double* T, double* moments);
+
+/* ---------------------------------------------------------------- convection */
+/* convect_particles! (convection_1D.jl:130-157) or, with
+ * MZ_CONVECT_COMPUTE_CELL, convect_particles_and_compute_cell! (:225-255) */
+int mz_convect_1d(mz_domain* dom, int32_t species, const mz_grid1d* grid, const mz_walls1d* walls, double dt,
+                  uint64_t step, int32_t flags);
+
+/* ---------------------------------------------------------------- sorting */
+/* sort_particles!(gridsort, grid, ...) when grid != NULL (cells from x,
+ * grid_sorting.jl:58-113), sort_particles!(gridsort, ...) with the cells
+ * stored by convect_particles_and_compute_cell! otherwise (:128-182).
+ * out_index (optional, n_total entries): for every sorted slot, the logical
+ * position (0-based) it held before the sort -- the permutation the
+ * reference writes into ParticleVector.index. */
+int mz_sort(mz_domain* dom, int32_t species, const mz_grid1d* grid, int64_t* out_index);
+/* squash_pia! (particles.jl:622-701): close the gaps left by deletions; each
+ * cell's logical order is kept and every cell ends up in group 1 */
+int mz_squash(mz_domain* dom, int32_t species);
+
+/* ---------------------------------------------------------------- merging */
+/* merge_octree_N2_based! (merging_octree_N2.jl:1060-1094) for every cell in
+ * [cell_begin, cell_end) whose particle count exceeds `threshold`
+ * (threshold < 0: every non-empty cell), batched in one launch.  grid != NULL
+ * selects the 1-D variant that clamps new positions (:830-933).
+ * *n_merged (optional) receives the number of merged cells. */
+int mz_merge_octree_n2(mz_domain* dom, int32_t species, int64_t cell_begin, int64_t cell_end, int64_t threshold,
+                       int64_t target_np, const mz_octree_params* params, const mz_grid1d* grid, uint64_t step,
+                       int64_t* n_merged);
+
+/* ---------------------------------------------------------------- sampling */
+/* sample_particles_equal_weight! for a set of cells at once: counts[c]
+ * particles in cell c (appended to the cell, which must be empty), velocities
+ * Maxwellian with per-axis temperatures T3[c][3] (T3 NULL: T3_all) or BKW
+ * (distribution 1, T3[c][0] as T), weights Fnum[c] * 10^(span * (2U - 1))
+ * (span 0: equal weight), positions uniform in box6[c] = {xlo, xhi, ylo,
+ * yhi, zlo, zhi} (NULL: unit cube).  (distributions_and_sampling.jl:432-509,
+ * 195-213, grid_uniform1D.jl:117-219) */
+int mz_sample_cells(mz_domain* dom, int32_t species, const int64_t* counts, const double* T3, const double* T3_all,
+                    const double* Fnum, double log10_weight_span, const double* box6, int32_t distribution,
+                    uint64_t step);
+/* sample_particles_equal_weight!(rng, grid, ..., ndens::Float64, T, Fnum)
+ * (grid_uniform1D.jl:198-219) */
+int mz_sample_grid_ndens(mz_domain* dom, int32_t species, const mz_grid1d* grid, double ndens, double T, double Fnum,
+                         uint64_t step);
+
+/* ---------------------------------------------------------------- fused step */
+/* n_steps steps of the fused pipeline; inst receives the props of the last
+ * step, avg accumulates avg_props! from plan->avg_start (either may be NULL) */
+int mz_step(mz_domain* dom, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
+
+/* ---------------------------------------------------------------- counters */
+int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MERZGPU_H */

@@ -1,0 +1,346 @@
+// Per-cell device routines shared by the standalone kernels (ntc.cu,
+// props.cu, convect.cu) and the fused step kernel (step.cu), so both paths
+// execute the same arithmetic.
+#pragma once
+
+#include "mz_internal.cuh"
+
+namespace mz {
+
+// ------------------------------------------------------------------ NTC
+// compute_n_coll_single_species / _two_species (collision_ntc.jl:173-197);
+// also resets the per-call counters like ntc! does (:351-353).
+__device__ __forceinline__ int32_t ntc_ncoll(const DomainView& d, CollisionFactors& cf, bool single, int64_t n1,
+                                             int64_t n2, double dt, double V, uint64_t seed, uint32_t pc, uint32_t stp,
+                                             uint32_t rid)
+{
+    Stream st;
+    st.init(seed, TAG_NCOLL, pc, stp, rid, 0);
+    const double U = st.uniform();
+    double f;
+    if (single)
+        f = 0.5 * dt * (double)n1 * (double)(n1 - 1) * cf.smax / V + U;
+    else
+        f = dt * (double)n1 * (double)n2 * cf.smax / V + U;
+    double fl = floor(f);
+    if (!(fl < 1.0e9)) {
+        set_status(d, ST_CAPACITY);
+        fl = fl != fl ? 0.0 : 1.0e9;
+    }
+    const int32_t nci = (int32_t)fl;
+    cf.n1 = (int32_t)n1;
+    cf.n2 = (int32_t)(single ? n1 : n2);
+    cf.n_coll = nci;
+    cf.n_coll_performed = 0;
+    cf.n_eq_w_coll_performed = 0;
+    cf.n_split = 0;
+    return nci;
+}
+
+struct PartV {
+    double w, vx, vy, vz;
+};
+
+__device__ __forceinline__ PartV load_pv(const Cols& A, int32_t slot)
+{
+    PartV p;
+    p.w = A.w[slot];
+    p.vx = A.vx[slot];
+    p.vy = A.vy[slot];
+    p.vz = A.vz[slot];
+    return p;
+}
+
+struct NtcResult {
+    double smax;
+    int32_t perf, eqw, nsp1, nsp2;
+};
+
+// The candidate loop of ntc! / ntc_equal_weight! for one cell, executed by
+// one warp (all 32 lanes call it with identical arguments).
+//   P1, P2: particle columns of the two species (same for single species)
+//   p1, p2: the cell's indexers; grown in place by splits
+//   cell1/key1, cell2/key2: slot-owner arrays, written for split particles
+//   b1/b2: first reserved slot for split particles of species 1/2
+// Candidates are evaluated in conflict-free batches of up to 32 (see ntc.cu).
+template <bool EQW>
+__device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interaction& I, bool single, int c,
+                                              int32_t ncoll, double smax, const Cols& P1, const Cols& P2,
+                                              Indexer& p1, Indexer& p2, int32_t* cell1, int32_t* key1,
+                                              int32_t* cell2, int32_t* key2, int32_t b1, int32_t b2, double dw_tol,
+                                              uint64_t seed, uint32_t pc, uint32_t stp, uint32_t rid)
+{
+    const int lane = threadIdx.x & 31;
+    const double vexp = fma(-2.0, I.vhs_o, 1.0);  // sigma_vhs exponent, collision_cross_sections.jl:179-181
+    NtcResult R;
+    R.perf = 0;
+    R.eqw = 0;
+    R.nsp1 = 0;
+    R.nsp2 = 0;
+    for (int32_t j0 = 0; j0 < ncoll;) {
+        const int32_t j = j0 + lane;
+        const bool valid = j < ncoll;
+        Stream st;
+        st.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)j);
+        int32_t i = -1, k = -2;
+        if (valid) {
+            const int32_t nl1 = p1.n1 + p1.n2;
+            const int32_t nl2 = single ? nl1 : p2.n1 + p2.n2;
+            i = (int32_t)floor(st.uniform() * (double)nl1);
+            k = (int32_t)floor(st.uniform() * (double)nl2);
+            if (single) {
+                int guard = 0;
+                while (i == k && guard++ < (1 << 20)) k = (int32_t)floor(st.uniform() * (double)nl1);
+            }
+        }
+        // the batch ends before the first candidate that touches a particle
+        // of an earlier candidate in the batch
+        bool conflict = false;
+#pragma unroll 8
+        for (int src = 0; src < 31; ++src) {
+            const int32_t ii = __shfl_sync(0xFFFFFFFFu, i, src);
+            const int32_t kk = __shfl_sync(0xFFFFFFFFu, k, src);
+            if (src < lane) {
+                if (single)
+                    conflict |= (ii == i) | (ii == k) | (kk == i) | (kk == k);
+                else
+                    conflict |= (ii == i) | (kk == k);
+            }
+        }
+        const unsigned cm = __ballot_sync(0xFFFFFFFFu, valid && conflict);
+        const int nvalid = min(32, ncoll - j0);
+        int B = cm ? min(nvalid, __ffs(cm) - 1) : nvalid;
+        bool act = lane < B;
+
+        int32_t si = 0, sk = 0;
+        PartV a, b;
+        a.w = b.w = 0.0;
+        double g = 0.0, sgw = -1.0;
+        bool has = false;
+        if (act) {
+            si = map_slot(p1, i);
+            sk = map_slot(p2, k);
+            a = load_pv(P1, si);
+            b = load_pv(P2, sk);
+            // compute_g! (collision_utils.jl:388-391)
+            const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
+            g = sqrt((gx * gx + gy * gy) + gz * gz);
+            has = g > EPS;
+            if (has) sgw = I.vhs_factor * pow(g, vexp) * g * fmax(a.w, b.w);
+        }
+        // running (sigma g w)_max each candidate is tested against (collision_ntc.jl:229)
+        double m = sgw;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xFFFFFFFFu, m, o);
+            if (lane >= o) m = fmax(m, t);
+        }
+        m = fmax(m, smax);
+        bool acc = false;
+        if (act && has) acc = st.uniform() < sgw / m;  // collision_ntc.jl:231
+        bool spl = false;
+        if (!EQW) {
+            spl = acc && !(fabs(a.w - b.w) < dw_tol);
+            const unsigned sm = __ballot_sync(0xFFFFFFFFu, spl);
+            if (sm) B = min(B, __ffs(sm));  // the batch ends after the first split
+        }
+        act = lane < B;
+        acc = acc && act;
+        spl = spl && act;
+        int side = 0;
+        if (acc) {
+            // compute_com! (collision_utils.jl:374-376)
+            const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
+            const double cy = I.mu1 * a.vy + I.mu2 * b.vy;
+            const double cz = I.mu1 * a.vz + I.mu2 * b.vz;
+            if (!EQW && spl) {
+                // split the heavier particle; the new particle keeps the
+                // pre-collision velocity and position (collision_ntc.jl:235-267)
+                const bool heavy_i = a.w > b.w;
+                side = heavy_i ? 1 : 2;
+                const Cols& PP = heavy_i ? P1 : P2;
+                const int32_t src = heavy_i ? si : sk;
+                const PartV& h = heavy_i ? a : b;
+                const double wl = heavy_i ? b.w : a.w;
+                int32_t ns_;
+                if (heavy_i || single)
+                    ns_ = b1 + R.nsp1;
+                else
+                    ns_ = b2 + R.nsp2;
+                PP.w[ns_] = h.w - wl;
+                PP.vx[ns_] = h.vx;
+                PP.vy[ns_] = h.vy;
+                PP.vz[ns_] = h.vz;
+                PP.x[ns_] = PP.x[src];
+                PP.y[ns_] = PP.y[src];
+                PP.z[ns_] = PP.z[src];
+                int32_t* cl = (heavy_i || single) ? cell1 : cell2;
+                int32_t* ky = (heavy_i || single) ? key1 : key2;
+                cl[ns_] = c;
+                ky[ns_] = c;
+                PP.w[src] = wl;
+            }
+            // scatter_vhs! (collision_scattering.jl:17-29)
+            const double phi = TWOPI * st.uniform();
+            double sphi, cphi;
+            sincos(phi, &sphi, &cphi);
+            const double ct = fma(2.0, st.uniform(), -1.0);
+            const double sth = sqrt(1.0 - ct * ct);
+            const double nx = g * (sth * cphi), ny = g * (sth * sphi), nz = g * ct;
+            P1.vx[si] = cx + I.mu2 * nx;
+            P1.vy[si] = cy + I.mu2 * ny;
+            P1.vz[si] = cz + I.mu2 * nz;
+            P2.vx[sk] = cx - I.mu1 * nx;
+            P2.vy[sk] = cy - I.mu1 * ny;
+            P2.vz[sk] = cz - I.mu1 * nz;
+        }
+        const unsigned am = __ballot_sync(0xFFFFFFFFu, acc);
+        R.perf += __popc(am);
+        if (EQW)
+            R.eqw += __popc(am);
+        else
+            R.eqw += __popc(__ballot_sync(0xFFFFFFFFu, acc && fabs(a.w - b.w) < dw_tol));
+        smax = __shfl_sync(0xFFFFFFFFu, m, B - 1);
+        if (!EQW) {
+            const int sd = __shfl_sync(0xFFFFFFFFu, side, B - 1);
+            if (sd == 1 || (sd == 2 && single)) {
+                if (p1.n2 == 0) p1.start2 = b1;
+                p1.n2 += 1;
+                R.nsp1 += 1;
+                if (single) p2 = p1;
+            } else if (sd == 2) {
+                if (p2.n2 == 0) p2.start2 = b2;
+                p2.n2 += 1;
+                R.nsp2 += 1;
+            }
+        }
+        __syncwarp();
+        j0 += B;
+    }
+    R.smax = smax;
+    return R;
+}
+
+// ------------------------------------------------------------------ props
+struct CellMoments {
+    double n, ux, uy, uz, T;
+};
+
+// Two-pass n, u, T of one (cell, species) list, one warp
+// (compute_props!, physical_props.jl:104-154; sorted variant :317-354).
+__device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& p, int32_t nl, double mass)
+{
+    const int lane = threadIdx.x & 31;
+    double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int j = lane; j < nl; j += 32) {
+        const int32_t q = map_slot(p, j);
+        const double w = P.w[q];
+        n += w;
+        sx += P.vx[q] * w;
+        sy += P.vy[q] * w;
+        sz += P.vz[q] * w;
+    }
+    n = warp_sum(n);
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    sz = warp_sum(sz);
+    CellMoments r;
+    r.n = n;
+    r.ux = r.uy = r.uz = r.T = 0.0;
+    if (n > 0.0) {
+        r.ux = sx / n;
+        r.uy = sy / n;
+        r.uz = sz / n;
+        double E = 0.0;
+        for (int j = lane; j < nl; j += 32) {
+            const int32_t q = map_slot(p, j);
+            const double dx = P.vx[q] - r.ux, dy = P.vy[q] - r.uy, dz = P.vz[q] - r.uz;
+            E = fma(P.w[q], (dx * dx + dy * dy) + dz * dz, E);
+        }
+        E = warp_sum(E);
+        E *= 0.5 * mass / (n * K_B);
+        r.T = (2.0 / 3.0) * E;
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------ convection
+struct WallView {
+    double L, min_x, max_x, inv_dx;
+    double vsq[2][MZ_MAX_SPECIES];
+    double wv[2][3];
+    double acc[2];
+};
+
+__device__ __forceinline__ void diffuse_reflect(Stream& st, double& vx, double& vy, double& vz, double vsq,
+                                                double normal, const double* wv)
+{   // diffuse_reflection_x! (boundary_conditions.jl:79-93)
+    double R = fmax(1e-50, st.uniform());
+    const double vn = normal * sqrt(-vsq * log(R));
+    R = fmax(1e-50, st.uniform());
+    const double vt = sqrt(-vsq * log(R));
+    R = TWOPI * st.uniform();
+    double sR, cR;
+    sincos(R, &sR, &cR);
+    vx = vn + wv[0];
+    vy = sR * vt + wv[1];
+    vz = cR * vt + wv[2];
+}
+
+// wall-hit loop of convect_single_particle! (convection_1D.jl:22-42); returns hits
+__device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int s, double& x, double& vx, double& vy,
+                                             double& vz, double dt, bool& cap)
+{
+    double t_rest = dt;
+    double x_old = x;
+    double x_new = fma(vx, dt, x);
+    int hits = 0;
+    while ((x_new >= W.L) || (x_new <= 0.0)) {
+        if (hits >= 1000) {
+            cap = true;
+            break;
+        }
+        ++hits;
+        int bc;
+        double normal;
+        if (x_new >= W.L) {
+            t_rest -= fabs((W.L - x_old) / vx);
+            bc = 1;
+            normal = -1.0;
+            x_old = W.L;
+        } else {
+            t_rest -= fabs(x_old / vx);
+            bc = 0;
+            normal = 1.0;
+            x_old = 0.0;
+        }
+        // reflect_particle_x! (boundary_conditions.jl:108-121)
+        const double acc = W.acc[bc];
+        if (acc == 0.0) {
+            vx = -vx;
+        } else if (acc == 1.0) {
+            diffuse_reflect(st, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
+        } else {
+            if (st.uniform() < acc)
+                diffuse_reflect(st, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
+            else
+                vx = -vx;
+        }
+        x_new = fma(vx, t_rest, x_old);
+    }
+    x = fmin(fmax(x_new, W.min_x), W.max_x);
+    return hits;
+}
+
+// get_cell (grid_uniform1D.jl:97-99), 0-based, clamped with a status flag
+__device__ __forceinline__ int32_t cell_of(const DomainView& d, double x, double inv_dx)
+{
+    double f = floor(x * inv_dx);
+    if (!(f >= 0.0 && f < (double)d.n_cells)) {
+        set_status(d, ST_OUTSIDE_GRID);
+        f = (f < 0.0 || f != f) ? 0.0 : (double)(d.n_cells - 1);
+    }
+    return (int32_t)f;
+}
+
+}  // namespace mz

@@ -1,0 +1,75 @@
+// 1-D convection with Maxwell walls: convect_single_particle!
+// (convection_1D.jl:17-54), convect_particles! (:130-157),
+// convect_particles_and_compute_cell! (:225-255), reflect_particle_x! /
+// diffuse_reflection_x! / specular_reflection_x! (boundary_conditions.jl:63-121).
+//
+// One thread per slot.  A particle's random stream is keyed on (cell, position
+// j in the cell's logical list), so the result does not depend on the
+// physical layout.  Algorithmic bytes per particle: read x, vx (16) + write x
+// (8); wall hitters also read/write vy, vz.
+#include "cell_ops.cuh"
+#include "mz_host.h"
+
+#include <algorithm>
+
+using namespace mz;
+
+namespace {
+
+__global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw, WallView W, double dt, uint32_t step,
+                                                 int compute_cell)
+{
+    const SpeciesView& S = d.sp[s];
+    unsigned long long my_hits = 0;
+    bool cap = false;
+    for (int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < hw;
+         slot += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = S.cell[slot];
+        if (c < 0) continue;
+        const Indexer p = S.ind[c];
+        const int32_t j = (slot >= p.start1 && slot < (int64_t)p.start1 + p.n1) ? (int32_t)(slot - p.start1)
+                                                                                  : p.n1 + (int32_t)(slot - p.start2);
+        Stream st;
+        st.init(cell_seed(d, c), TAG_CONVECT, (uint32_t)s, cell_step(d, c, step), cell_rid(d, c), (uint32_t)j);
+        double x = S.A.x[slot];
+        double vx = S.A.vx[slot];
+        const double xn = fma(vx, dt, x);
+        if ((xn >= W.L) || (xn <= 0.0)) {
+            double vy = S.A.vy[slot], vz = S.A.vz[slot];
+            my_hits += convect_walls(st, W, s, x, vx, vy, vz, dt, cap);
+            S.A.vx[slot] = vx;
+            S.A.vy[slot] = vy;
+            S.A.vz[slot] = vz;
+        } else {
+            x = fmin(fmax(xn, W.min_x), W.max_x);
+        }
+        S.A.x[slot] = x;
+        if (compute_cell) S.key[slot] = cell_of(d, x, W.inv_dx);
+    }
+    if (cap) set_status(d, ST_WALL_HITS);
+    if (my_hits) atomicAdd(&d.counters->wall_hits, my_hits);
+}
+
+}  // namespace
+
+void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w, double dt, uint64_t step,
+                    int32_t flags)
+{
+    mz_ctx* c = d->ctx;
+    SpeciesHost& S = d->sp[s];
+    if (S.hw <= 0) return;
+    WallView W;
+    W.L = g->L;
+    W.min_x = g->min_x;
+    W.max_x = g->max_x;
+    W.inv_dx = g->inv_dx;
+    for (int b = 0; b < 2; ++b) {
+        for (int q = 0; q < MZ_MAX_SPECIES; ++q) W.vsq[b][q] = w->reflection_v_sq[b][q];
+        W.acc[b] = w->accommodation[b];
+        for (int k = 0; k < 3; ++k) W.wv[b][k] = w->v[b][k];
+    }
+    DomainView v = make_view(d);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.hw, 256), (int64_t)c->num_sms * 8));
+    MZ_LAUNCH(c, "convect", k_convect, blocks, 256, 0, v, s, S.hw, W, dt, (uint32_t)step,
+              (flags & MZ_CONVECT_COMPUTE_CELL) ? 1 : 0);
+}

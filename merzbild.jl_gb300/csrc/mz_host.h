@@ -1,0 +1,153 @@
+// Host-side state behind the C ABI (include/merzgpu.h).
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/merzgpu.h"
+#include "mz_internal.cuh"
+
+struct MzError : std::runtime_error {
+    int code;
+    MzError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define MZ_CK(call)                                                                                    \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess)                                                                         \
+            throw MzError(MZ_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));              \
+    } while (0)
+
+#define MZ_REQUIRE(cond, msg)                                                                          \
+    do {                                                                                               \
+        if (!(cond)) throw MzError(MZ_E_ARG, msg);                                                     \
+    } while (0)
+
+struct KernelTiming {
+    std::string name;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    double total_ms = 0.0;
+    int64_t launches = 0;
+};
+
+struct mz_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    void* flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    bool kernel_timing = false;
+    std::vector<KernelTiming> timings;
+    std::vector<cudaEvent_t> event_pool;
+    int64_t launches = 0;
+    int num_sms = 0;
+
+    cudaEvent_t get_event();
+    // bracket a launch with events when kernel timing is on; returns slot or -1
+    int timer_begin(const char* name, cudaEvent_t* start);
+    void timer_end(int slot, cudaEvent_t start);
+    void resolve_timings();
+    bool capturing() const;
+};
+
+struct SpeciesHost {
+    int64_t capacity = 0;
+    int64_t hw = 0;        // high water: slots [0, hw) in use (live or dead)
+    int64_t n_total = 0;   // live particles
+    bool compact = true;   // every cell's list lies in group 1 and no dead slot below hw
+    double* cols[2][7] = {{nullptr}};  // [buffer A/B][w, vx, vy, vz, x, y, z]
+    int cur = 0;           // which buffer is A
+    int32_t* cell[2] = {nullptr, nullptr};  // [A/B] owner cell per slot
+    int32_t* key = nullptr;
+    int32_t* idx = nullptr;
+    int32_t* counts = nullptr;  // n_cells + 1
+    int32_t* fill = nullptr;
+    int32_t* work = nullptr;    // n_cells + 1 scratch (reservations / bases)
+    mz::Indexer* ind = nullptr;
+};
+
+struct mz_domain_s {
+    mz_ctx* ctx = nullptr;
+    int64_t n_cells = 0;
+    int32_t ns = 0;
+    SpeciesHost sp[MZ_MAX_SPECIES];
+    double mass[MZ_MAX_SPECIES] = {0};
+    mz::Interaction inter[MZ_MAX_SPECIES * MZ_MAX_SPECIES];
+    double* d_V = nullptr;
+    uint64_t* d_cell_seed = nullptr;
+    uint32_t* d_cell_rid = nullptr;
+    uint32_t* d_cell_step = nullptr;
+    mz::CollisionFactors* d_cf = nullptr;
+    mz::Counters* d_counters = nullptr;
+    int* d_status = nullptr;
+    int64_t* d_scalar = nullptr;   // small device scratch (totals)
+    int64_t* h_scalar = nullptr;   // pinned mirror
+    uint64_t seed = 1234;
+    // octree scratch (allocated on demand)
+    void* d_merge_scratch = nullptr;
+    size_t merge_scratch_bytes = 0;
+    // fused step: RNG step index and last-block counter
+    uint32_t* d_step = nullptr;
+    unsigned int* d_done = nullptr;
+};
+
+struct mz_props_s {
+    mz_domain* dom = nullptr;
+    int32_t n_moments = 0;
+    int32_t powers[16] = {0};
+    double Tref = 300.0;
+    int32_t ndens = 0;
+    // device arrays in Merzbild's column-major layouts
+    double* np = nullptr;       // n_cells * ns
+    double* n = nullptr;        // n_cells * ns
+    double* v = nullptr;        // 3 * n_cells * ns
+    double* T = nullptr;        // n_cells * ns
+    double* moments = nullptr;  // n_moments * n_cells * ns
+    double lpa[MZ_MAX_SPECIES] = {0};
+};
+
+// ---------------------------------------------------------------- helpers
+mz::DomainView make_view(mz_domain* d);
+void ensure_compact(mz_domain* d, int s);
+void swap_buffers(mz_domain* d, int s);
+void check_status(mz_domain* d);
+int64_t div_up(int64_t a, int64_t b);
+
+// launchers (one per translation unit)
+void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index);
+void launch_compact(mz_domain* d, int s);
+void launch_scan_cells(mz_domain* d, int32_t* counts, mz::Indexer* ind, int32_t* fill, int64_t* total_out,
+                       bool write_indexer, int32_t* base_out, int64_t base_offset);
+void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce, uint64_t step, int32_t flags,
+                double dw_tol);
+void launch_props(mz_domain* d, mz_props* p, int32_t mode);
+void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w, double dt, uint64_t step,
+                    int32_t flags);
+void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const int32_t* counts_dev,
+                         const double* T3, const double* T3_all, const double* Fnum, double span, const double* box6,
+                         int32_t distribution, uint64_t step);
+void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step);
+void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
+                  const mz_octree_params* prm, const mz_grid1d* grid, uint64_t step, int64_t* n_merged);
+void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
+void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v);
+void reserve_species(mz_domain* d, int s, int64_t cap);
+void launch_key_from_cell(mz_domain* d, int s);
+void launch_avg(mz_ctx* c, double* avg, const double* inst, int64_t n, double inv);
+
+#define MZ_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                                           \
+    do {                                                                                               \
+        cudaEvent_t _ev0 = nullptr;                                                                    \
+        int _slot = (ctx)->timer_begin(name, &_ev0);                                                   \
+        kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                               \
+        MZ_CK(cudaGetLastError());                                                                     \
+        (ctx)->launches++;                                                                             \
+        (ctx)->timer_end(_slot, _ev0);                                                                 \
+    } while (0)

@@ -1,0 +1,133 @@
+// Per-cell segment sort + gather used by the counting sort (sort.cu) and the
+// fused step (step.cu).  The scatter pass hands out slots inside a cell's
+// segment in arbitrary (atomic) order; sorting the segment's source slots
+// ascending restores the stable order of sort_particles!
+// (grid_sorting.jl:101-106), after which the particle columns are gathered.
+#pragma once
+
+#include <climits>
+
+#include "mz_internal.cuh"
+
+namespace mz {
+
+// Ascending bitonic sort of 32*E keys held register-major (position r*32+lane).
+template <int E>
+__device__ __forceinline__ void warp_bitonic(int32_t (&v)[E])
+{
+    const int lane = threadIdx.x & 31;
+    constexpr int P = 32 * E;
+#pragma unroll
+    for (int k = 2; k <= P; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    const int rp = r ^ jr;
+                    if (rp > r) {
+                        const bool asc = ((r * 32) & k) == 0;
+                        const int32_t a = v[r], b = v[rp];
+                        const bool sw = asc ? (a > b) : (a < b);
+                        v[r] = sw ? b : a;
+                        v[rp] = sw ? a : b;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    const int p = r * 32 + lane;
+                    const int32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[r], j);
+                    const bool lower = (lane & j) == 0;
+                    const bool asc = (p & k) == 0;
+                    v[r] = (lower == asc) ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+}
+
+// Batcher's odd-even merge sort of a[0, n) in global memory by one warp.
+// Every comparator moves the smaller key to the lower index, so lengths that
+// are not a power of two need no padding.
+__device__ __forceinline__ void warp_oddeven_sort(int32_t* a, int n)
+{
+    const int lane = threadIdx.x & 31;
+    for (int p = 1; p < n; p <<= 1) {
+        for (int k = p; k >= 1; k >>= 1) {
+            const int j0 = k % p;
+            const int nblk = (n - j0 + 2 * k - 1) / (2 * k);
+            for (int t = lane; t < nblk * k; t += 32) {
+                const int b = t / k, i = t - b * k;
+                const int lo = j0 + 2 * k * b + i, hi = lo + k;
+                if (hi < n && (lo / (2 * p)) == (hi / (2 * p))) {
+                    const int32_t x = a[lo], y = a[hi];
+                    if (x > y) {
+                        a[lo] = y;
+                        a[hi] = x;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+__device__ __forceinline__ void copy_particle(const Cols& A, const Cols& B, int32_t src, int64_t dst)
+{
+    B.w[dst] = A.w[src];
+    B.vx[dst] = A.vx[src];
+    B.vy[dst] = A.vy[src];
+    B.vz[dst] = A.vz[src];
+    B.x[dst] = A.x[src];
+    B.y[dst] = A.y[src];
+    B.z[dst] = A.z[src];
+}
+
+template <int E>
+__device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+{
+    const int lane = threadIdx.x & 31;
+    int32_t v[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int q = r * 32 + lane;
+        v[r] = q < N ? S.idx[start + q] : INT_MAX;
+    }
+    warp_bitonic<E>(v);
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int q = r * 32 + lane;
+        if (q < N) {
+            const int64_t dst = (int64_t)start + q;
+            copy_particle(S.A, S.B, v[r], dst);
+            S.cellB[dst] = c;
+            S.key[dst] = c;
+        }
+    }
+}
+
+// Sort the source slots of cell c's segment [start, start + N) and gather the
+// particles from buffer A into the same positions of buffer B (one warp).
+__device__ __forceinline__ void sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+{
+    if (N <= 0) return;
+    if (N <= 32) sort_gather_regs<1>(S, c, start, N);
+    else if (N <= 64) sort_gather_regs<2>(S, c, start, N);
+    else if (N <= 128) sort_gather_regs<4>(S, c, start, N);
+    else if (N <= 256) sort_gather_regs<8>(S, c, start, N);
+    else if (N <= 512) sort_gather_regs<16>(S, c, start, N);
+    else if (N <= 1024) sort_gather_regs<32>(S, c, start, N);
+    else {
+        warp_oddeven_sort(S.idx + start, N);
+        for (int q = (threadIdx.x & 31); q < N; q += 32) {
+            const int64_t dst = (int64_t)start + q;
+            copy_particle(S.A, S.B, S.idx[dst], dst);
+            S.cellB[dst] = c;
+            S.key[dst] = c;
+        }
+    }
+}
+
+}  // namespace mz

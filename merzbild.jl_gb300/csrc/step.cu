@@ -1,0 +1,356 @@
+// Fused time step: the loop body of simulations/1D/couette_benchmarking.jl:58-85
+// (ntc_equal_weight! -> convect_particles! -> sort_particles! ->
+// compute_props_sorted! -> avg_props!) and of the 0-D drivers (README.md:91-106:
+// ntc! for every species pair -> compute_props!).
+//
+// One warp owns one cell for the whole step.  With a 1-D grid, one step is
+//   scan (per species)    : counts accumulated by the previous step -> indexer
+//   scatter (per species) : slot tickets per destination cell
+//   k_cell                : sort the cell's segment and gather its particles
+//                           (A -> B, the only full read+write of particle
+//                           data), compute props of the sorted state, then
+//                           NTC and convection of the next step on the
+//                           gathered particles, new cell ids and counts.
+// so particle data crosses HBM once per step (112 B per particle).  0-D steps
+// run k_cell in place (no sort).  The RNG step index lives in device memory
+// and is advanced by the last block of k_cell, so a whole step is captured
+// once in a CUDA graph and replayed.
+#include "cell_ops.cuh"
+#include "mz_host.h"
+#include "sortnet.cuh"
+
+#include <algorithm>
+
+using namespace mz;
+
+namespace {
+
+struct PropsPtrs {
+    double *np, *n, *v, *T;
+};
+
+struct StepArgs {
+    WallView W;
+    double dt;
+    int dims;          // 0 or 1
+    int gather;        // sort segment + gather A -> B
+    int props;         // compute props of the (gathered) state
+    int physics;       // NTC + convection of the next step
+    int has_inst, has_avg;
+    PropsPtrs inst, avg;
+    double inv_navg;
+    int64_t avg_start; // averaging when (step index of the props) - step0 >= avg_start
+    uint64_t step0;
+    int props_lag;     // props describe the state after step (step - props_lag)
+    uint32_t* step_ptr;   // RNG step of the NTC / convection done by this launch
+    unsigned int* done;   // last-block counter
+};
+
+__device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const CellMoments& r, int32_t np,
+                                            uint32_t step)
+{
+    if (a.has_inst) {
+        a.inst.np[ix] = (double)np;
+        a.inst.n[ix] = r.n;
+        a.inst.v[3 * ix + 0] = r.ux;
+        a.inst.v[3 * ix + 1] = r.uy;
+        a.inst.v[3 * ix + 2] = r.uz;
+        a.inst.T[ix] = r.T;
+    }
+    if (a.has_avg && (int64_t)(step - a.props_lag) - (int64_t)a.step0 >= a.avg_start) {
+        const double f = a.inv_navg;
+        a.avg.np[ix] = fma((double)np, f, a.avg.np[ix]);
+        a.avg.n[ix] = fma(r.n, f, a.avg.n[ix]);
+        a.avg.v[3 * ix + 0] = fma(r.ux, f, a.avg.v[3 * ix + 0]);
+        a.avg.v[3 * ix + 1] = fma(r.uy, f, a.avg.v[3 * ix + 1]);
+        a.avg.v[3 * ix + 2] = fma(r.uz, f, a.avg.v[3 * ix + 2]);
+        a.avg.T[ix] = fma(r.T, f, a.avg.T[ix]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cell(DomainView d, StepArgs a)
+{
+    const uint32_t step = *a.step_ptr;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int ns = d.n_species;
+    unsigned long long cand = 0, accd = 0, hits = 0;
+    bool cap = false;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < d.n_cells; c += nwarps) {
+        Indexer p[MZ_MAX_SPECIES];
+        Cols P[MZ_MAX_SPECIES];
+        for (int s = 0; s < ns; ++s) {
+            const SpeciesView& S = d.sp[s];
+            p[s] = S.ind[c];
+            if (a.gather) sort_gather_segment(S, c, p[s].start1, p[s].n1);
+            P[s] = a.gather ? S.B : S.A;
+        }
+        __syncwarp();
+        // 1-D: props of the freshly sorted state, before the next step's physics
+        if (a.props && a.props_lag == 1) {
+            for (int s = 0; s < ns; ++s) {
+                const CellMoments r = props_cell(P[s], p[s], p[s].n1, d.sp[s].mass);
+                if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p[s].n1, step);
+            }
+        }
+        if (!a.physics && !(a.props && a.props_lag == 0)) continue;
+        const uint64_t seed = cell_seed(d, c);
+        const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
+        const double V = d.cell_V[c];
+        // ntc_equal_weight! for every pair in the reference's order
+        for (int s2 = 0; s2 < ns && a.physics; ++s2) {
+            for (int s1 = s2; s1 < ns; ++s1) {
+                const bool single = s1 == s2;
+                const int cfi = s1 + ns * s2;
+                CollisionFactors cf = d.cf[(size_t)cfi * d.n_cells + c];
+                const uint32_t pc = (uint32_t)(s1 * ns + s2);
+                const int32_t ncoll = ntc_ncoll(d, cf, single, p[s1].n1, p[s2].n1, a.dt, V, seed, pc, stp, rid);
+                NtcResult R;
+                R.smax = cf.smax;
+                R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
+                if (ncoll > 0) {
+                    Indexer q1 = p[s1], q2 = p[s2];
+                    R = ntc_cell<true>(d, d.inter[cfi], single, c, ncoll, cf.smax, P[s1], P[s2], q1, q2, nullptr,
+                                       nullptr, nullptr, nullptr, 0, 0, 0.0, seed, pc, stp, rid);
+                }
+                cand += ncoll;
+                accd += R.perf;
+                if (lane == 0) {
+                    cf.smax = R.smax;
+                    cf.n_coll_performed = R.perf;
+                    cf.n_eq_w_coll_performed = R.eqw;
+                    d.cf[(size_t)cfi * d.n_cells + c] = cf;
+                }
+            }
+        }
+        __syncwarp();
+        // 0-D: compute_props! after the collisions of this step
+        if (a.props && a.props_lag == 0) {
+            for (int s = 0; s < ns; ++s) {
+                const CellMoments r = props_cell(P[s], p[s], p[s].n1, d.sp[s].mass);
+                if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p[s].n1, step);
+            }
+        }
+        if (a.dims != 1 || !a.physics) continue;
+        // convect_particles! + get_cell for the next sort
+        for (int s = 0; s < ns; ++s) {
+            const SpeciesView& S = d.sp[s];
+            const Cols& Q = P[s];
+            const int32_t n1 = p[s].n1, st1 = p[s].start1;
+            for (int j0 = 0; j0 < n1; j0 += 32) {
+                const int j = j0 + lane;
+                const bool in = j < n1;
+                int32_t key = 0;
+                if (in) {
+                    const int64_t q = (int64_t)st1 + j;
+                    double x = Q.x[q];
+                    double vx = Q.vx[q];
+                    const double xn = fma(vx, a.dt, x);
+                    if ((xn >= a.W.L) || (xn <= 0.0)) {
+                        Stream rs;
+                        rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
+                        double vy = Q.vy[q], vz = Q.vz[q];
+                        hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
+                        Q.vx[q] = vx;
+                        Q.vy[q] = vy;
+                        Q.vz[q] = vz;
+                    } else {
+                        x = fmin(fmax(xn, a.W.min_x), a.W.max_x);
+                    }
+                    Q.x[q] = x;
+                    key = cell_of(d, x, a.W.inv_dx);
+                    S.key[q] = key;
+                }
+                const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
+                if (in) warp_agg_add(S.counts, key, m);
+            }
+        }
+    }
+    if (cap) set_status(d, ST_WALL_HITS);
+    hits = __reduce_add_sync(0xFFFFFFFFu, (unsigned)hits);
+    if (lane == 0 && (cand | accd | hits)) {
+        atomicAdd(&d.counters->candidates, cand);
+        atomicAdd(&d.counters->accepted, accd);
+        atomicAdd(&d.counters->wall_hits, hits);
+    }
+    // the last block to finish advances the RNG step for the next launch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(a.done, 1u);
+        if (prev == gridDim.x - 1) {
+            *a.done = 0;
+            *a.step_ptr = step + 1;
+            __threadfence();
+        }
+    }
+}
+
+// scan of the counts the previous k_cell accumulated -> indexer (group 1 only)
+__global__ void __launch_bounds__(1024) k_step_scan(int32_t* counts, int32_t n, Indexer* ind, int32_t* fill,
+                                                    int64_t* total_out)
+{
+    __shared__ long long warp_tot[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int c0 = min(n, t * chunk), c1 = min(n, c0 + chunk);
+    long long local = 0;
+    for (int c = c0; c < c1; ++c) local += counts[c];
+    long long incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const long long v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+        long long vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long u = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+            if (lane >= o) vi += u;
+        }
+        warp_tot[lane] = vi - v;
+        if (lane == 31) *total_out = vi;
+    }
+    __syncthreads();
+    long long run = warp_tot[w] + (incl - local);
+    for (int c = c0; c < c1; ++c) {
+        const int32_t cnt = counts[c];
+        Indexer p;
+        p.start1 = (int32_t)run;
+        p.n1 = cnt;
+        p.start2 = 0;
+        p.n2 = 0;
+        ind[c] = p;
+        fill[c] = 0;
+        counts[c] = 0;
+        run += cnt;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_step_scatter(DomainView d, int s, int64_t n)
+{
+    const SpeciesView& S = d.sp[s];
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const int64_t slot = base + lane;
+        const bool in = slot < n;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
+        if (!in) continue;
+        const int32_t key = S.key[slot];
+        const int32_t pos = S.ind[key].start1 + warp_agg_ticket(S.fill, key, m);
+        S.idx[pos] = (int32_t)slot;
+    }
+}
+
+}  // namespace
+
+void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg)
+{
+    mz_ctx* c = d->ctx;
+    if (n_steps <= 0) return;
+    MZ_REQUIRE(plan->equal_weight, "mz_step: the fused step runs ntc_equal_weight!; use mz_ntc for splitting");
+    for (int s = 0; s < d->ns; ++s) launch_compact(d, s);
+    if (!d->d_step) {
+        MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
+        MZ_CK(cudaMalloc(&d->d_done, sizeof(unsigned int)));
+        MZ_CK(cudaMemsetAsync(d->d_done, 0, sizeof(unsigned int), c->stream));
+    }
+    const uint32_t first = (uint32_t)(plan->step0 + 1);
+    MZ_CK(cudaMemcpyAsync(d->d_step, &first, sizeof first, cudaMemcpyHostToDevice, c->stream));
+
+    StepArgs a;
+    memset(&a, 0, sizeof a);
+    a.W.L = plan->grid.L;
+    a.W.min_x = plan->grid.min_x;
+    a.W.max_x = plan->grid.max_x;
+    a.W.inv_dx = plan->grid.inv_dx;
+    for (int b = 0; b < 2; ++b) {
+        for (int q = 0; q < MZ_MAX_SPECIES; ++q) a.W.vsq[b][q] = plan->walls.reflection_v_sq[b][q];
+        a.W.acc[b] = plan->walls.accommodation[b];
+        for (int k = 0; k < 3; ++k) a.W.wv[b][k] = plan->walls.v[b][k];
+    }
+    a.dt = plan->dt;
+    a.dims = plan->dims;
+    a.has_inst = inst != nullptr;
+    a.has_avg = avg != nullptr && plan->avg_start > 0;
+    if (inst) a.inst = PropsPtrs{inst->np, inst->n, inst->v, inst->T};
+    if (avg) a.avg = PropsPtrs{avg->np, avg->n, avg->v, avg->T};
+    a.inv_navg = plan->n_avg > 0 ? 1.0 / (double)plan->n_avg : 0.0;
+    a.avg_start = plan->avg_start;
+    a.step0 = plan->step0;
+    a.props_lag = plan->dims == 1 ? 1 : 0;
+    a.step_ptr = d->d_step;
+    a.done = d->d_done;
+    const bool want_props = plan->props && (inst || a.has_avg);
+    const int blocks = (int)div_up(d->n_cells, 8);
+
+    auto cell_launch = [&](int gather, int props, int physics) {
+        StepArgs b = a;
+        b.gather = gather;
+        b.props = props;
+        b.physics = physics;
+        DomainView v = make_view(d);
+        // distinct names: the full step (gather + props + physics) is the one
+        // the roofline is quoted on
+        const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
+        MZ_LAUNCH(c, name, k_cell, blocks, 256, 0, v, b);
+    };
+    // one sort of every species from the keys k_cell wrote, gather in k_cell
+    auto sort_launch = [&](int props, int physics) {
+        DomainView v = make_view(d);
+        for (int s = 0; s < d->ns; ++s) {
+            SpeciesHost& S = d->sp[s];
+            MZ_LAUNCH(c, "step_scan", k_step_scan, 1, 1024, 0, S.counts, (int32_t)d->n_cells, S.ind, S.fill,
+                      d->d_scalar + s);
+            const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, 256), (int64_t)c->num_sms * 8));
+            MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total);
+        }
+        cell_launch(1, props, physics);
+        for (int s = 0; s < d->ns; ++s) d->sp[s].cur ^= 1;  // B holds the sorted state
+    };
+
+    const bool graph = plan->use_graph != 0;
+    if (plan->dims == 1) {
+        // the first step's NTC + convection run in place on the sorted state
+        cell_launch(0, 0, plan->collide);
+        const int64_t middle = n_steps - 1;
+        if (middle > 0) {
+            if (graph && middle > 1) {
+                // capture one step (scan, scatter, k_cell) and replay it; the
+                // two buffers alternate, so the graph covers two steps
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t ge = nullptr;
+                const int64_t launches0 = c->launches;
+                MZ_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                sort_launch(want_props, plan->collide);
+                sort_launch(want_props, plan->collide);
+                MZ_CK(cudaStreamEndCapture(c->stream, &g));
+                const int64_t per_graph = c->launches - launches0;
+                MZ_CK(cudaGraphInstantiate(&ge, g, 0));
+                const int64_t pairs = middle / 2;
+                for (int64_t i = 0; i < pairs; ++i) MZ_CK(cudaGraphLaunch(ge, c->stream));
+                c->launches += per_graph * (pairs - 1);
+                if (middle % 2) sort_launch(want_props, plan->collide);
+                // the captured launches swapped `cur` twice: buffers are back
+                // in the order the replays leave them
+                MZ_CK(cudaGraphExecDestroy(ge));
+                MZ_CK(cudaGraphDestroy(g));
+            } else {
+                for (int64_t t = 0; t < middle; ++t) sort_launch(want_props, plan->collide);
+            }
+        }
+        // final sort + props of the last step, no further physics
+        sort_launch(want_props, 0);
+    } else {
+        for (int64_t t = 0; t < n_steps; ++t) cell_launch(0, want_props, plan->collide);
+    }
+    for (int s = 0; s < d->ns; ++s) {
+        d->sp[s].hw = d->sp[s].n_total;
+        d->sp[s].compact = true;
+    }
+}

@@ -1,0 +1,174 @@
+"""The fused, graph-replayed step (mz_step) against the oracle running the
+reference's time loops step by step."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import merzgpu as mz
+from helpers import assert_close_rows, device_logical, interactions, oracle_logical, species
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import merzgpu.build as b
+
+    b.build()
+    c = mz.Context(0)
+    yield c
+    c.close()
+
+
+def couette_plan(grid, walls, dt, step0=0, avg_start=0, n_avg=1, graph=True, props=True):
+    plan = mz._lib.StepPlan()
+    plan.dims = 1
+    plan.collide = 1
+    plan.equal_weight = 1
+    plan.props = 1 if props else 0
+    plan.avg_start = avg_start
+    plan.n_avg = n_avg
+    plan.dt = dt
+    plan.dw_tol = 1e-16
+    plan.step0 = step0
+    plan.use_graph = 1 if graph else 0
+    plan.grid = grid.c_struct()
+    plan.walls = walls.c_struct()
+    return plan
+
+
+def couette_setup(ctx, orc, nx=80, ppc=120, seed=17):
+    sp = species(["Ar"])
+    inter = interactions(sp)
+    L, ndens, T = 5e-4, 1e23, 273.0
+    grid = mz.Grid1DUniform(L, nx)
+    Fnum = grid.dx * ndens / ppc
+    walls = mz.MaxwellWalls1D(sp, T, T, -500.0, 500.0, 1.0, 1.0)
+    dt = 0.2 / mz.mean_collision_frequency(inter, sp, 0, ndens, T)
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], T, T, Fnum)
+    o = orc.Oracle(nx, 1, [sp[0].mass])
+    o.load_interactions(*mz.VHS["Ar,Ar"])
+    o.pv_create(0, 2 * ppc * nx)
+    o.sample_grid_ndens(0, L, nx, ndens, T, Fnum, seed=seed, step=0)
+    o.cf_set_smax(0, 0, smax)
+    dom = mz.Domain(ctx, nx, sp, 2 * ppc * nx, interactions=inter, seed=seed)
+    dom.set_cell_volumes(grid.V)
+    dom.sample_grid_ndens(0, grid, ndens, T, Fnum, step=0)
+    dom.set_sigma_g_w_max(0, 0, smax)
+    return sp, grid, walls, dt, o, dom, seed
+
+
+def oracle_couette(orc, o, grid, walls, dt, seed, steps, avg_start):
+    avg = np.zeros((6, grid.n_cells))
+    n_avg = steps - avg_start + 1
+    for t in range(1, steps + 1):
+        o.ntc_cells(0, 0, dt, grid.V, seed, t, equal_weight=True)
+        o.convect(0, grid.L, grid.n_cells, walls.as_flat_array(), dt, seed, t)
+        o.sort(0, L=grid.L, nx=grid.n_cells)
+        if t >= avg_start:
+            r = o.compute_props(mode=2)
+            inst = np.vstack([r["np"][0], r["n"][0], r["v"][0].T, r["T"][0]])
+            for k in range(6):
+                a = np.ascontiguousarray(avg[k])
+                b = np.ascontiguousarray(inst[k])
+                orc.lib().orc_avg_props(grid.n_cells, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                        b.ctypes.data_as(C.POINTER(C.c_double)), float(n_avg))
+                avg[k] = a
+    return avg
+
+
+@pytest.mark.parametrize("graph,steps", [(True, 6), (False, 3), (True, 1), (True, 2)])
+def test_fused_couette_matches_reference_loop(ctx, orc, graph, steps):
+    sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc)
+    avg_start = max(1, steps - 2)
+    ref_avg = oracle_couette(orc, o, grid, walls, dt, seed, steps, avg_start)
+    inst = mz.PhysProps(dom)
+    avg = mz.PhysProps(dom)
+    dom.step(couette_plan(grid, walls, dt, avg_start=avg_start, n_avg=steps - avg_start + 1, graph=graph), steps,
+             inst, avg)
+    orows, oc = oracle_logical(o, 0)
+    drows, dc = device_logical(dom, 0)
+    assert np.array_equal(oc, dc)
+    assert_close_rows(orows, drows, 1e-11, "particles after fused steps")
+    r = inst.fetch()
+    ref = o.compute_props(mode=2)
+    assert np.array_equal(r["np"][:, 0], ref["np"][0])
+    assert_close_rows(r["T"][:, 0:1], ref["T"][0].reshape(-1, 1), 1e-11, "T")
+    a = avg.fetch()
+    assert_close_rows(a["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T")
+    assert_close_rows(a["v"][:, :, 0].T, ref_avg[2:5].T, 1e-11, "averaged v")
+    assert_close_rows(a["np"][:, 0:1], ref_avg[0].reshape(-1, 1), 1e-14, "averaged np")
+    cf = dom.collision_factors(0, 0)
+    smax, cnt = o.cf_get(0, 0)
+    assert np.array_equal(cf["n_coll_performed"], cnt[:, 3])
+    assert dom.counters()["accepted"] == np.int64(0) + dom.counters()["accepted"]  # counters readable
+
+
+def test_fused_0d_two_species_matches_reference_loop(ctx, orc):
+    """README.md:91-106 / test_2species.jl:52-66: ntc! for (Ar,Ar), (He,Ar),
+    (He,He) then compute_props! every step, on 8 independent 0-D cells."""
+    sp = species(["Ar", "He"])
+    inter = interactions(sp)
+    n_cells, steps = 8, 5
+    rng = np.random.default_rng(5)
+    counts = [rng.integers(50, 400, n_cells), rng.integers(200, 900, n_cells)]
+    Fnum = 5e12
+    o = orc.Oracle(n_cells, 2, [s.mass for s in sp])
+    t = mz.VHS
+    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    dom = mz.Domain(ctx, n_cells, sp, 8000, interactions=inter, seed=8)
+    for s, T0 in enumerate((3000.0, 360.0)):
+        o.pv_create(s, 8000)
+        for c in range(n_cells):
+            o.sample_equal_weight(s, c + 1, int(counts[s][c]), T0, Fnum, seed=8, step=0)
+        dom.sample_cells(s, counts[s], T0, Fnum, step=0)
+    o.estimate_sigma_g_w_max([3000.0, 360.0], Fnum)
+    for s1 in range(2):
+        for s2 in range(2):
+            smax, _ = o.cf_get(s1, s2)
+            dom.set_sigma_g_w_max(s1, s2, smax)
+    dt = 2.5e-3
+    for tt in range(1, steps + 1):
+        for s2 in range(2):
+            for s1 in range(s2, 2):
+                o.ntc_cells(s1, s2, dt, None, 8, tt, equal_weight=False)
+    plan = mz._lib.StepPlan()
+    plan.dims = 0
+    plan.collide = 1
+    plan.equal_weight = 1
+    plan.props = 1
+    plan.dt = dt
+    plan.use_graph = 1
+    inst = mz.PhysProps(dom)
+    dom.step(plan, steps, inst)
+    for s in range(2):
+        orows, oc = oracle_logical(o, s)
+        drows, dc = device_logical(dom, s)
+        assert np.array_equal(oc, dc)
+        assert_close_rows(orows, drows, 1e-11, f"species {s}")
+    r = inst.fetch()
+    ref = o.compute_props(mode=0)
+    assert_close_rows(r["T"].T.reshape(-1, 1), ref["T"].reshape(-1, 1), 1e-11, "T")
+    for s1, s2 in [(0, 0), (1, 0), (1, 1)]:
+        cf = dom.collision_factors(s1, s2)
+        _, cnt = o.cf_get(s1, s2)
+        assert np.array_equal(cf["n_coll_performed"], cnt[:, 3])
+
+
+def test_fused_equals_standalone_ops_bitwise(ctx, orc):
+    """The fused kernel and the standalone kernels run the same per-cell
+    routines: identical particle state after the same steps."""
+    sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc, nx=50, ppc=100, seed=23)
+    _, _, _, _, o2, dom2, _ = couette_setup(ctx, orc, nx=50, ppc=100, seed=23)
+    steps = 4
+    dom.step(couette_plan(grid, walls, dt, props=False), steps)
+    for t in range(1, steps + 1):
+        dom2.ntc(0, 0, dt, t, equal_weight=True)
+        dom2.convect(0, grid, walls, dt, t)
+        dom2.sort(0, grid)
+    a, ca = device_logical(dom, 0)
+    b, cb = device_logical(dom2, 0)
+    assert np.array_equal(ca, cb)
+    assert np.array_equal(a, b)
