@@ -48,6 +48,10 @@ def parse():
     return p.parse_args()
 
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -258,7 +262,7 @@ def run_reference(args):
                    "d2h_bytes_per_step": 0},
            "note": "reference Julia path unavailable here (no Julia toolchain); timed: the oracle's C++ "
                    "restatement of the reference algorithm on the host cores"}
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
 
 
 def run_gpu(args):
@@ -269,17 +273,22 @@ def run_gpu(args):
     from merzgpu import build as b
 
     b.build()
+    log("library ready")
     barrier = Barrier(world)
     ctx = mz.Context(local)
     seed = args.seed + 7919 * rank  # independent replicas
     sp, inter, grid, Fnum, walls, dt, dom, smax = setup_device(mz, ctx, args, seed)
+    log("domain created")
     dom.sample_grid_ndens(0, grid, NDENS, T_WALL, Fnum, step=0)
     n = dom.info(0)["n_total"]
+    log(f"sampled {n} particles")
     inst = mz.PhysProps(dom)
     avg = mz.PhysProps(dom)
     K, W = args.steps, args.warmup
     # warm-up
     dom.step(make_plan(mz, grid, walls, dt, 0, K), W, inst, avg)
+    ctx.synchronize()
+    log("warm-up done")
     mz.clear_props(avg)
     dom.counters(reset=True)
     plan = make_plan(mz, grid, walls, dt, W, K)
@@ -294,6 +303,7 @@ def run_gpu(args):
     ctx.synchronize()
     barrier()
     launches = ctx.launch_count() - launches0
+    log(f"timed {K} steps: {ms:.3f} ms")
     clk = clocks.stop()
     cnt = dom.counters(reset=True)
     t_max = barrier.max(ms / 1e3)
@@ -303,6 +313,7 @@ def run_gpu(args):
     cand = barrier.sum(float(cnt["candidates"])) / t_max
 
     # per-kernel CUDA-event timing (direct launches, same stream) for the roofline
+    log("kernel timing pass")
     ctx.set_kernel_timing(True)
     kt_steps = max(3, min(K, 6))
     dom.step(make_plan(mz, grid, walls, dt, W + K, kt_steps, graph=False), kt_steps, inst, avg)
@@ -329,6 +340,7 @@ def run_gpu(args):
     # plain form: the reference's call granularity -- one ntc launch per cell,
     # then convect, sort and props as separate calls
     plain = None
+    log("roofline: " + json.dumps({k: (v if not isinstance(v, dict) else None) for k, v in roofline.items()}))
     if not args.no_plain and rank == 0:
         rng = mz.PhiloxRNG(seed, W + K + kt_steps)
         pp = mz.PhysProps(dom)
@@ -351,6 +363,7 @@ def run_gpu(args):
     # end to end through the C ABI with host buffers: upload the initial state,
     # K steps, read the cell properties back every step
     e2e = None
+    log(f"plain: {plain}")
     if not args.no_e2e:
         w, v, x, cell = dom.download(0)
         w, v, x = np.ascontiguousarray(w), np.ascontiguousarray(v), np.ascontiguousarray(x)
@@ -374,6 +387,7 @@ def run_gpu(args):
                        "cell properties (np, n, v, T) read back after every step"}
 
     cpu = None
+    log(f"e2e: {e2e}")
     if not args.no_cpu_baseline and rank == 0:
         r = cpu_oracle_run(args, 20, time_budget=15.0)
         cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -387,12 +401,14 @@ def run_gpu(args):
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
                "plain": plain}
-        print(json.dumps(out))
-    dom.close()
+        print(json.dumps(out), flush=True)
     ctx.close()
 
 
 def main():
+    import faulthandler
+
+    faulthandler.enable()
     args = parse()
     if args.impl == "reference":
         run_reference(args)

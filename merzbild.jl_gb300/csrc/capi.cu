@@ -365,11 +365,23 @@ int mz_domain_create(mz_ctx* c, int64_t n_cells, int32_t n_species, const int64_
     API_CATCH(c)
 }
 
+static void free_props(mz_props* p)
+{
+    cudaFree(p->np);
+    cudaFree(p->n);
+    cudaFree(p->v);
+    cudaFree(p->T);
+    cudaFree(p->moments);
+    delete p;
+}
+
 int mz_domain_destroy(mz_domain* d)
 {
     if (!d) return MZ_OK;
     cudaSetDevice(d->ctx->device);
     cudaStreamSynchronize(d->ctx->stream);
+    for (mz_props* p : d->props) free_props(p);
+    d->props.clear();
     for (int s = 0; s < d->ns; ++s) {
         free_species(d->sp[s]);
         cudaFree(d->sp[s].counts);
@@ -696,6 +708,7 @@ int mz_props_create(mz_domain* d, int32_t n_moments, const int32_t* powers, doub
     MZ_CK(cudaMalloc(&p->v, 3 * m * sizeof(double)));
     MZ_CK(cudaMalloc(&p->T, m * sizeof(double)));
     MZ_CK(cudaMalloc(&p->moments, std::max<size_t>(1, n_moments * m) * sizeof(double)));
+    d->props.push_back(p);
     *out = p;
     int r = mz_clear_props(p);
     p = nullptr;
@@ -706,14 +719,11 @@ int mz_props_create(mz_domain* d, int32_t n_moments, const int32_t* powers, doub
 int mz_props_destroy(mz_props* p)
 {
     if (!p) return MZ_OK;
-    cudaSetDevice(p->dom->ctx->device);
-    cudaStreamSynchronize(p->dom->ctx->stream);
-    cudaFree(p->np);
-    cudaFree(p->n);
-    cudaFree(p->v);
-    cudaFree(p->T);
-    cudaFree(p->moments);
-    delete p;
+    mz_domain* d = p->dom;
+    cudaSetDevice(d->ctx->device);
+    cudaStreamSynchronize(d->ctx->stream);
+    d->props.erase(std::remove(d->props.begin(), d->props.end(), p), d->props.end());
+    free_props(p);
     return MZ_OK;
 }
 

@@ -93,6 +93,8 @@ struct mz_domain_s {
     // octree scratch (allocated on demand)
     void* d_merge_scratch = nullptr;
     size_t merge_scratch_bytes = 0;
+    // property sets created on this domain (freed with it)
+    std::vector<mz_props*> props;
     // fused step: RNG step index and last-block counter
     uint32_t* d_step = nullptr;
     unsigned int* d_done = nullptr;

@@ -16,6 +16,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import tomllib
+import weakref
 from dataclasses import dataclass
 from fractions import Fraction
 
@@ -211,12 +212,17 @@ class PhiloxRNG:
 
 # --------------------------------------------------------------------- device objects
 class Context:
+    """One device and one CUDA stream.  Closing it closes its domains first."""
+
     def __init__(self, device=0):
         self.h = C.c_void_p()
+        self._children = weakref.WeakSet()
         check(lib().mz_ctx_create(device, C.byref(self.h)))
 
     def close(self):
         if self.h:
+            for child in list(self._children):
+                child.close()
             lib().mz_ctx_destroy(self.h)
             self.h = C.c_void_p()
 
@@ -267,6 +273,7 @@ class Domain:
 
     def __init__(self, ctx: Context, n_cells, species_data, capacity, interactions=None, seed=1234):
         self.ctx = ctx
+        self._children = weakref.WeakSet()
         self.n_cells = int(n_cells)
         self.species_data = list(species_data)
         self.n_species = len(self.species_data)
@@ -274,6 +281,7 @@ class Domain:
         self.h = C.c_void_p()
         check(lib().mz_domain_create(ctx.h, self.n_cells, self.n_species, ptr(cap, C.c_int64), C.byref(self.h)),
               ctx.h)
+        ctx._children.add(self)
         m = f64([s.mass for s in self.species_data])
         self._ck(lib().mz_set_species(self.h, ptr(m)))
         if interactions is not None:
@@ -284,8 +292,12 @@ class Domain:
         check(rc, self.ctx.h)
 
     def close(self):
+        """Destroy the device state; property sets of this domain close first."""
         if self.h:
-            lib().mz_domain_destroy(self.h)
+            for child in list(self._children):
+                child.close()
+            if self.ctx.h:
+                lib().mz_domain_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):
@@ -462,12 +474,14 @@ class PhysProps:
         self.h = C.c_void_p()
         domain._ck(lib().mz_props_create(domain.h, len(p), ptr(p, C.c_int32) if len(p) else None, float(Tref),
                                          1 if ndens_not_Np else 0, C.byref(self.h)))
+        domain._children.add(self)
         self.ndens_not_Np = ndens_not_Np
         self.Tref = Tref
 
     def close(self):
         if self.h:
-            lib().mz_props_destroy(self.h)
+            if self.domain.h:
+                lib().mz_props_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

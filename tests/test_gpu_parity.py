@@ -361,3 +361,17 @@ def test_couette_steps_vs_oracle(ctx, orc):
     ref = o.compute_props(mode=2)
     assert np.array_equal(r["np"].T, ref["np"])
     assert_close_rows(r["T"].T.reshape(-1, 1), ref["T"].reshape(-1, 1), 1e-11, "T")
+
+
+def test_close_order_is_safe(ctx):
+    """Closing a context closes its domains and their property sets first;
+    later finalizers are no-ops (no use after free)."""
+    c2 = mz.Context(0)
+    sp = species(["Ar"])
+    dom = mz.Domain(c2, 4, sp, 16)
+    p = mz.PhysProps(dom)
+    q = mz.PhysProps(dom)
+    q.close()
+    c2.close()
+    assert not dom.h and not p.h
+    del p, dom
