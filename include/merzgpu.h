@@ -256,6 +256,30 @@ int mz_step(mz_domain* dom, const mz_step_plan* plan, int64_t n_steps, mz_props*
 /* ---------------------------------------------------------------- counters */
 int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
 
+/* ---------------------------------------------------------------- no-allocation sort */
+/* Largest n_cells mz_sort_keys_noalloc accepts.  Its scratch (per-cell counts
+ * and cursors, 2 * 4 B per cell, 2 MiB) is a static device array that every
+ * GPU loading the library holds until the process exits. */
+#define MZ_NOALLOC_MAX_CELLS 262144
+
+/* No counterpart in the reference.  The stable counting sort of n cell keys
+ * (the permutation part of sort_particles!), for callers that must not
+ * allocate device memory: a process whose device memory is owned by another
+ * framework's caching allocator, or a loop that must not take the device-wide
+ * synchronisation of cudaMalloc / cudaFree.  Everything is the caller's and in
+ * device memory: d_keys[n] in [0, n_cells) (out-of-range keys are clamped and
+ * reported as MZ_E_STATE), d_perm[n] receives for every sorted position the
+ * index of the key that lands there (stable: equal keys keep their order),
+ * d_cell_start[n_cells + 1] the exclusive prefix of the per-cell counts.
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it
+ * before returning.  Allocates nothing: the per-cell counters live in a
+ * static device array shared by every call, cleared at the start of each
+ * call; calls that overlap on the GPU race on it, so serialise them.  The
+ * first call on a device looks up that array's device address (with the
+ * device current); make that first call before any stream capture. */
+int mz_sort_keys_noalloc(void* stream, const int32_t* d_keys, int64_t n, int32_t n_cells, int32_t* d_perm,
+                         int32_t* d_cell_start);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,7 +103,9 @@ _SIGS = {
     "mz_sample_grid_ndens": (i32, [vp, i32, P(Grid1D), d, d, d, u64]),
     "mz_step": (i32, [vp, P(StepPlan), i64, vp, vp]),
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
+    "mz_sort_keys_noalloc": (i32, [vp, vp, i64, i32, vp, vp]),
 }
+NOALLOC_MAX_CELLS = 262144
 
 _lib = None
 
