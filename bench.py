@@ -35,7 +35,7 @@ ALG_BYTES = 112  # per particle-step: every particle read once and written once 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="merzgpu", choices=["merzgpu", "reference"])
     p.add_argument("--cells", type=int, default=50000)

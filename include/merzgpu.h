@@ -256,6 +256,13 @@ int mz_step(mz_domain* dom, const mz_step_plan* plan, int64_t n_steps, mz_props*
 /* ---------------------------------------------------------------- counters */
 int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
 
+/* ---------------------------------------------------------------- diagnostics */
+/* No counterpart in the reference.  Evaluates, on the device, the sine and
+ * cosine the collision kernels use for the scattering angle phi = 2 pi rand():
+ * s[i], c[i] = sin, cos of 2 pi m[i] 2^-52 for 52-bit integers m[i] (the
+ * uniform draw's mantissa).  Host arrays of n elements; for accuracy tests. */
+int mz_sincos_2pi(mz_ctx* ctx, int64_t n, const uint64_t* m, double* s, double* c);
+
 /* ---------------------------------------------------------------- no-allocation sort */
 /* Largest n_cells mz_sort_keys_noalloc accepts.  Its scratch (per-cell counts
  * and cursors, 2 * 4 B per cell, 2 MiB) is a static device array that every

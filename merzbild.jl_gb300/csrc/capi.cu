@@ -120,6 +120,7 @@ mz::DomainView make_view(mz_domain* d)
     v.cell_rid = d->d_cell_rid;
     v.cell_step = d->d_cell_step;
     v.cf = d->d_cf;
+    v.trig = d->ctx->d_trig;
     v.status = d->d_status;
     v.counters = d->d_counters;
     v.seed = d->seed;
@@ -210,6 +211,21 @@ int mz_ctx_create(int device, mz_ctx** out)
     MZ_CK(cudaEventCreate(&c->t0));
     MZ_CK(cudaEventCreate(&c->t1));
     MZ_CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    {
+        // {sin, cos} at the sector centres 2 pi (i + 1/2) / TRIG_SECTORS in
+        // extended precision, split into leading and trailing doubles
+        std::vector<double2> tab(2 * mz::TRIG_SECTORS);
+        const long double pi = acosl(-1.0L);
+        for (int i = 0; i < mz::TRIG_SECTORS; ++i) {
+            const long double a = 2.0L * pi * ((long double)i + 0.5L) / (long double)mz::TRIG_SECTORS;
+            const long double sa = sinl(a), ca = cosl(a);
+            const double sh = (double)sa, ch = (double)ca;
+            tab[2 * i] = make_double2(sh, ch);
+            tab[2 * i + 1] = make_double2((double)(sa - (long double)sh), (double)(ca - (long double)ch));
+        }
+        MZ_CK(cudaMalloc(&c->d_trig, tab.size() * sizeof(double2)));
+        MZ_CK(cudaMemcpy(c->d_trig, tab.data(), tab.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    }
     *out = c;
     API_CATCH(c)
 }
@@ -228,6 +244,7 @@ int mz_ctx_destroy(mz_ctx* c)
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->flush_buf) cudaFree(c->flush_buf);
+    if (c->d_trig) cudaFree(c->d_trig);
     cudaStreamDestroy(c->stream);
     delete c;
     return MZ_OK;
@@ -359,6 +376,7 @@ int mz_domain_create(mz_ctx* c, int64_t n_cells, int32_t n_species, const int64_
     MZ_CK(cudaMalloc(&d->d_status, sizeof(int)));
     MZ_CK(cudaMemset(d->d_status, 0, sizeof(int)));
     MZ_CK(cudaMalloc(&d->d_scalar, 8 * sizeof(int64_t)));
+    MZ_CK(cudaMalloc(&d->d_tile_sums, (scan_tiles(n_cells) + 1) * sizeof(int64_t)));
     MZ_CK(cudaMallocHost(&d->h_scalar, 8 * sizeof(int64_t)));
     *out = d;
     d = nullptr;
@@ -397,6 +415,7 @@ int mz_domain_destroy(mz_domain* d)
     cudaFree(d->d_counters);
     cudaFree(d->d_status);
     cudaFree(d->d_scalar);
+    cudaFree(d->d_tile_sums);
     cudaFree(d->d_merge_scratch);
     cudaFree(d->d_step);
     cudaFree(d->d_done);
@@ -892,3 +911,39 @@ int mz_get_counters(mz_domain* d, mz_counters* out, int32_t reset)
 }
 
 }  // extern "C"
+
+namespace {
+__global__ void k_sincos_2pi(const double2* tab, int64_t n, const uint64_t* m, double* s, double* c)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a, b;
+        mz::sincos_2pi_u52(tab, m[i] & 0xFFFFFFFFFFFFFull, a, b);
+        s[i] = a;
+        c[i] = b;
+    }
+}
+}  // namespace
+
+int mz_sincos_2pi(mz_ctx* c, int64_t n, const uint64_t* m, double* s, double* co)
+{
+    struct DevBuf {
+        void* p = nullptr;
+        ~DevBuf() { if (p) cudaFree(p); }
+    };
+    API_TRY
+    MZ_REQUIRE(c && n >= 0 && (n == 0 || (m && s && co)), "mz_sincos_2pi: bad arguments");
+    if (n == 0) return MZ_OK;
+    MZ_CK(cudaSetDevice(c->device));
+    DevBuf dm, ds;
+    MZ_CK(cudaMalloc(&dm.p, n * sizeof(uint64_t)));
+    MZ_CK(cudaMalloc(&ds.p, 2 * n * sizeof(double)));
+    uint64_t* um = static_cast<uint64_t*>(dm.p);
+    double* out = static_cast<double*>(ds.p);
+    MZ_CK(cudaMemcpyAsync(um, m, n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+    const int blocks = (int)std::min<int64_t>(div_up(n, 256), 4096);
+    MZ_LAUNCH(c, "sincos_2pi", k_sincos_2pi, blocks, 256, 0, c->d_trig, n, um, out, out + n);
+    MZ_CK(cudaMemcpyAsync(s, out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MZ_CK(cudaMemcpyAsync(co, out + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MZ_CK(cudaStreamSynchronize(c->stream));
+    API_CATCH(c)
+}

@@ -56,67 +56,112 @@ struct NtcResult {
     int32_t perf, eqw, nsp1, nsp2;
 };
 
+// Screening of sigma*g*w_max in the FP32 log domain.  The FP64 pipe of GB300
+// runs at ~1/60 of the FP32 rate, and FP64 pow and division dominate a
+// candidate's cost.  log2(s) = log2(C) + log2(w_max) + (1 - omega) log2(g^2) is
+// formed from FP32 approximations; the exact FP64 value is computed only where
+// it can change a decision:
+//   * a candidate whose s may reach the running maximum (it may raise it), and
+//   * an acceptance test U < s / max whose two sides lie within SCREEN_MARGIN.
+// Error budget: every log2 term is kept below LOG_RANGE in magnitude (terms
+// beyond it take the exact path), so each of the <= 7 FP32 additions and
+// products rounds by at most 2^-14, and each approximate log2 errs by < 1e-6;
+// the total stays below 5e-4 < SCREEN_MARGIN.  Every decision taken on the
+// screened value is therefore the decision of the all-FP64 loop, and so is
+// the running maximum (screened candidates lie strictly below it).
+// Weights are positive, so max(w_i, w_k) may compare bit patterns.
+constexpr float SCREEN_MARGIN = 1e-3f;                    // log2 units
+constexpr float LOG_RANGE = 128.0f;                       // |log2| bound of a screened term
+constexpr uint64_t G2_TINY_BITS = 0x3990000000000000ull;  // bits of 4 eps^2 = 2^-102
+
+__device__ __forceinline__ double dmax_pos(double a, double b)
+{   // max of two positive doubles through their bit patterns
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x > y ? x : y);
+}
+
+// Bit pattern of sigma*g*w for the running-maximum scan: positive doubles
+// order like their bit patterns; "no value" and NaN (which never raise the
+// maximum: `smax < s` is false) map to -1.
+__device__ __forceinline__ long long max_key(double s, bool present)
+{
+    const long long k = __double_as_longlong(s);
+    return (present && k <= 0x7FF0000000000000ll) ? k : -1ll;
+}
+
 // The candidate loop of ntc! / ntc_equal_weight! for one cell, executed by
-// one warp (all 32 lanes call it with identical arguments).
+// one group of G lanes (all G lanes call it with identical arguments; a warp
+// holds 32 / G groups, each on its own cell).
 //   P1, P2: particle columns of the two species (same for single species)
 //   p1, p2: the cell's indexers; grown in place by splits
 //   cell1/key1, cell2/key2: slot-owner arrays, written for split particles
 //   b1/b2: first reserved slot for split particles of species 1/2
-// Candidates are evaluated in conflict-free batches of up to 32 (see ntc.cu).
-template <bool EQW>
+// Candidates are evaluated in conflict-free batches of up to G (see ntc.cu).
+// A warp instruction serves every group, so with G = 8 one FP64 instruction
+// covers the candidates of four cells instead of the ~12 conflict-free
+// candidates one cell offers.
+template <bool EQW, int G>
 __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interaction& I, bool single, int c,
                                               int32_t ncoll, double smax, const Cols& P1, const Cols& P2,
                                               Indexer& p1, Indexer& p2, int32_t* cell1, int32_t* key1,
                                               int32_t* cell2, int32_t* key2, int32_t b1, int32_t b2, double dw_tol,
                                               uint64_t seed, uint32_t pc, uint32_t stp, uint32_t rid)
 {
-    const int lane = threadIdx.x & 31;
+    const WarpGroup<G> grp;
+    const int gl = grp.rank;
     const double vexp = fma(-2.0, I.vhs_o, 1.0);  // sigma_vhs exponent, collision_cross_sections.jl:179-181
+    const float lC = I.vhs_factor > 0.0 ? log2_pos(I.vhs_factor) : 1e30f;
+    const bool screen = fabsf(lC) < LOG_RANGE;
+    const float ex = 1.0f - (float)I.vhs_o;       // s = C w_max (g^2)^(1 - omega)
     NtcResult R;
     R.perf = 0;
     R.eqw = 0;
     R.nsp1 = 0;
     R.nsp2 = 0;
     for (int32_t j0 = 0; j0 < ncoll;) {
-        const int32_t j = j0 + lane;
+        const int32_t j = j0 + gl;
         const bool valid = j < ncoll;
         Stream st;
         st.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)j);
         int32_t i = -1, k = -2;
         if (valid) {
+            // i, k = floor(rand() * n_local) (collision_ntc.jl:358-363)
             const int32_t nl1 = p1.n1 + p1.n2;
             const int32_t nl2 = single ? nl1 : p2.n1 + p2.n2;
-            i = (int32_t)floor(st.uniform() * (double)nl1);
-            k = (int32_t)floor(st.uniform() * (double)nl2);
+            i = floor_u52_times(st.u52(), nl1);
+            k = floor_u52_times(st.u52(), nl2);
             if (single) {
                 int guard = 0;
-                while (i == k && guard++ < (1 << 20)) k = (int32_t)floor(st.uniform() * (double)nl1);
+                while (i == k && guard++ < (1 << 20)) k = floor_u52_times(st.u52(), nl1);
             }
         }
         // the batch ends before the first candidate that touches a particle
         // of an earlier candidate in the batch
         bool conflict = false;
-#pragma unroll 8
-        for (int src = 0; src < 31; ++src) {
-            const int32_t ii = __shfl_sync(0xFFFFFFFFu, i, src);
-            const int32_t kk = __shfl_sync(0xFFFFFFFFu, k, src);
-            if (src < lane) {
+#pragma unroll
+        for (int src = 0; src < G - 1; ++src) {
+            const int32_t ii = grp.shfl(i, src);
+            const int32_t kk = grp.shfl(k, src);
+            if (src < gl) {
                 if (single)
                     conflict |= (ii == i) | (ii == k) | (kk == i) | (kk == k);
                 else
                     conflict |= (ii == i) | (kk == k);
             }
         }
-        const unsigned cm = __ballot_sync(0xFFFFFFFFu, valid && conflict);
-        const int nvalid = min(32, ncoll - j0);
+        const unsigned cm = grp.ballot(valid && conflict);
+        const int nvalid = min(G, ncoll - j0);
         int B = cm ? min(nvalid, __ffs(cm) - 1) : nvalid;
-        bool act = lane < B;
+        bool act = gl < B;
 
+        const float l_smax = log2_pos(smax);
+        const bool screen_b = screen && fabsf(l_smax) < 2.0f * LOG_RANGE;
         int32_t si = 0, sk = 0;
         PartV a, b;
         a.w = b.w = 0.0;
-        double g = 0.0, sgw = -1.0;
-        bool has = false;
+        double g2 = 0.0, g = 0.0, sgw = -1.0, wmax = 0.0;
+        bool has = false, exact = false, have_g = false;
+        float ls = 0.0f;
         if (act) {
             si = map_slot(p1, i);
             sk = map_slot(p2, k);
@@ -124,31 +169,70 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
             b = load_pv(P2, sk);
             // compute_g! (collision_utils.jl:388-391)
             const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
-            g = sqrt((gx * gx + gy * gy) + gz * gz);
-            has = g > EPS;
-            if (has) sgw = I.vhs_factor * pow(g, vexp) * g * fmax(a.w, b.w);
+            g2 = (gx * gx + gy * gy) + gz * gz;
+            wmax = dmax_pos(a.w, b.w);
+            // g > eps() (collision_ntc.jl:375) is certain unless g^2 <= 4 eps^2
+            if ((uint64_t)__double_as_longlong(g2) > G2_TINY_BITS) {
+                has = true;
+            } else {
+                g = sqrt(g2);
+                have_g = true;
+                has = g > EPS;
+            }
+            if (has) {
+                const float lw = log2_pos(wmax), lg = log2_pos(g2);
+                ls = lC + lw + ex * lg;
+                exact = !screen_b || fabsf(lw) >= LOG_RANGE || fabsf(lg) >= LOG_RANGE ||
+                        ls > l_smax - SCREEN_MARGIN;
+                if (exact) {
+                    if (!have_g) g = sqrt(g2);
+                    have_g = true;
+                    sgw = I.vhs_factor * pow(g, vexp) * g * wmax;  // sigma_vhs(g) * g * max(w_i, w_k)
+                }
+            }
         }
-        // running (sigma g w)_max each candidate is tested against (collision_ntc.jl:229)
-        double m = sgw;
+        // running (sigma g w)_max each candidate is tested against
+        // (collision_ntc.jl:229), as an inclusive max-scan over the batch on
+        // bit patterns; candidates screened out lie below smax
+        long long mk = max_key(sgw, act && exact);
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double t = __shfl_up_sync(0xFFFFFFFFu, m, o);
-            if (lane >= o) m = fmax(m, t);
+        for (int o = 1; o < G; o <<= 1) {
+            const long long t = grp.up(mk, o);
+            if (gl >= o) mk = max(mk, t);
         }
-        m = fmax(m, smax);
+        mk = max(mk, __double_as_longlong(smax));
+        const double m = __longlong_as_double(mk);
         bool acc = false;
-        if (act && has) acc = st.uniform() < sgw / m;  // collision_ntc.jl:231
+        if (act && has) {
+            // rand() < sigma_g_w / (sigma g w)_max (collision_ntc.jl:231)
+            const uint64_t um = st.u52();
+            if (exact) {
+                acc = u52_to_double(um) < sgw / m;
+            } else {
+                const float lm = log2_pos(m);
+                const float dl = ls - lm - log2_u52(um);
+                if (dl > SCREEN_MARGIN && fabsf(lm) < 2.0f * LOG_RANGE) {
+                    acc = true;
+                } else if (dl >= -SCREEN_MARGIN || fabsf(lm) >= 2.0f * LOG_RANGE) {
+                    if (!have_g) g = sqrt(g2);
+                    have_g = true;
+                    const double se = I.vhs_factor * pow(g, vexp) * g * wmax;
+                    acc = u52_to_double(um) < se / m;
+                }
+            }
+        }
         bool spl = false;
         if (!EQW) {
             spl = acc && !(fabs(a.w - b.w) < dw_tol);
-            const unsigned sm = __ballot_sync(0xFFFFFFFFu, spl);
+            const unsigned sm = grp.ballot(spl);
             if (sm) B = min(B, __ffs(sm));  // the batch ends after the first split
         }
-        act = lane < B;
+        act = gl < B;
         acc = acc && act;
         spl = spl && act;
         int side = 0;
         if (acc) {
+            if (!have_g) g = sqrt(g2);
             // compute_com! (collision_utils.jl:374-376)
             const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
             const double cy = I.mu1 * a.vy + I.mu2 * b.vy;
@@ -180,10 +264,10 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
                 ky[ns_] = c;
                 PP.w[src] = wl;
             }
-            // scatter_vhs! (collision_scattering.jl:17-29)
-            const double phi = TWOPI * st.uniform();
+            // scatter_vhs! (collision_scattering.jl:17-29): phi = 2 pi rand(),
+            // cos(theta) = 2 rand() - 1
             double sphi, cphi;
-            sincos(phi, &sphi, &cphi);
+            sincos_2pi_u52(d.trig, st.u52(), sphi, cphi);
             const double ct = fma(2.0, st.uniform(), -1.0);
             const double sth = sqrt(1.0 - ct * ct);
             const double nx = g * (sth * cphi), ny = g * (sth * sphi), nz = g * ct;
@@ -194,15 +278,15 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
             P2.vy[sk] = cy - I.mu1 * ny;
             P2.vz[sk] = cz - I.mu1 * nz;
         }
-        const unsigned am = __ballot_sync(0xFFFFFFFFu, acc);
+        const unsigned am = grp.ballot(acc);
         R.perf += __popc(am);
         if (EQW)
             R.eqw += __popc(am);
         else
-            R.eqw += __popc(__ballot_sync(0xFFFFFFFFu, acc && fabs(a.w - b.w) < dw_tol));
-        smax = __shfl_sync(0xFFFFFFFFu, m, B - 1);
+            R.eqw += __popc(grp.ballot(acc && fabs(a.w - b.w) < dw_tol));
+        smax = __longlong_as_double(grp.shfl(mk, B - 1));
         if (!EQW) {
-            const int sd = __shfl_sync(0xFFFFFFFFu, side, B - 1);
+            const int sd = grp.shfl(side, B - 1);
             if (sd == 1 || (sd == 2 && single)) {
                 if (p1.n2 == 0) p1.start2 = b1;
                 p1.n2 += 1;
@@ -214,7 +298,7 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
                 R.nsp2 += 1;
             }
         }
-        __syncwarp();
+        grp.sync();
         j0 += B;
     }
     R.smax = smax;
@@ -267,6 +351,7 @@ __device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& 
 // ------------------------------------------------------------------ convection
 struct WallView {
     double L, min_x, max_x, inv_dx;
+    long long bits_L, bits_min, bits_max;  // bit patterns of L, min_x, max_x (positive doubles order like integers)
     double vsq[2][MZ_MAX_SPECIES];
     double wv[2][3];
     double acc[2];
@@ -335,12 +420,31 @@ __device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int 
 // get_cell (grid_uniform1D.jl:97-99), 0-based, clamped with a status flag
 __device__ __forceinline__ int32_t cell_of(const DomainView& d, double x, double inv_dx)
 {
-    double f = floor(x * inv_dx);
-    if (!(f >= 0.0 && f < (double)d.n_cells)) {
+    int32_t k = __double2int_rd(x * inv_dx);
+    if (k < 0 || k >= d.n_cells) {
         set_status(d, ST_OUTSIDE_GRID);
-        f = (f < 0.0 || f != f) ? 0.0 : (double)(d.n_cells - 1);
+        k = k < 0 ? 0 : d.n_cells - 1;
     }
-    return (int32_t)f;
+    return k;
+}
+
+// x + vx*dt for a particle that stays inside (0, L): the clamp of
+// convect_single_particle! (convection_1D.jl:44-46).  Returns false when the
+// new position hits a wall: x_new >= L or x_new <= 0 (the comparisons are made
+// on the bit patterns, where doubles of one sign order like integers).
+__device__ __forceinline__ bool move_free(const WallView& W, double xn, double& x)
+{
+    const long long b = __double_as_longlong(xn);
+    if (b <= 0 || b >= W.bits_L) return false;
+    x = b < W.bits_min ? W.min_x : (b > W.bits_max ? W.max_x : xn);
+    return true;
+}
+
+__host__ inline void wall_bits(WallView& W)
+{
+    memcpy(&W.bits_L, &W.L, 8);
+    memcpy(&W.bits_min, &W.min_x, 8);
+    memcpy(&W.bits_max, &W.max_x, 8);
 }
 
 }  // namespace mz

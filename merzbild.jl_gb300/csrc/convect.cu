@@ -34,14 +34,12 @@ __global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw
         double x = S.A.x[slot];
         double vx = S.A.vx[slot];
         const double xn = fma(vx, dt, x);
-        if ((xn >= W.L) || (xn <= 0.0)) {
+        if (!move_free(W, xn, x)) {
             double vy = S.A.vy[slot], vz = S.A.vz[slot];
             my_hits += convect_walls(st, W, s, x, vx, vy, vz, dt, cap);
             S.A.vx[slot] = vx;
             S.A.vy[slot] = vy;
             S.A.vz[slot] = vz;
-        } else {
-            x = fmin(fmax(xn, W.min_x), W.max_x);
         }
         S.A.x[slot] = x;
         if (compute_cell) S.key[slot] = cell_of(d, x, W.inv_dx);
@@ -63,6 +61,7 @@ void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w
     W.min_x = g->min_x;
     W.max_x = g->max_x;
     W.inv_dx = g->inv_dx;
+    wall_bits(W);
     for (int b = 0; b < 2; ++b) {
         for (int q = 0; q < MZ_MAX_SPECIES; ++q) W.vsq[b][q] = w->reflection_v_sq[b][q];
         W.acc[b] = w->accommodation[b];

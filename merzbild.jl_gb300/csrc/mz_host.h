@@ -48,6 +48,7 @@ struct mz_ctx_s {
     std::vector<cudaEvent_t> event_pool;
     int64_t launches = 0;
     int num_sms = 0;
+    double2* d_trig = nullptr;  // sector table of sincos_2pi_u52 (2 x TRIG_SECTORS)
 
     cudaEvent_t get_event();
     // bracket a launch with events when kernel timing is on; returns slot or -1
@@ -88,6 +89,7 @@ struct mz_domain_s {
     mz::Counters* d_counters = nullptr;
     int* d_status = nullptr;
     int64_t* d_scalar = nullptr;   // small device scratch (totals)
+    int64_t* d_tile_sums = nullptr;  // per-tile totals of the cell scans
     int64_t* h_scalar = nullptr;   // pinned mirror
     uint64_t seed = 1234;
     // octree scratch (allocated on demand)
@@ -125,8 +127,12 @@ int64_t div_up(int64_t a, int64_t b);
 // launchers (one per translation unit)
 void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index);
 void launch_compact(mz_domain* d, int s);
+// exclusive scan of per-cell counts (or of n1 + n2 of nlocal_from): cell
+// starts into base_out and/or a fresh group-1 indexer (write_indexer, which
+// also zeroes fill and counts), the total into total_out
 void launch_scan_cells(mz_domain* d, int32_t* counts, mz::Indexer* ind, int32_t* fill, int64_t* total_out,
-                       bool write_indexer, int32_t* base_out, int64_t base_offset);
+                       bool write_indexer, int32_t* base_out, int64_t base_offset,
+                       const mz::Indexer* nlocal_from = nullptr);
 void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce, uint64_t step, int32_t flags,
                 double dw_tol);
 void launch_props(mz_domain* d, mz_props* p, int32_t mode);
@@ -143,6 +149,20 @@ void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v);
 void reserve_species(mz_domain* d, int s, int64_t cap);
 void launch_key_from_cell(mz_domain* d, int s);
 void launch_avg(mz_ctx* c, double* avg, const double* inst, int64_t n, double inv);
+
+// Lanes per cell in the NTC kernels.  A conflict-free batch of a cell with n
+// particles holds about sqrt(pi n / 8) candidates (12 at n = 400), and one warp
+// instruction serves all of a warp's groups, so 8-lane groups (four cells per
+// warp) use the FP64 pipe best; with few cells, wider groups shorten the
+// sequential chain of each cell instead.
+// cells per tile of the two-pass cell scan (sort.cu)
+#define MZ_SCAN_TILE 2048
+inline int64_t scan_tiles(int64_t cells) { return (cells + MZ_SCAN_TILE - 1) / MZ_SCAN_TILE; }
+
+inline int ntc_group_width(int64_t cells)
+{
+    return cells >= 4096 ? 8 : (cells >= 1024 ? 16 : 32);
+}
 
 #define MZ_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                                           \
     do {                                                                                               \

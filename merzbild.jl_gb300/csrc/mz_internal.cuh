@@ -97,6 +97,8 @@ struct Stream {
         ++n;
         return (uint64_t)buf[2 * e] | ((uint64_t)buf[2 * e + 1] << 32);
     }
+    // the 52-bit integer m of the next uniform U = m * 2^-52
+    __host__ __device__ inline uint64_t u52() { return bits() >> 12; }
     // uniform in [0, 1), multiples of 2^-52: [1, 2) - 1 like Julia's rand(Float64)
     __host__ __device__ inline double uniform()
     {
@@ -110,6 +112,45 @@ struct Stream {
 #endif
     }
 };
+
+// U = m * 2^-52 as a double (exact)
+__device__ __forceinline__ double u52_to_double(uint64_t m)
+{
+    return __longlong_as_double((long long)(0x3FF0000000000000ull | m)) - 1.0;
+}
+
+// floor(U * n) for U = m * 2^-52 with the FP64 product's rounding, computed in
+// integer arithmetic: the exact product m * n / 2^52 splits into an integer
+// part and a 64-bit fraction.  The rounded FP64 product can only differ from
+// the exact floor when the fraction lies within half an ulp of the next
+// integer (for n < 2^31 half an ulp is at most 2^-23); only then is the FP64
+// formula evaluated.
+__device__ __forceinline__ int32_t floor_u52_times(uint64_t m, int32_t n)
+{
+    const uint64_t a = m << 12;  // U * 2^64
+    const uint64_t hi = __umul64hi(a, (uint64_t)n);
+    const uint64_t lo = a * (uint64_t)n;
+    if (lo >= 0xFFFFFE0000000000ull) return (int32_t)floor(u52_to_double(m) * (double)n);
+    return (int32_t)hi;
+}
+
+// approximate log2 of a positive normal double (FP32 accuracy, no FP64 pipe)
+__device__ __forceinline__ float log2_pos(double x)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023;
+    const float mf = __int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF));
+    return (float)e + __log2f(mf);
+}
+
+// approximate log2(m * 2^-52) for a 52-bit integer m (U == 0 -> -1e30)
+__device__ __forceinline__ float log2_u52(uint64_t m)
+{
+    if (m == 0) return -1e30f;
+    const int lz = __clzll((long long)m);
+    const uint32_t top = lz == 63 ? 0u : (uint32_t)((m << (lz + 1)) >> 41);  // 23 bits after the leading one
+    return (float)(63 - lz - 52) + __log2f(__int_as_float(0x3F800000 | (int)top));
+}
 
 // ------------------------------------------------------------------ data
 struct Interaction {  // Interaction, collision_utils.jl:73-82
@@ -156,6 +197,7 @@ struct DomainView {
     const uint32_t* cell_rid;  // per-cell RNG id, nullptr = cell index
     const uint32_t* cell_step; // per-cell step offset, nullptr = 0
     CollisionFactors* cf;      // [(s1 + ns * s2) * n_cells + cell]
+    const double2* trig;       // sector table of sincos_2pi_u52
     int* status;               // device status word (ST_* bits)
     Counters* counters;
     uint64_t seed;
@@ -204,6 +246,30 @@ __device__ inline double warp_sum(double v)
     return v;
 }
 
+// G consecutive lanes of a warp acting as one unit (G = 8, 16 or 32); the
+// masks let groups of one warp run loops of different lengths.
+template <int G>
+struct WarpGroup {
+    static_assert(G == 8 || G == 16 || G == 32, "group width");
+    int rank;       // lane within the group
+    int base;       // first lane of the group
+    unsigned mask;  // lanes of the group
+    __device__ __forceinline__ WarpGroup()
+    {
+        const int lane = threadIdx.x & 31;
+        rank = lane & (G - 1);
+        base = lane & ~(G - 1);
+        mask = G == 32 ? 0xFFFFFFFFu : (((1u << G) - 1u) << base);
+    }
+    // bit r set when group rank r has p
+    __device__ __forceinline__ unsigned ballot(bool p) const { return __ballot_sync(mask, p) >> base; }
+    template <class T>
+    __device__ __forceinline__ T shfl(T v, int src) const { return __shfl_sync(mask, v, src, G); }
+    template <class T>
+    __device__ __forceinline__ T up(T v, int o) const { return __shfl_up_sync(mask, v, o, G); }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+};
+
 __device__ inline void set_status(const DomainView& d, int bits)
 {
     if (d.status) atomicOr(d.status, bits);
@@ -212,5 +278,38 @@ __device__ inline void set_status(const DomainView& d, int bits)
 constexpr double K_B = 1.380649e-23;           // constants.jl:4
 constexpr double TWOPI = 2.0 * 3.141592653589793;
 constexpr double EPS = 2.220446049250313e-16;  // Julia eps()
+
+// ------------------------------------------------------------------ trig
+// sin and cos of 2 pi m 2^-52 for a 52-bit integer m (the angle 2 pi rand()
+// of the scattering), table-driven (P. T. P. Tang, "Table-driven implementation
+// of the sine and cosine functions", 1990, in its simplest form): the top 8
+// bits of m pick a sector whose centre angle c_i has {sin, cos} tabulated as
+// double-double; the offset d = 2 pi (m - centre) 2^-52, |d| <= pi / 256,
+// enters through
+//   sin d = d - d^3/6 + d^5/120 - d^7/5040      (next term < 2e-23)
+//   cos d - 1 = -d^2/2 + d^4/24 - d^6/720        (next term < 5e-20)
+// and the angle-addition formulas, with the small terms summed before the
+// tabulated leading part so that one rounding of the result dominates.
+// About 16 FP64 operations replace the range reduction and the two long
+// polynomials of a general sincos; the error stays within 1.5 ulp of the exact
+// sine and cosine of 2 pi m 2^-52 (a double-rounded 2 pi U fed to sin/cos
+// already differs from it by up to 4 ulp).
+constexpr int TRIG_SECTORS = 256;
+
+// tab: 2 * TRIG_SECTORS entries, {sin, cos} leading parts at 2 i and
+// trailing parts at 2 i + 1
+__device__ __forceinline__ void sincos_2pi_u52(const double2* tab, uint64_t m, double& s, double& c)
+{
+    const int i = (int)(m >> 44);
+    const long long t = (long long)(m & 0xFFFFFFFFFFFull) - (1ll << 43);
+    const double dl = (double)t * (TWOPI * 0x1p-52);
+    const double d2 = dl * dl;
+    const double sd = fma(dl * d2, fma(d2, fma(d2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), dl);
+    const double cm1 = d2 * fma(d2, fma(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5);
+    const double2 hi = __ldg(tab + 2 * i);
+    const double2 lo = __ldg(tab + 2 * i + 1);
+    s = hi.x + fma(hi.y, sd, fma(hi.x, cm1, lo.x));
+    c = hi.y + fma(-hi.x, sd, fma(hi.y, cm1, lo.y));
+}
 
 }  // namespace mz

@@ -3,10 +3,11 @@
 // collide_2particles_vhs! (:223-270), scatter_vhs! (collision_scattering.jl:17-29)
 // and variable-weight splitting.
 //
-// One warp owns one cell.  The reference's candidate loop is sequential:
-// candidates may share particles and (sigma g w)_max is raised before each
-// acceptance test.  The warp evaluates candidates in batches of up to 32 and
-// keeps the sequential semantics exactly:
+// One group of G lanes (8, 16 or 32; a warp holds 32 / G groups) owns one
+// cell.  The reference's candidate loop is sequential: candidates may share
+// particles and (sigma g w)_max is raised before each acceptance test.  The
+// group evaluates candidates in batches of up to G and keeps the sequential
+// semantics exactly:
 //   * every candidate j draws from its own Philox stream (i, k, retries,
 //     acceptance, scattering angles -- the reference's draw order);
 //   * a batch ends before the first candidate that shares a particle with an
@@ -49,7 +50,7 @@ __global__ void k_ntc_prepare(DomainView d, int s1, int s2, uint32_t pc, int cfi
     }
 }
 
-template <bool EQW>
+template <bool EQW, int G>
 __global__ void __launch_bounds__(256) k_ntc(DomainView d, int s1, int s2, uint32_t pc, int cfi, int cb, int ce,
                                              uint32_t step, double dw_tol, const int32_t* base1,
                                              const int32_t* base2, const int32_t* res1, const int32_t* res2)
@@ -58,9 +59,9 @@ __global__ void __launch_bounds__(256) k_ntc(DomainView d, int s1, int s2, uint3
     const SpeciesView& S2 = d.sp[s2];
     const bool single = (s1 == s2);
     const Interaction I = d.inter[s1 + d.n_species * s2];
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int c = cb + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < ce; c += nwarps) {
+    const WarpGroup<G> grp;
+    const int ngroups = (gridDim.x * blockDim.x) / G;
+    for (int c = cb + (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); c < ce; c += ngroups) {
         CollisionFactors* cfp = &d.cf[(size_t)cfi * d.n_cells + c];
         const int32_t ncoll = cfp->n_coll;
         if (ncoll <= 0) continue;
@@ -68,10 +69,10 @@ __global__ void __launch_bounds__(256) k_ntc(DomainView d, int s1, int s2, uint3
         Indexer p2 = single ? p1 : S2.ind[c];
         const int32_t b1 = EQW ? 0 : base1[c];
         const int32_t b2 = EQW ? 0 : (single ? 0 : base2[c]);
-        const NtcResult R = ntc_cell<EQW>(d, I, single, c, ncoll, cfp->smax, S1.A, S2.A, p1, p2, S1.cell, S1.key,
-                                          S2.cell, S2.key, b1, b2, dw_tol, cell_seed(d, c), pc,
-                                          cell_step(d, c, step), cell_rid(d, c));
-        if (lane == 0) {
+        const NtcResult R = ntc_cell<EQW, G>(d, I, single, c, ncoll, cfp->smax, S1.A, S2.A, p1, p2, S1.cell,
+                                             S1.key, S2.cell, S2.key, b1, b2, dw_tol, cell_seed(d, c), pc,
+                                             cell_step(d, c, step), cell_rid(d, c));
+        if (grp.rank == 0) {
             cfp->smax = R.smax;
             cfp->n_coll_performed = R.perf;
             cfp->n_eq_w_coll_performed = R.eqw;
@@ -87,10 +88,10 @@ __global__ void __launch_bounds__(256) k_ntc(DomainView d, int s1, int s2, uint3
         if (!EQW) {
             // reserved slots not used by splits become dead
             const int32_t r1 = res1[c];
-            for (int32_t q = R.nsp1 + lane; q < r1; q += 32) S1.cell[b1 + q] = -1;
+            for (int32_t q = R.nsp1 + grp.rank; q < r1; q += G) S1.cell[b1 + q] = -1;
             if (!single) {
                 const int32_t r2 = res2[c];
-                for (int32_t q = R.nsp2 + lane; q < r2; q += 32) S2.cell[b2 + q] = -1;
+                for (int32_t q = R.nsp2 + grp.rank; q < r2; q += G) S2.cell[b2 + q] = -1;
             }
         }
     }
@@ -146,16 +147,17 @@ void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce,
         if (!single && B.hw + tot2 > B.capacity) reserve_species(d, s2, B.hw + tot2 + 256);
         v = make_view(d);
     }
-    const int nwarps_needed = (int)std::max<int64_t>(1, ce - cb);
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(nwarps_needed * 32, 256), (int64_t)c->num_sms * 16));
-    if (eqw)
-        MZ_LAUNCH(c, "ntc", k_ntc<true>, blocks, 256, 0, v, s1, s2, pc, cfi, (int)cb, (int)ce, (uint32_t)step, dw_tol,
-                  (const int32_t*)nullptr, (const int32_t*)nullptr, (const int32_t*)nullptr,
-                  (const int32_t*)nullptr);
-    else
-        MZ_LAUNCH(c, "ntc", k_ntc<false>, blocks, 256, 0, v, s1, s2, pc, cfi, (int)cb, (int)ce, (uint32_t)step,
-                  dw_tol, A.work, single ? (const int32_t*)nullptr : B.work, A.fill,
-                  single ? (const int32_t*)nullptr : B.fill);
+    const int G = ntc_group_width(ce - cb);
+    const int64_t groups_needed = std::max<int64_t>(1, ce - cb);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(groups_needed * G, 256), (int64_t)c->num_sms * 16));
+    using KNtc = void (*)(DomainView, int, int, uint32_t, int, int, int, uint32_t, double, const int32_t*,
+                          const int32_t*, const int32_t*, const int32_t*);
+    const KNtc kern = eqw ? (G == 8 ? k_ntc<true, 8> : G == 16 ? k_ntc<true, 16> : k_ntc<true, 32>)
+                          : (G == 8 ? k_ntc<false, 8> : G == 16 ? k_ntc<false, 16> : k_ntc<false, 32>);
+    const int32_t* nul = nullptr;
+    MZ_LAUNCH(c, "ntc", kern, blocks, 256, 0, v, s1, s2, pc, cfi, (int)cb, (int)ce, (uint32_t)step, dw_tol,
+              eqw ? nul : A.work, (eqw || single) ? nul : B.work, eqw ? nul : A.fill,
+              (eqw || single) ? nul : B.fill);
     if (!eqw) {
         MZ_LAUNCH(c, "ntc_split_total", k_split_total, 1, 1024, 0, v, cfi, d->d_scalar + 2);
         MZ_CK(cudaMemcpyAsync(d->h_scalar + 2, d->d_scalar + 2, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));

@@ -62,52 +62,110 @@ __global__ void k_key_from_cell(DomainView d, int s, int64_t hw)
 
 // Single-block exclusive scan over n cells.  Writes the indexer (group 1 only)
 // and zeroes fill/counts when write_indexer, else writes base_out[c].
-__global__ void __launch_bounds__(1024) k_scan(int32_t* counts, int32_t n, Indexer* ind, int32_t* fill,
-                                               int32_t* base_out, int64_t base_offset, int64_t* total_out,
-                                               int write_indexer, const Indexer* nlocal_from)
+// Exclusive scan of per-cell counts in two passes over tiles of SCAN_TILE
+// cells (one block of SCAN_THREADS threads per tile, SCAN_PER_THREAD
+// consecutive cells per thread): k_scan_tiles sums every tile, k_scan_apply
+// adds the sums of the tiles before its own and scans the tile.
+constexpr int SCAN_THREADS = 256, SCAN_PER_THREAD = 8, SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+static_assert(SCAN_TILE == MZ_SCAN_TILE, "tile size");
+
+struct ScanArgs {
+    int32_t* counts;
+    int32_t n;
+    Indexer* ind;
+    int32_t* fill;
+    int32_t* base_out;
+    int64_t base_offset;
+    int64_t* total_out;
+    int write_indexer;
+    const Indexer* nlocal_from;  // counts from n1 + n2 of an indexer instead
+    int64_t* tile_sums;
+};
+
+__device__ __forceinline__ int32_t scan_count(const ScanArgs& a, int c)
 {
-    __shared__ long long warp_tot[32];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int chunk = (n + blockDim.x - 1) / blockDim.x;
-    const int c0 = min(n, t * chunk), c1 = min(n, c0 + chunk);
-    long long local = 0;
-    for (int c = c0; c < c1; ++c) local += nlocal_from ? (nlocal_from[c].n1 + nlocal_from[c].n2) : counts[c];
-    long long incl = local;
+    return a.nlocal_from ? a.nlocal_from[c].n1 + a.nlocal_from[c].n2 : a.counts[c];
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total
+__device__ __forceinline__ long long block_exclusive_scan(long long v, long long& excl)
+{
+    __shared__ long long warp_tot[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += v;
+        const long long u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += u;
     }
     if (lane == 31) warp_tot[w] = incl;
     __syncthreads();
-    if (w == 0) {
-        long long v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
-        long long vi = v;
+    long long before = 0, total = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            long long u = __shfl_up_sync(0xFFFFFFFFu, vi, o);
-            if (lane >= o) vi += u;
-        }
-        warp_tot[lane] = vi - v;  // exclusive prefix of warp totals
-        if (lane == 31 && total_out) *total_out = vi;
+    for (int k = 0; k < SCAN_THREADS / 32; ++k) {
+        const long long t = warp_tot[k];
+        before += k < w ? t : 0;
+        total += t;
     }
+    excl = before + incl - v;
+    return total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(ScanArgs a)
+{
+    const int c0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    long long local = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k)
+        if (c0 + k < a.n) local += scan_count(a, c0 + k);
+    long long excl;
+    const long long total = block_exclusive_scan(local, excl);
+    if (threadIdx.x == 0) a.tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(ScanArgs a)
+{
+    __shared__ long long prefix_sh;
+    // sum of the tiles before this one
+    long long pre = 0;
+    for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) pre += a.tile_sums[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xFFFFFFFFu, pre, o);
+    if (threadIdx.x == 0) prefix_sh = 0;
     __syncthreads();
-    long long run = base_offset + warp_tot[w] + (incl - local);
-    for (int c = c0; c < c1; ++c) {
-        int32_t cnt = nlocal_from ? (nlocal_from[c].n1 + nlocal_from[c].n2) : counts[c];
-        if (write_indexer) {
+    if ((threadIdx.x & 31) == 0 && pre) atomicAdd((unsigned long long*)&prefix_sh, (unsigned long long)pre);
+    __syncthreads();
+    const long long tile_base = a.base_offset + prefix_sh;
+
+    const int c0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int32_t cnt[SCAN_PER_THREAD];
+    long long local = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+        cnt[k] = c0 + k < a.n ? scan_count(a, c0 + k) : 0;
+        local += cnt[k];
+    }
+    long long excl;
+    const long long total = block_exclusive_scan(local, excl);
+    long long run = tile_base + excl;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+        const int c = c0 + k;
+        if (c >= a.n) break;
+        if (a.write_indexer) {
             Indexer p;
             p.start1 = (int32_t)run;
-            p.n1 = cnt;
+            p.n1 = cnt[k];
             p.start2 = 0;
             p.n2 = 0;
-            ind[c] = p;
-            fill[c] = 0;
-            counts[c] = 0;
+            a.ind[c] = p;
+            a.fill[c] = 0;
+            a.counts[c] = 0;
         }
-        if (base_out) base_out[c] = (int32_t)run;
-        run += cnt;
+        if (a.base_out) a.base_out[c] = (int32_t)run;
+        run += cnt[k];
     }
+    if (a.total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *a.total_out = tile_base - a.base_offset + total;
 }
 
 __global__ void k_scatter(DomainView d, int s, int64_t hw)
@@ -181,10 +239,22 @@ void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v)
 }
 
 void launch_scan_cells(mz_domain* d, int32_t* counts, Indexer* ind, int32_t* fill, int64_t* total_out,
-                       bool write_indexer, int32_t* base_out, int64_t base_offset)
+                       bool write_indexer, int32_t* base_out, int64_t base_offset, const Indexer* nlocal_from)
 {
-    MZ_LAUNCH(d->ctx, "scan", k_scan, 1, 1024, 0, counts, (int32_t)d->n_cells, ind, fill, base_out, base_offset,
-              total_out, write_indexer ? 1 : 0, (const Indexer*)nullptr);
+    ScanArgs a;
+    a.counts = counts;
+    a.n = (int32_t)d->n_cells;
+    a.ind = ind;
+    a.fill = fill;
+    a.base_out = base_out;
+    a.base_offset = base_offset;
+    a.total_out = total_out;
+    a.write_indexer = write_indexer ? 1 : 0;
+    a.nlocal_from = nlocal_from;
+    a.tile_sums = d->d_tile_sums;
+    const int tiles = (int)std::max<int64_t>(1, scan_tiles(d->n_cells));
+    MZ_LAUNCH(d->ctx, "scan_tiles", k_scan_tiles, tiles, SCAN_THREADS, 0, a);
+    MZ_LAUNCH(d->ctx, "scan", k_scan_apply, tiles, SCAN_THREADS, 0, a);
 }
 
 static int grid_for(mz_ctx* c, int64_t work, int threads, int per_sm = 8)
@@ -208,8 +278,7 @@ void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index)
         int mode = grid ? 1 : 0;
         MZ_LAUNCH(c, "sort_count", k_count, grid_for(c, hw, 256), 256, 0, v, s, hw, mode, grid ? grid->inv_dx : 0.0);
     }
-    MZ_LAUNCH(c, "scan", k_scan, 1, 1024, 0, S.counts, (int32_t)d->n_cells, S.ind, S.fill, (int32_t*)nullptr,
-              (int64_t)0, d->d_scalar, 1, (const Indexer*)nullptr);
+    launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar, true, nullptr, 0, nullptr);
     if (hw > 0) {
         MZ_LAUNCH(c, "sort_scatter", k_scatter, grid_for(c, hw, 256), 256, 0, v, s, hw);
         MZ_LAUNCH(c, "sort_gather", k_sort_gather, grid_for(c, d->n_cells * 32, 256, 16), 256, 0, v, s);
@@ -246,8 +315,7 @@ void launch_compact(mz_domain* d, int s)
     SpeciesHost& S = d->sp[s];
     if (S.compact) return;
     DomainView v = make_view(d);
-    MZ_LAUNCH(c, "compact_scan", k_scan, 1, 1024, 0, S.counts, (int32_t)d->n_cells, S.ind, S.fill, S.work, (int64_t)0,
-              d->d_scalar, 0, (const Indexer*)S.ind);
+    launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar, false, S.work, 0, S.ind);
     MZ_LAUNCH(c, "compact_gather", k_compact_gather, grid_for(c, d->n_cells * 32, 256, 16), 256, 0, v, s, S.work);
     MZ_CK(cudaMemcpyAsync(d->h_scalar, d->d_scalar, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     MZ_CK(cudaStreamSynchronize(c->stream));

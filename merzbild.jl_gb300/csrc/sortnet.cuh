@@ -85,6 +85,23 @@ __device__ __forceinline__ void copy_particle(const Cols& A, const Cols& B, int3
     B.z[dst] = A.z[src];
 }
 
+// dst[start + q] = src[v[q]] for the warp's E register-major rows: all E loads
+// of a lane are issued before its first store (the gather is bound by the
+// latency of these scattered reads, so they must be in flight together).  The
+// source buffer is not written while a gather runs.
+template <int E>
+__device__ __forceinline__ void gather_column(const double* __restrict__ src, double* __restrict__ dst,
+                                              const int32_t (&v)[E], int32_t start, int32_t N)
+{
+    const int lane = threadIdx.x & 31;
+    double t[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) t[r] = (r * 32 + lane) < N ? __ldg(src + v[r]) : 0.0;
+#pragma unroll
+    for (int r = 0; r < E; ++r)
+        if ((r * 32 + lane) < N) dst[start + r * 32 + lane] = t[r];
+}
+
 template <int E>
 __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
 {
@@ -96,14 +113,19 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
         v[r] = q < N ? S.idx[start + q] : INT_MAX;
     }
     warp_bitonic<E>(v);
+    gather_column<E>(S.A.w, S.B.w, v, start, N);
+    gather_column<E>(S.A.vx, S.B.vx, v, start, N);
+    gather_column<E>(S.A.vy, S.B.vy, v, start, N);
+    gather_column<E>(S.A.vz, S.B.vz, v, start, N);
+    gather_column<E>(S.A.x, S.B.x, v, start, N);
+    gather_column<E>(S.A.y, S.B.y, v, start, N);
+    gather_column<E>(S.A.z, S.B.z, v, start, N);
 #pragma unroll
     for (int r = 0; r < E; ++r) {
         const int q = r * 32 + lane;
         if (q < N) {
-            const int64_t dst = (int64_t)start + q;
-            copy_particle(S.A, S.B, v[r], dst);
-            S.cellB[dst] = c;
-            S.key[dst] = c;
+            S.cellB[start + q] = c;
+            S.key[start + q] = c;
         }
     }
 }

@@ -3,8 +3,10 @@
 // compute_props_sorted! -> avg_props!) and of the 0-D drivers (README.md:91-106:
 // ntc! for every species pair -> compute_props!).
 //
-// One warp owns one cell for the whole step.  With a 1-D grid, one step is
+// One warp owns 32 / G cells for the whole step (G: lanes per cell in NTC,
+// ntc_group_width).  With a 1-D grid, one step is
 //   scan (per species)    : counts accumulated by the previous step -> indexer
+//                           (two passes, launch_scan_cells)
 //   scatter (per species) : slot tickets per destination cell
 //   k_cell                : sort the cell's segment and gather its particles
 //                           (A -> B, the only full read+write of particle
@@ -44,6 +46,7 @@ struct StepArgs {
     int props_lag;     // props describe the state after step (step - props_lag)
     uint32_t* step_ptr;   // RNG step of the NTC / convection done by this launch
     unsigned int* done;   // last-block counter
+    unsigned int* next;   // next cell to hand out (cells are taken CPW at a time)
 };
 
 __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const CellMoments& r, int32_t np,
@@ -68,106 +71,139 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
     }
 }
 
+// A warp takes CPW = 32 / G consecutive cells at a time.  Sorting, gathering,
+// props and convection run cell by cell on the whole warp; NTC runs on all CPW
+// cells at once, one group of G lanes per cell.  The grid is resident (one
+// wave) and hands out cells through an atomic counter, so no partial last wave
+// idles the GPU.
+template <int G>
 __global__ void __launch_bounds__(256) k_cell(DomainView d, StepArgs a)
 {
+    constexpr int CPW = 32 / G;
     const uint32_t step = *a.step_ptr;
     const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const WarpGroup<G> grp;
+    const int gi = lane / G;
     const int ns = d.n_species;
     unsigned long long cand = 0, accd = 0, hits = 0;
     bool cap = false;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < d.n_cells; c += nwarps) {
-        Indexer p[MZ_MAX_SPECIES];
-        Cols P[MZ_MAX_SPECIES];
-        for (int s = 0; s < ns; ++s) {
-            const SpeciesView& S = d.sp[s];
-            p[s] = S.ind[c];
-            if (a.gather) sort_gather_segment(S, c, p[s].start1, p[s].n1);
-            P[s] = a.gather ? S.B : S.A;
-        }
-        __syncwarp();
-        // 1-D: props of the freshly sorted state, before the next step's physics
-        if (a.props && a.props_lag == 1) {
+    // a resident grid; warps take the next CPW cells until none are left
+    for (;;) {
+        unsigned int t = 0;
+        if (lane == 0) t = atomicAdd(a.next, (unsigned)CPW);
+        const int c0 = (int)__shfl_sync(0xFFFFFFFFu, t, 0);
+        if (c0 >= d.n_cells) break;
+        const int nq = min(CPW, d.n_cells - c0);
+        // sort + gather (A -> B), then 1-D props of the freshly sorted state
+        for (int q = 0; q < nq; ++q) {
+            const int c = c0 + q;
             for (int s = 0; s < ns; ++s) {
-                const CellMoments r = props_cell(P[s], p[s], p[s].n1, d.sp[s].mass);
-                if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p[s].n1, step);
+                const SpeciesView& S = d.sp[s];
+                const Indexer p = S.ind[c];
+                if (a.gather) sort_gather_segment(S, c, p.start1, p.n1);
+            }
+            __syncwarp();
+            if (a.props && a.props_lag == 1) {
+                for (int s = 0; s < ns; ++s) {
+                    const SpeciesView& S = d.sp[s];
+                    const Indexer p = S.ind[c];
+                    const CellMoments r = props_cell(a.gather ? S.B : S.A, p, p.n1, S.mass);
+                    if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p.n1, step);
+                }
             }
         }
         if (!a.physics && !(a.props && a.props_lag == 0)) continue;
-        const uint64_t seed = cell_seed(d, c);
-        const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
-        const double V = d.cell_V[c];
-        // ntc_equal_weight! for every pair in the reference's order
-        for (int s2 = 0; s2 < ns && a.physics; ++s2) {
-            for (int s1 = s2; s1 < ns; ++s1) {
-                const bool single = s1 == s2;
-                const int cfi = s1 + ns * s2;
-                CollisionFactors cf = d.cf[(size_t)cfi * d.n_cells + c];
-                const uint32_t pc = (uint32_t)(s1 * ns + s2);
-                const int32_t ncoll = ntc_ncoll(d, cf, single, p[s1].n1, p[s2].n1, a.dt, V, seed, pc, stp, rid);
-                NtcResult R;
-                R.smax = cf.smax;
-                R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
-                if (ncoll > 0) {
-                    Indexer q1 = p[s1], q2 = p[s2];
-                    R = ntc_cell<true>(d, d.inter[cfi], single, c, ncoll, cf.smax, P[s1], P[s2], q1, q2, nullptr,
-                                       nullptr, nullptr, nullptr, 0, 0, 0.0, seed, pc, stp, rid);
-                }
-                cand += ncoll;
-                accd += R.perf;
-                if (lane == 0) {
-                    cf.smax = R.smax;
-                    cf.n_coll_performed = R.perf;
-                    cf.n_eq_w_coll_performed = R.eqw;
-                    d.cf[(size_t)cfi * d.n_cells + c] = cf;
+        // ntc_equal_weight! for every pair in the reference's order, one
+        // group per cell
+        const int c = c0 + gi;
+        if (a.physics && gi < nq) {
+            const uint64_t seed = cell_seed(d, c);
+            const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
+            const double V = d.cell_V[c];
+            for (int s2 = 0; s2 < ns; ++s2) {
+                for (int s1 = s2; s1 < ns; ++s1) {
+                    const bool single = s1 == s2;
+                    const int cfi = s1 + ns * s2;
+                    const SpeciesView& S1 = d.sp[s1];
+                    const SpeciesView& S2 = d.sp[s2];
+                    Indexer q1 = S1.ind[c], q2 = S2.ind[c];
+                    CollisionFactors cf = d.cf[(size_t)cfi * d.n_cells + c];
+                    const uint32_t pc = (uint32_t)(s1 * ns + s2);
+                    const int32_t ncoll = ntc_ncoll(d, cf, single, q1.n1, q2.n1, a.dt, V, seed, pc, stp, rid);
+                    NtcResult R;
+                    R.smax = cf.smax;
+                    R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
+                    if (ncoll > 0)
+                        R = ntc_cell<true, G>(d, d.inter[cfi], single, c, ncoll, cf.smax, a.gather ? S1.B : S1.A,
+                                              a.gather ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
+                                              0, 0.0, seed, pc, stp, rid);
+                    if (grp.rank == 0) {
+                        cand += ncoll;
+                        accd += R.perf;
+                        cf.smax = R.smax;
+                        cf.n_coll_performed = R.perf;
+                        cf.n_eq_w_coll_performed = R.eqw;
+                        d.cf[(size_t)cfi * d.n_cells + c] = cf;
+                    }
                 }
             }
         }
         __syncwarp();
-        // 0-D: compute_props! after the collisions of this step
-        if (a.props && a.props_lag == 0) {
-            for (int s = 0; s < ns; ++s) {
-                const CellMoments r = props_cell(P[s], p[s], p[s].n1, d.sp[s].mass);
-                if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p[s].n1, step);
-            }
-        }
-        if (a.dims != 1 || !a.physics) continue;
-        // convect_particles! + get_cell for the next sort
-        for (int s = 0; s < ns; ++s) {
-            const SpeciesView& S = d.sp[s];
-            const Cols& Q = P[s];
-            const int32_t n1 = p[s].n1, st1 = p[s].start1;
-            for (int j0 = 0; j0 < n1; j0 += 32) {
-                const int j = j0 + lane;
-                const bool in = j < n1;
-                int32_t key = 0;
-                if (in) {
-                    const int64_t q = (int64_t)st1 + j;
-                    double x = Q.x[q];
-                    double vx = Q.vx[q];
-                    const double xn = fma(vx, a.dt, x);
-                    if ((xn >= a.W.L) || (xn <= 0.0)) {
-                        Stream rs;
-                        rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
-                        double vy = Q.vy[q], vz = Q.vz[q];
-                        hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
-                        Q.vx[q] = vx;
-                        Q.vy[q] = vy;
-                        Q.vz[q] = vz;
-                    } else {
-                        x = fmin(fmax(xn, a.W.min_x), a.W.max_x);
-                    }
-                    Q.x[q] = x;
-                    key = cell_of(d, x, a.W.inv_dx);
-                    S.key[q] = key;
+        for (int q = 0; q < nq; ++q) {
+            const int cq = c0 + q;
+            // 0-D: compute_props! after the collisions of this step
+            if (a.props && a.props_lag == 0) {
+                for (int s = 0; s < ns; ++s) {
+                    const SpeciesView& S = d.sp[s];
+                    const Indexer p = S.ind[cq];
+                    const CellMoments r = props_cell(a.gather ? S.B : S.A, p, p.n1, S.mass);
+                    if (lane == 0) write_props(a, (int64_t)cq + (int64_t)d.n_cells * s, r, p.n1, step);
                 }
-                const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
-                if (in) warp_agg_add(S.counts, key, m);
+            }
+            if (a.dims != 1 || !a.physics) continue;
+            // convect_particles! + get_cell for the next sort
+            const uint64_t seed = cell_seed(d, cq);
+            const uint32_t rid = cell_rid(d, cq), stp = cell_step(d, cq, step);
+            for (int s = 0; s < ns; ++s) {
+                const SpeciesView& S = d.sp[s];
+                const Cols& Q = a.gather ? S.B : S.A;
+                const Indexer p = S.ind[cq];
+                const int32_t n1 = p.n1, st1 = p.start1;
+                for (int j0 = 0; j0 < n1; j0 += 32) {
+                    const int j = j0 + lane;
+                    const bool in = j < n1;
+                    int32_t key = 0;
+                    if (in) {
+                        const int64_t qq = (int64_t)st1 + j;
+                        double x = Q.x[qq];
+                        double vx = Q.vx[qq];
+                        const double xn = fma(vx, a.dt, x);
+                        if (!move_free(a.W, xn, x)) {
+                            Stream rs;
+                            rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
+                            double vy = Q.vy[qq], vz = Q.vz[qq];
+                            hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
+                            Q.vx[qq] = vx;
+                            Q.vy[qq] = vy;
+                            Q.vz[qq] = vz;
+                        }
+                        Q.x[qq] = x;
+                        key = cell_of(d, x, a.W.inv_dx);
+                        S.key[qq] = key;
+                    }
+                    const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
+                    if (in) warp_agg_add(S.counts, key, m);
+                }
             }
         }
     }
     if (cap) set_status(d, ST_WALL_HITS);
-    hits = __reduce_add_sync(0xFFFFFFFFu, (unsigned)hits);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand += __shfl_xor_sync(0xFFFFFFFFu, cand, o);
+        accd += __shfl_xor_sync(0xFFFFFFFFu, accd, o);
+        hits += __shfl_xor_sync(0xFFFFFFFFu, hits, o);
+    }
     if (lane == 0 && (cand | accd | hits)) {
         atomicAdd(&d.counters->candidates, cand);
         atomicAdd(&d.counters->accepted, accd);
@@ -180,54 +216,10 @@ __global__ void __launch_bounds__(256) k_cell(DomainView d, StepArgs a)
         const unsigned prev = atomicAdd(a.done, 1u);
         if (prev == gridDim.x - 1) {
             *a.done = 0;
+            *a.next = 0;
             *a.step_ptr = step + 1;
             __threadfence();
         }
-    }
-}
-
-// scan of the counts the previous k_cell accumulated -> indexer (group 1 only)
-__global__ void __launch_bounds__(1024) k_step_scan(int32_t* counts, int32_t n, Indexer* ind, int32_t* fill,
-                                                    int64_t* total_out)
-{
-    __shared__ long long warp_tot[32];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int chunk = (n + blockDim.x - 1) / blockDim.x;
-    const int c0 = min(n, t * chunk), c1 = min(n, c0 + chunk);
-    long long local = 0;
-    for (int c = c0; c < c1; ++c) local += counts[c];
-    long long incl = local;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) warp_tot[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-        const long long v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
-        long long vi = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const long long u = __shfl_up_sync(0xFFFFFFFFu, vi, o);
-            if (lane >= o) vi += u;
-        }
-        warp_tot[lane] = vi - v;
-        if (lane == 31) *total_out = vi;
-    }
-    __syncthreads();
-    long long run = warp_tot[w] + (incl - local);
-    for (int c = c0; c < c1; ++c) {
-        const int32_t cnt = counts[c];
-        Indexer p;
-        p.start1 = (int32_t)run;
-        p.n1 = cnt;
-        p.start2 = 0;
-        p.n2 = 0;
-        ind[c] = p;
-        fill[c] = 0;
-        counts[c] = 0;
-        run += cnt;
     }
 }
 
@@ -257,8 +249,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     for (int s = 0; s < d->ns; ++s) launch_compact(d, s);
     if (!d->d_step) {
         MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
-        MZ_CK(cudaMalloc(&d->d_done, sizeof(unsigned int)));
-        MZ_CK(cudaMemsetAsync(d->d_done, 0, sizeof(unsigned int), c->stream));
+        MZ_CK(cudaMalloc(&d->d_done, 2 * sizeof(unsigned int)));
+        MZ_CK(cudaMemsetAsync(d->d_done, 0, 2 * sizeof(unsigned int), c->stream));
     }
     const uint32_t first = (uint32_t)(plan->step0 + 1);
     MZ_CK(cudaMemcpyAsync(d->d_step, &first, sizeof first, cudaMemcpyHostToDevice, c->stream));
@@ -269,6 +261,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.W.min_x = plan->grid.min_x;
     a.W.max_x = plan->grid.max_x;
     a.W.inv_dx = plan->grid.inv_dx;
+    wall_bits(a.W);
     for (int b = 0; b < 2; ++b) {
         for (int q = 0; q < MZ_MAX_SPECIES; ++q) a.W.vsq[b][q] = plan->walls.reflection_v_sq[b][q];
         a.W.acc[b] = plan->walls.accommodation[b];
@@ -286,8 +279,14 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.props_lag = plan->dims == 1 ? 1 : 0;
     a.step_ptr = d->d_step;
     a.done = d->d_done;
+    a.next = d->d_done + 1;
     const bool want_props = plan->props && (inst || a.has_avg);
-    const int blocks = (int)div_up(d->n_cells, 8);
+    const int G = ntc_group_width(d->n_cells);
+    void (*kern)(DomainView, StepArgs) = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
+    int per_sm = 0;
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    const int blocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>(div_up(d->n_cells, 8 * (32 / G)), (int64_t)c->num_sms * std::max(per_sm, 1)));
 
     auto cell_launch = [&](int gather, int props, int physics) {
         StepArgs b = a;
@@ -298,15 +297,14 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
-        MZ_LAUNCH(c, name, k_cell, blocks, 256, 0, v, b);
+        MZ_LAUNCH(c, name, kern, blocks, 256, 0, v, b);
     };
     // one sort of every species from the keys k_cell wrote, gather in k_cell
     auto sort_launch = [&](int props, int physics) {
         DomainView v = make_view(d);
         for (int s = 0; s < d->ns; ++s) {
             SpeciesHost& S = d->sp[s];
-            MZ_LAUNCH(c, "step_scan", k_step_scan, 1, 1024, 0, S.counts, (int32_t)d->n_cells, S.ind, S.fill,
-                      d->d_scalar + s);
+            launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar + s, true, nullptr, 0);
             const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, 256), (int64_t)c->num_sms * 8));
             MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total);
         }

@@ -104,6 +104,7 @@ _SIGS = {
     "mz_step": (i32, [vp, P(StepPlan), i64, vp, vp]),
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
     "mz_sort_keys_noalloc": (i32, [vp, vp, i64, i32, vp, vp]),
+    "mz_sincos_2pi": (i32, [vp, i64, P(u64), P(d), P(d)]),
 }
 NOALLOC_MAX_CELLS = 262144
 
