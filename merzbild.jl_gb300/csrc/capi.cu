@@ -100,10 +100,8 @@ mz::DomainView make_view(mz_domain* d)
     for (int s = 0; s < d->ns; ++s) {
         SpeciesHost& S = d->sp[s];
         SpeciesView& o = v.sp[s];
-        double** a = S.cols[S.cur];
-        double** b = S.cols[S.cur ^ 1];
-        o.A = Cols{a[0], a[1], a[2], a[3], a[4], a[5], a[6]};
-        o.B = Cols{b[0], b[1], b[2], b[3], b[4], b[5], b[6]};
+        o.A = Cols{S.wv[S.cur], S.pos[S.cur]};
+        o.B = Cols{S.wv[S.cur ^ 1], S.pos[S.cur ^ 1]};
         o.cell = S.cell[S.cur];
         o.cellB = S.cell[S.cur ^ 1];
         o.key = S.key;
@@ -148,7 +146,8 @@ void check_status(mz_domain* d)
 static void free_species(SpeciesHost& S)
 {
     for (int b = 0; b < 2; ++b) {
-        for (int k = 0; k < 7; ++k) cudaFree(S.cols[b][k]);
+        cudaFree(S.wv[b]);
+        cudaFree(S.pos[b]);
         cudaFree(S.cell[b]);
     }
     cudaFree(S.key);
@@ -158,7 +157,8 @@ static void free_species(SpeciesHost& S)
 static void alloc_cols(SpeciesHost& S, int64_t cap)
 {
     for (int b = 0; b < 2; ++b) {
-        for (int k = 0; k < 7; ++k) MZ_CK(cudaMalloc(&S.cols[b][k], std::max<int64_t>(cap, 1) * sizeof(double)));
+        MZ_CK(cudaMalloc(&S.wv[b], std::max<int64_t>(cap, 1) * sizeof(PV)));
+        MZ_CK(cudaMalloc(&S.pos[b], std::max<int64_t>(cap, 1) * sizeof(PX)));
         MZ_CK(cudaMalloc(&S.cell[b], std::max<int64_t>(cap, 1) * sizeof(int32_t)));
     }
     MZ_CK(cudaMalloc(&S.key, std::max<int64_t>(cap, 1) * sizeof(int32_t)));
@@ -176,16 +176,16 @@ void reserve_species(mz_domain* d, int s, int64_t cap)
     alloc_cols(N, cap);
     const int64_t hw = S.hw;
     if (hw > 0) {
-        for (int k = 0; k < 7; ++k)
-            MZ_CK(cudaMemcpyAsync(N.cols[0][k], S.cols[S.cur][k], hw * sizeof(double), cudaMemcpyDeviceToDevice,
-                                  d->ctx->stream));
+        MZ_CK(cudaMemcpyAsync(N.wv[0], S.wv[S.cur], hw * sizeof(PV), cudaMemcpyDeviceToDevice, d->ctx->stream));
+        MZ_CK(cudaMemcpyAsync(N.pos[0], S.pos[S.cur], hw * sizeof(PX), cudaMemcpyDeviceToDevice, d->ctx->stream));
         MZ_CK(cudaMemcpyAsync(N.cell[0], S.cell[S.cur], hw * sizeof(int32_t), cudaMemcpyDeviceToDevice, d->ctx->stream));
         MZ_CK(cudaMemcpyAsync(N.key, S.key, hw * sizeof(int32_t), cudaMemcpyDeviceToDevice, d->ctx->stream));
     }
     MZ_CK(cudaStreamSynchronize(d->ctx->stream));
     free_species(S);
     for (int b = 0; b < 2; ++b) {
-        for (int k = 0; k < 7; ++k) S.cols[b][k] = N.cols[b][k];
+        S.wv[b] = N.wv[b];
+        S.pos[b] = N.pos[b];
         S.cell[b] = N.cell[b];
     }
     S.key = N.key;
@@ -510,19 +510,32 @@ int mz_set_cell_rng(mz_domain* d, const uint64_t* seed, const uint32_t* rid, con
     API_CATCH(d->ctx)
 }
 
+namespace {
+// records from the caller's columns staged in device memory
+__global__ void k_pack(int64_t n, const double* w, const double* v, const double* x, PV* ov, PX* ox)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        ov[i] = PV{w[i], v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+        ox[i] = PX{x[3 * i], x[3 * i + 1], x[3 * i + 2], 0.0};
+    }
+}
+}  // namespace
+
+// w (n), v (3n) and x (3n, row-major) into buffer A's records: the columns
+// are staged in buffer B (free outside a sort) and packed on the device
 static void upload_cols(mz_domain* d, int s, int64_t n, const double* w, const double* v, const double* x)
 {
     SpeciesHost& S = d->sp[s];
-    std::vector<double> col(n);
-    cudaStream_t st = d->ctx->stream;
-    MZ_CK(cudaMemcpyAsync(S.cols[S.cur][0], w, n * sizeof(double), cudaMemcpyHostToDevice, st));
-    for (int k = 0; k < 6; ++k) {
-        const double* src = k < 3 ? v : x;
-        const int comp = k % 3;
-        for (int64_t i = 0; i < n; ++i) col[i] = src[3 * i + comp];
-        MZ_CK(cudaMemcpyAsync(S.cols[S.cur][1 + k], col.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
-        MZ_CK(cudaStreamSynchronize(st));
-    }
+    mz_ctx* c = d->ctx;
+    double* sw = reinterpret_cast<double*>(S.wv[S.cur ^ 1]);  // 4n doubles: w then v
+    double* sv = sw + n;
+    double* sx = reinterpret_cast<double*>(S.pos[S.cur ^ 1]);  // 3n doubles
+    MZ_CK(cudaMemcpyAsync(sw, w, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sv, v, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sx, x, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(n, 256), (int64_t)c->num_sms * 8));
+    MZ_LAUNCH(c, "pack", k_pack, blocks, 256, 0, n, sw, sv, sx, S.wv[S.cur], S.pos[S.cur]);
+    MZ_CK(cudaStreamSynchronize(c->stream));
 }
 
 int mz_upload_particles(mz_domain* d, int32_t s, int64_t n, const double* w, const double* v, const double* x,
@@ -610,11 +623,11 @@ int mz_download_particles(mz_domain* d, int32_t s, int64_t max_n, double* w, dou
     for (auto& p : ind) total += p.n1 + p.n2;
     if (n_out) *n_out = total;
     if (total > max_n) throw MzError(MZ_E_CAPACITY, "mz_download_particles: output buffers too small");
-    std::vector<double> col[7];
-    for (int k = 0; k < 7; ++k) {
-        col[k].resize(std::max<int64_t>(hw, 1));
-        if (hw > 0)
-            MZ_CK(cudaMemcpy(col[k].data(), S.cols[S.cur][k], hw * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<PV> rv(std::max<int64_t>(hw, 1));
+    std::vector<PX> rx(std::max<int64_t>(hw, 1));
+    if (hw > 0) {
+        MZ_CK(cudaMemcpy(rv.data(), S.wv[S.cur], hw * sizeof(PV), cudaMemcpyDeviceToHost));
+        MZ_CK(cudaMemcpy(rx.data(), S.pos[S.cur], hw * sizeof(PX), cudaMemcpyDeviceToHost));
     }
     int64_t o = 0;
     for (int64_t c = 0; c < d->n_cells; ++c) {
@@ -622,11 +635,17 @@ int mz_download_particles(mz_domain* d, int32_t s, int64_t max_n, double* w, dou
         for (int32_t j = 0; j < p.n1 + p.n2; ++j, ++o) {
             const int64_t q = j < p.n1 ? p.start1 + j : p.start2 + (j - p.n1);
             MZ_REQUIRE(q >= 0 && q < hw, "mz_download_particles: indexer points outside the slots in use");
-            if (w) w[o] = col[0][q];
-            if (v)
-                for (int k = 0; k < 3; ++k) v[3 * o + k] = col[1 + k][q];
-            if (x)
-                for (int k = 0; k < 3; ++k) x[3 * o + k] = col[4 + k][q];
+            if (w) w[o] = rv[q].w;
+            if (v) {
+                v[3 * o] = rv[q].vx;
+                v[3 * o + 1] = rv[q].vy;
+                v[3 * o + 2] = rv[q].vz;
+            }
+            if (x) {
+                x[3 * o] = rx[q].x;
+                x[3 * o + 1] = rx[q].y;
+                x[3 * o + 2] = rx[q].z;
+            }
             if (cell) cell[o] = (int32_t)c;
         }
     }

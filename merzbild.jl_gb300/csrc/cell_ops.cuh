@@ -37,19 +37,6 @@ __device__ __forceinline__ int32_t ntc_ncoll(const DomainView& d, CollisionFacto
     return nci;
 }
 
-struct PartV {
-    double w, vx, vy, vz;
-};
-
-__device__ __forceinline__ PartV load_pv(const Cols& A, int32_t slot)
-{
-    PartV p;
-    p.w = A.w[slot];
-    p.vx = A.vx[slot];
-    p.vy = A.vy[slot];
-    p.vz = A.vz[slot];
-    return p;
-}
 
 struct NtcResult {
     double smax;
@@ -157,7 +144,7 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
         const float l_smax = log2_pos(smax);
         const bool screen_b = screen && fabsf(l_smax) < 2.0f * LOG_RANGE;
         int32_t si = 0, sk = 0;
-        PartV a, b;
+        PV a, b;
         a.w = b.w = 0.0;
         double g2 = 0.0, g = 0.0, sgw = -1.0, wmax = 0.0;
         bool has = false, exact = false, have_g = false;
@@ -165,8 +152,8 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
         if (act) {
             si = map_slot(p1, i);
             sk = map_slot(p2, k);
-            a = load_pv(P1, si);
-            b = load_pv(P2, sk);
+            a = P1.wv[si];
+            b = P2.wv[sk];
             // compute_g! (collision_utils.jl:388-391)
             const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
             g2 = (gx * gx + gy * gy) + gz * gz;
@@ -232,6 +219,7 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
         spl = spl && act;
         int side = 0;
         if (acc) {
+            double wi = a.w, wk = b.w;  // weights after a split
             if (!have_g) g = sqrt(g2);
             // compute_com! (collision_utils.jl:374-376)
             const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
@@ -244,25 +232,23 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
                 side = heavy_i ? 1 : 2;
                 const Cols& PP = heavy_i ? P1 : P2;
                 const int32_t src = heavy_i ? si : sk;
-                const PartV& h = heavy_i ? a : b;
+                const PV& h = heavy_i ? a : b;
                 const double wl = heavy_i ? b.w : a.w;
                 int32_t ns_;
                 if (heavy_i || single)
                     ns_ = b1 + R.nsp1;
                 else
                     ns_ = b2 + R.nsp2;
-                PP.w[ns_] = h.w - wl;
-                PP.vx[ns_] = h.vx;
-                PP.vy[ns_] = h.vy;
-                PP.vz[ns_] = h.vz;
-                PP.x[ns_] = PP.x[src];
-                PP.y[ns_] = PP.y[src];
-                PP.z[ns_] = PP.z[src];
+                PP.wv[ns_] = PV{h.w - wl, h.vx, h.vy, h.vz};
+                PP.pos[ns_] = PP.pos[src];
                 int32_t* cl = (heavy_i || single) ? cell1 : cell2;
                 int32_t* ky = (heavy_i || single) ? key1 : key2;
                 cl[ns_] = c;
                 ky[ns_] = c;
-                PP.w[src] = wl;
+                if (heavy_i)
+                    wi = wl;
+                else
+                    wk = wl;
             }
             // scatter_vhs! (collision_scattering.jl:17-29): phi = 2 pi rand(),
             // cos(theta) = 2 rand() - 1
@@ -271,12 +257,8 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
             const double ct = fma(2.0, st.uniform(), -1.0);
             const double sth = sqrt(1.0 - ct * ct);
             const double nx = g * (sth * cphi), ny = g * (sth * sphi), nz = g * ct;
-            P1.vx[si] = cx + I.mu2 * nx;
-            P1.vy[si] = cy + I.mu2 * ny;
-            P1.vz[si] = cz + I.mu2 * nz;
-            P2.vx[sk] = cx - I.mu1 * nx;
-            P2.vy[sk] = cy - I.mu1 * ny;
-            P2.vz[sk] = cz - I.mu1 * nz;
+            P1.wv[si] = PV{wi, cx + I.mu2 * nx, cy + I.mu2 * ny, cz + I.mu2 * nz};
+            P2.wv[sk] = PV{wk, cx - I.mu1 * nx, cy - I.mu1 * ny, cz - I.mu1 * nz};
         }
         const unsigned am = grp.ballot(acc);
         R.perf += __popc(am);
@@ -317,12 +299,11 @@ __device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& 
     const int lane = threadIdx.x & 31;
     double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     for (int j = lane; j < nl; j += 32) {
-        const int32_t q = map_slot(p, j);
-        const double w = P.w[q];
-        n += w;
-        sx += P.vx[q] * w;
-        sy += P.vy[q] * w;
-        sz += P.vz[q] * w;
+        const PV r = P.wv[map_slot(p, j)];
+        n += r.w;
+        sx += r.vx * r.w;
+        sy += r.vy * r.w;
+        sz += r.vz * r.w;
     }
     n = warp_sum(n);
     sx = warp_sum(sx);
@@ -337,9 +318,9 @@ __device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& 
         r.uz = sz / n;
         double E = 0.0;
         for (int j = lane; j < nl; j += 32) {
-            const int32_t q = map_slot(p, j);
-            const double dx = P.vx[q] - r.ux, dy = P.vy[q] - r.uy, dz = P.vz[q] - r.uz;
-            E = fma(P.w[q], (dx * dx + dy * dy) + dz * dz, E);
+            const PV u = P.wv[map_slot(p, j)];
+            const double dx = u.vx - r.ux, dy = u.vy - r.uy, dz = u.vz - r.uz;
+            E = fma(u.w, (dx * dx + dy * dy) + dz * dz, E);
         }
         E = warp_sum(E);
         E *= 0.5 * mass / (n * K_B);

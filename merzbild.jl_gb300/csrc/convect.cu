@@ -31,17 +31,16 @@ __global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw
                                                                                   : p.n1 + (int32_t)(slot - p.start2);
         Stream st;
         st.init(cell_seed(d, c), TAG_CONVECT, (uint32_t)s, cell_step(d, c, step), cell_rid(d, c), (uint32_t)j);
-        double x = S.A.x[slot];
-        double vx = S.A.vx[slot];
+        double x = S.A.pos[slot].x;
+        double vx = S.A.wv[slot].vx;
         const double xn = fma(vx, dt, x);
         if (!move_free(W, xn, x)) {
-            double vy = S.A.vy[slot], vz = S.A.vz[slot];
+            const PV r = S.A.wv[slot];
+            double vy = r.vy, vz = r.vz;
             my_hits += convect_walls(st, W, s, x, vx, vy, vz, dt, cap);
-            S.A.vx[slot] = vx;
-            S.A.vy[slot] = vy;
-            S.A.vz[slot] = vz;
+            S.A.wv[slot] = PV{r.w, vx, vy, vz};
         }
-        S.A.x[slot] = x;
+        S.A.pos[slot].x = x;
         if (compute_cell) S.key[slot] = cell_of(d, x, W.inv_dx);
     }
     if (cap) set_status(d, ST_WALL_HITS);

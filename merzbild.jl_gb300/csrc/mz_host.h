@@ -63,7 +63,8 @@ struct SpeciesHost {
     int64_t hw = 0;        // high water: slots [0, hw) in use (live or dead)
     int64_t n_total = 0;   // live particles
     bool compact = true;   // every cell's list lies in group 1 and no dead slot below hw
-    double* cols[2][7] = {{nullptr}};  // [buffer A/B][w, vx, vy, vz, x, y, z]
+    mz::PV* wv[2] = {nullptr, nullptr};   // [buffer A/B] weight + velocity records
+    mz::PX* pos[2] = {nullptr, nullptr};  // [buffer A/B] position records
     int cur = 0;           // which buffer is A
     int32_t* cell[2] = {nullptr, nullptr};  // [A/B] owner cell per slot
     int32_t* key = nullptr;

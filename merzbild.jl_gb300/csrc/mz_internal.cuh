@@ -1,8 +1,9 @@
 // Internal definitions shared by the merzgpu CUDA translation units.
 //
 // Device layout of one domain (n_cells cells x n_species species):
-//   per species, structure-of-arrays FP64 columns w, vx, vy, vz, x, y, z in
-//   two buffers (A = live, B = sort target), int32 `cell` (cell that owns the
+//   per species, two arrays of 32-byte records -- {w, vx, vy, vz} and
+//   {x, y, z, unused}, one DRAM sector each -- in two buffers (A = live,
+//   B = sort target), int32 `cell` (cell that owns the
 //   slot in the current layout, -1 = dead slot), int32 `key` (cell the slot
 //   moves to at the next sort), and a per-cell indexer {start1, n_group1,
 //   start2, n_group2} that has the meaning of Merzbild's ParticleIndexer
@@ -157,9 +158,33 @@ struct Interaction {  // Interaction, collision_utils.jl:73-82
     double m_r, mu1, mu2, vhs_d, vhs_o, vhs_Tref, vhs_muref, vhs_factor;
 };
 
-struct Cols {  // one SoA buffer of a species
-    double *w, *vx, *vy, *vz, *x, *y, *z;
+struct __align__(32) PV {  // weight and velocity of one particle
+    double w, vx, vy, vz;
 };
+
+struct __align__(32) PX {  // position of one particle (the fourth word is unused)
+    double x, y, z, unused;
+};
+
+struct Cols {  // one buffer of a species: record arrays indexed by slot
+    PV* wv;
+    PX* pos;
+};
+
+// 32-byte record moves as two 16-byte accesses; ldg_* read through the
+// read-only path (for buffers no thread writes during the kernel)
+__device__ __forceinline__ PV ldg_pv(const PV* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return PV{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ PX ldg_px(const PX* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return PX{a.x, a.y, b.x, b.y};
+}
 
 struct Indexer {  // {start1, n_group1, start2, n_group2}, 0-based slots
     int32_t start1, n1, start2, n2;

@@ -49,12 +49,11 @@ __global__ void __launch_bounds__(256) k_props(DomainView d, PropsView P, int mo
             n = 0.0;
             double sx = 0.0, sy = 0.0, sz = 0.0;
             for (int j = lane; j < nl; j += 32) {
-                const int32_t q = map_slot(p, j);
-                const double w = S.A.w[q];
-                n += w;
-                sx += S.A.vx[q] * w;
-                sy += S.A.vy[q] * w;
-                sz += S.A.vz[q] * w;
+                const PV r = S.A.wv[map_slot(p, j)];
+                n += r.w;
+                sx += r.vx * r.w;
+                sy += r.vy * r.w;
+                sz += r.vz * r.w;
             }
             n = warp_sum(n);
             sx = warp_sum(sx);
@@ -68,9 +67,9 @@ __global__ void __launch_bounds__(256) k_props(DomainView d, PropsView P, int mo
                 uz = sz / n;
                 double E = 0.0;
                 for (int j = lane; j < nl; j += 32) {
-                    const int32_t q = map_slot(p, j);
-                    const double w = S.A.w[q];
-                    const double dx = S.A.vx[q] - ux, dy = S.A.vy[q] - uy, dz = S.A.vz[q] - uz;
+                    const PV r = S.A.wv[map_slot(p, j)];
+                    const double w = r.w;
+                    const double dx = r.vx - ux, dy = r.vy - uy, dz = r.vz - uz;
                     const double nv = sqrt((dx * dx + dy * dy) + dz * dz);
                     E = fma(w, nv * nv, E);
                     for (int m = 0; m < P.n_moments; ++m) mom[m] = fma(w, pow(nv, (double)P.powers[m]), mom[m]);

@@ -108,13 +108,8 @@ __global__ void __launch_bounds__(256) k_sample(DomainView d, int s, SampleArgs 
             }
             double w = Fn;
             if (a.span > 0.0) w = Fn * pow(10.0, a.span * (2.0 * st.uniform() - 1.0));
-            S.A.w[q] = w;
-            S.A.vx[q] = vx;
-            S.A.vy[q] = vy;
-            S.A.vz[q] = vz;
-            S.A.x[q] = x[0];
-            S.A.y[q] = x[1];
-            S.A.z[q] = x[2];
+            S.A.wv[q] = PV{w, vx, vy, vz};
+            S.A.pos[q] = PX{x[0], x[1], x[2], 0.0};
             S.cell[q] = c;
             S.key[q] = c;
         }

@@ -37,7 +37,7 @@ __global__ void k_count(DomainView d, int s, int64_t hw, int mode, double inv_dx
         int32_t key;
         if (mode == 1) {
             // get_cell (grid_uniform1D.jl:97-99), 0-based
-            double f = floor(S.A.x[slot] * inv_dx);
+            double f = floor(S.A.pos[slot].x * inv_dx);
             if (!(f >= 0.0 && f < (double)d.n_cells)) {
                 set_status(d, ST_OUTSIDE_GRID);
                 f = f < 0.0 || f != f ? 0.0 : (double)(d.n_cells - 1);

@@ -76,30 +76,47 @@ __device__ __forceinline__ void warp_oddeven_sort(int32_t* a, int n)
 
 __device__ __forceinline__ void copy_particle(const Cols& A, const Cols& B, int32_t src, int64_t dst)
 {
-    B.w[dst] = A.w[src];
-    B.vx[dst] = A.vx[src];
-    B.vy[dst] = A.vy[src];
-    B.vz[dst] = A.vz[src];
-    B.x[dst] = A.x[src];
-    B.y[dst] = A.y[src];
-    B.z[dst] = A.z[src];
+    B.wv[dst] = ldg_pv(A.wv + src);
+    B.pos[dst] = ldg_px(A.pos + src);
 }
 
-// dst[start + q] = src[v[q]] for the warp's E register-major rows: all E loads
-// of a lane are issued before its first store (the gather is bound by the
-// latency of these scattered reads, so they must be in flight together).  The
-// source buffer is not written while a gather runs.
+// B[start + q] = A[v[q]] (both records) for the warp's E register-major rows,
+// in chunks of two rows whose loads are all issued before the chunk's
+// stores: the gather is bound by the latency of these scattered reads, so
+// they must be in flight together.  Plain loads keep each chunk's loads behind
+// the previous chunk's stores, which bounds the registers in flight.
 template <int E>
-__device__ __forceinline__ void gather_column(const double* __restrict__ src, double* __restrict__ dst,
-                                              const int32_t (&v)[E], int32_t start, int32_t N)
+__device__ __forceinline__ void gather_records(const Cols& A, const Cols& B, const int32_t (&v)[E], int32_t start,
+                                               int32_t N)
 {
+    constexpr int CH = E < 2 ? E : 2;
     const int lane = threadIdx.x & 31;
-    double t[E];
 #pragma unroll
-    for (int r = 0; r < E; ++r) t[r] = (r * 32 + lane) < N ? __ldg(src + v[r]) : 0.0;
+    for (int r0 = 0; r0 < E; r0 += CH) {
+        double2 t[CH][4];
 #pragma unroll
-    for (int r = 0; r < E; ++r)
-        if ((r * 32 + lane) < N) dst[start + r * 32 + lane] = t[r];
+        for (int r = 0; r < CH; ++r) {
+            const bool in = ((r0 + r) * 32 + lane) < N;
+            const double2* pv = reinterpret_cast<const double2*>(A.wv + (in ? v[r0 + r] : 0));
+            const double2* px = reinterpret_cast<const double2*>(A.pos + (in ? v[r0 + r] : 0));
+            t[r][0] = in ? pv[0] : make_double2(0.0, 0.0);
+            t[r][1] = in ? pv[1] : make_double2(0.0, 0.0);
+            t[r][2] = in ? px[0] : make_double2(0.0, 0.0);
+            t[r][3] = in ? px[1] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            const int q = (r0 + r) * 32 + lane;
+            if (q < N) {
+                double2* ov = reinterpret_cast<double2*>(B.wv + start + q);
+                double2* ox = reinterpret_cast<double2*>(B.pos + start + q);
+                ov[0] = t[r][0];
+                ov[1] = t[r][1];
+                ox[0] = t[r][2];
+                ox[1] = t[r][3];
+            }
+        }
+    }
 }
 
 template <int E>
@@ -113,13 +130,7 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
         v[r] = q < N ? S.idx[start + q] : INT_MAX;
     }
     warp_bitonic<E>(v);
-    gather_column<E>(S.A.w, S.B.w, v, start, N);
-    gather_column<E>(S.A.vx, S.B.vx, v, start, N);
-    gather_column<E>(S.A.vy, S.B.vy, v, start, N);
-    gather_column<E>(S.A.vz, S.B.vz, v, start, N);
-    gather_column<E>(S.A.x, S.B.x, v, start, N);
-    gather_column<E>(S.A.y, S.B.y, v, start, N);
-    gather_column<E>(S.A.z, S.B.z, v, start, N);
+    gather_records<E>(S.A, S.B, v, start, N);
 #pragma unroll
     for (int r = 0; r < E; ++r) {
         const int q = r * 32 + lane;
@@ -128,6 +139,13 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
             S.key[start + q] = c;
         }
     }
+}
+
+// Segments above 512 particles take an out-of-line call, so the registers
+// their 32-row sort needs do not raise the register count of every caller.
+static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+{
+    sort_gather_regs<32>(S, c, start, N);
 }
 
 // Sort the source slots of cell c's segment [start, start + N) and gather the
@@ -140,7 +158,7 @@ __device__ __forceinline__ void sort_gather_segment(const SpeciesView& S, int32_
     else if (N <= 128) sort_gather_regs<4>(S, c, start, N);
     else if (N <= 256) sort_gather_regs<8>(S, c, start, N);
     else if (N <= 512) sort_gather_regs<16>(S, c, start, N);
-    else if (N <= 1024) sort_gather_regs<32>(S, c, start, N);
+    else if (N <= 1024) sort_gather_regs_32(S, c, start, N);
     else {
         warp_oddeven_sort(S.idx + start, N);
         for (int q = (threadIdx.x & 31); q < N; q += 32) {

@@ -77,7 +77,7 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
 // wave) and hands out cells through an atomic counter, so no partial last wave
 // idles the GPU.
 template <int G>
-__global__ void __launch_bounds__(256) k_cell(DomainView d, StepArgs a)
+__global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
 {
     constexpr int CPW = 32 / G;
     const uint32_t step = *a.step_ptr;
@@ -175,19 +175,18 @@ __global__ void __launch_bounds__(256) k_cell(DomainView d, StepArgs a)
                     int32_t key = 0;
                     if (in) {
                         const int64_t qq = (int64_t)st1 + j;
-                        double x = Q.x[qq];
-                        double vx = Q.vx[qq];
+                        double x = Q.pos[qq].x;
+                        double vx = Q.wv[qq].vx;
                         const double xn = fma(vx, a.dt, x);
                         if (!move_free(a.W, xn, x)) {
                             Stream rs;
                             rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
-                            double vy = Q.vy[qq], vz = Q.vz[qq];
+                            const PV r = Q.wv[qq];
+                            double vy = r.vy, vz = r.vz;
                             hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
-                            Q.vx[qq] = vx;
-                            Q.vy[qq] = vy;
-                            Q.vz[qq] = vz;
+                            Q.wv[qq] = PV{r.w, vx, vy, vz};
                         }
-                        Q.x[qq] = x;
+                        Q.pos[qq].x = x;
                         key = cell_of(d, x, a.W.inv_dx);
                         S.key[qq] = key;
                     }
