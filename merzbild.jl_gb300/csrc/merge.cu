@@ -1,0 +1,511 @@
+// N:2 octree merging -- merge_octree_N2_based! (merging_octree_N2.jl:1060-1094)
+// with OctreeBinMidSplit, the three initial-bound rules and both bound rules,
+// with or without the 1-D position clamp (compute_new_particles!, :736-933).
+//
+// One warp merges one cell; cells are independent, so a launch covers every
+// selected cell.  The warp keeps the reference's octree exactly:
+//   * the bin to split is the heaviest refinable one, first in bin order on
+//     ties (compute_octree!, :998-1039), found by a warp arg-max;
+//   * split_bin! (:503-633): octants and counts per particle in parallel; the
+//     per-octant weight sums are accumulated sequentially in particle order
+//     (one lane per octant), so bin weights -- which decide later splits --
+//     carry the reference's rounding; children are numbered as the reference
+//     numbers them and the particle list is re-ordered with the reference's
+//     counting sort (which reverses the order inside each octant);
+//   * bin moments (compute_bin_props!, :646-700) are sequential sums, one
+//     lane per bin;
+//   * the k-th bin that holds more than two particles draws its six direction
+//     signs from draws 6k .. 6k+5 of the cell's stream: the reference's
+//     sequential draws in bin order.
+// New particles overwrite the cell's first slots in logical order and the
+// remaining ones are deleted from the end (delete_particle_end!,
+// particles.jl:478-566): group 2 first, then group 1; deleted slots become dead.
+//
+// Each warp works in its own slice of a scratch buffer: the bins, the
+// particle list, the octant of every particle and the new particles.
+#include "mz_host.h"
+
+#include <algorithm>
+
+using namespace mz;
+
+namespace {
+
+enum : int { INIT_MINMAX = 1, INIT_MINMAX_SYM = 2, INIT_C = 3 };
+enum : int { BOUNDS_INHERIT = 1, BOUNDS_RECOMPUTE = 2 };
+
+struct MergeBin {  // OctreeCell (merging_octree_N2.jl:49-59) + its range of the particle list
+    double w;
+    double vmin[3], vmax[3];
+    int32_t np, start, end;  // [start, end] positions in the particle list
+    int32_t depth;
+    int32_t refinable;
+    int32_t pad;
+};
+
+struct MergeArgs {
+    int s;
+    int cb, ce;
+    int64_t threshold;
+    int32_t target;
+    mz_octree_params prm;
+    int clamp;
+    double min_x, max_x;
+    uint32_t step;
+    // per-warp scratch: stride in bytes and offsets of each array
+    char* scratch;
+    size_t stride, off_pis, off_tmp, off_w, off_oct, off_ov, off_ox;
+    int64_t* deleted;  // total particles deleted
+    int64_t* merged;   // cells merged
+};
+
+__device__ __forceinline__ double warp_min(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+// compute_octant (merging_octree_N2.jl:304-316), 0-based
+__device__ __forceinline__ int octant_of(const PV& v, const double* mid)
+{
+    return (v.vx > mid[0] ? 1 : 0) + (v.vy > mid[1] ? 2 : 0) + (v.vz > mid[2] ? 4 : 0);
+}
+
+// bin_bounds_recompute! (:382-418): min / max of the velocities of list[bs, be]
+__device__ __forceinline__ void bounds_of(const Cols& A, const int32_t* pis, int bs, int be, double* mn, double* mx)
+{
+    const int lane = threadIdx.x & 31;
+    double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
+    double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
+    for (int i = bs + lane; i <= be; i += 32) {
+        const PV v = A.wv[pis[i]];
+        lo[0] = fmin(lo[0], v.vx);
+        lo[1] = fmin(lo[1], v.vy);
+        lo[2] = fmin(lo[2], v.vz);
+        hi[0] = fmax(hi[0], v.vx);
+        hi[1] = fmax(hi[1], v.vy);
+        hi[2] = fmax(hi[2], v.vz);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        mn[c] = warp_min(lo[c]);
+        mx[c] = warp_max(hi[c]);
+    }
+}
+
+__device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char* base)
+{
+    const int lane = threadIdx.x & 31;
+    const SpeciesView& S = d.sp[a.s];
+    const Cols& A = S.A;
+    MergeBin* bins = reinterpret_cast<MergeBin*>(base);
+    int32_t* pis = reinterpret_cast<int32_t*>(base + a.off_pis);
+    int32_t* tmp = reinterpret_cast<int32_t*>(base + a.off_tmp);
+    double* wl = reinterpret_cast<double*>(base + a.off_w);
+    uint8_t* oct = reinterpret_cast<uint8_t*>(base + a.off_oct);
+    PV* ov = reinterpret_cast<PV*>(base + a.off_ov);
+    PX* ox = reinterpret_cast<PX*>(base + a.off_ox);
+    const Indexer p = S.ind[c];
+    const int n = p.n1 + p.n2;
+
+    // init_octree! (:947-984)
+    for (int i = lane; i < n; i += 32) pis[i] = map_slot(p, i);
+    __syncwarp();
+    double mn[3], mx[3];
+    if (a.prm.init_bin_bounds == INIT_C) {
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = -299792458.0;
+            mx[k] = 299792458.0;
+        }
+    } else {
+        bounds_of(A, pis, 0, n - 1, mn, mx);
+        if (a.prm.init_bin_bounds == INIT_MINMAX_SYM)
+            for (int k = 0; k < 3; ++k) {
+                const double m = fmax(fabs(mn[k]), fabs(mx[k]));
+                mn[k] = -m;
+                mx[k] = m;
+            }
+    }
+    if (lane == 0) {
+        MergeBin b;
+        b.w = 1e50;
+        for (int k = 0; k < 3; ++k) {
+            b.vmin[k] = mn[k];
+            b.vmax[k] = mx[k];
+        }
+        b.np = n;
+        b.start = 0;
+        b.end = n - 1;
+        b.depth = 0;
+        b.refinable = (n > 2) && (a.prm.max_depth > 0);
+        b.pad = 0;
+        bins[0] = b;
+    }
+    int nbins = 1;
+    int total = n >= 2 ? 2 : n;  // total_post_merge_np
+    __syncwarp();
+
+    // compute_octree! (:998-1039)
+    for (;;) {
+        double bw = -1.0;
+        int bid = -1;
+        for (int b = lane; b < nbins; b += 32) {
+            const MergeBin& B = bins[b];
+            if (B.refinable && B.w > bw) {
+                bw = B.w;
+                bid = b;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
+            const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+            if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
+                bw = w2;
+                bid = id2;
+            }
+        }
+        if (bid < 0) break;
+        if (total + 14 > a.target) break;
+
+        // split_bin! (:503-633)
+        const MergeBin P = bins[bid];
+        const int bs = P.start, be = P.end, nb = be - bs + 1;
+        double vmin[3], vmax[3];
+        for (int k = 0; k < 3; ++k) {
+            vmin[k] = P.vmin[k];
+            vmax[k] = P.vmax[k];
+        }
+        if (a.prm.bin_bounds_compute == BOUNDS_RECOMPUTE) bounds_of(A, pis, bs, be, vmin, vmax);
+        double mid[3];
+        for (int k = 0; k < 3; ++k) mid[k] = 0.5 * (vmin[k] + vmax[k]);
+        int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i = lane; i < nb; i += 32) {
+            const PV v = A.wv[pis[bs + i]];
+            const int o = octant_of(v, mid);
+            oct[i] = (uint8_t)o;
+            wl[i] = v.w;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cnt[k] += (o == k);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cnt[k] = __reduce_add_sync(0xFFFFFFFFu, cnt[k]);
+        __syncwarp();
+        // weight per octant, summed in particle order as the reference does
+        int mine = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (lane == k) mine = cnt[k];
+        double wo = 0.0;
+        if (lane < 8 && mine > 0)
+            for (int i = 0; i < nb; ++i)
+                if (oct[i] == lane) wo += wl[i];
+        // children: non-empty octants in order; the first keeps the bin id
+        int incl[8], run = 0;
+        int nne = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            run += cnt[k];
+            incl[k] = run;
+            nne += cnt[k] > 0;
+        }
+        {
+            int kch = 0, startk = bs;
+            for (int k = 0; k < 8; ++k) {
+                if (cnt[k] == 0) continue;
+                const int id = kch == 0 ? bid : nbins + kch - 1;
+                const double wk = __shfl_sync(0xFFFFFFFFu, wo, k);
+                if (lane == 0) {
+                    MergeBin b;
+                    for (int q = 0; q < 3; ++q) {
+                        const bool upper = (k >> q) & 1;
+                        if (a.prm.bin_bounds_compute == BOUNDS_INHERIT) {
+                            // bin_bounds_inherit! (:341-367)
+                            b.vmin[q] = upper ? mid[q] : P.vmin[q];
+                            b.vmax[q] = upper ? P.vmax[q] : mid[q];
+                        } else {
+                            b.vmin[q] = P.vmin[q];
+                            b.vmax[q] = P.vmax[q];
+                        }
+                    }
+                    b.np = cnt[k];
+                    b.w = wk;
+                    b.depth = P.depth + 1;
+                    b.start = startk;
+                    b.end = startk + cnt[k] - 1;
+                    b.refinable = (cnt[k] > 2) && (b.depth < a.prm.max_depth);
+                    b.pad = 0;
+                    bins[id] = b;
+                }
+                total += cnt[k] >= 2 ? 2 : cnt[k];
+                startk += cnt[k];
+                ++kch;
+            }
+            total -= 2;
+        }
+        // the reference's counting sort: octant k fills [incl[k-1], incl[k])
+        // from its end, in particle order
+        int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i0 = 0; i0 < nb; i0 += 32) {
+            const int i = i0 + lane;
+            const bool in = i < nb;
+            const int o = in ? oct[i] : 8;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, o);
+            int r = __popc(peers & lanemask_lt()), end_o = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (o == k) {
+                    r += seen[k];
+                    end_o = incl[k];
+                }
+            if (in) tmp[end_o - 1 - r] = pis[bs + i];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
+        }
+        __syncwarp();
+        for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
+        nbins += nne - 1;
+        __syncwarp();
+        if (nbins + 7 > a.prm.max_Nbins) break;
+    }
+    if (nbins == 1 && lane == 0) {
+        double w = 0.0;
+        for (int i = 0; i < n; ++i) w += A.wv[pis[i]].w;
+        bins[0].w = w;
+    }
+    __syncwarp();
+
+    // compute_bin_props! (:646-700) and compute_new_particles! (:736-933),
+    // one lane per bin; outputs in bin order
+    int out_base = 0, big_base = 0;
+    Stream st;
+    st.init(cell_seed(d, c), TAG_MERGE, (uint32_t)a.s, cell_step(d, c, a.step), cell_rid(d, c), 0);
+    for (int b0 = 0; b0 < nbins; b0 += 32) {
+        const int b = b0 + lane;
+        MergeBin B;
+        int npe = 0;
+        if (b < nbins) {
+            B = bins[b];
+            npe = B.w == 0.0 ? 0 : B.np;
+        }
+        const int cnt_out = npe >= 2 ? 2 : npe;
+        const int big = npe > 2 ? 1 : 0;
+        int io = cnt_out, ib = big;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t1 = __shfl_up_sync(0xFFFFFFFFu, io, o);
+            const int t2 = __shfl_up_sync(0xFFFFFFFFu, ib, o);
+            if (lane >= o) {
+                io += t1;
+                ib += t2;
+            }
+        }
+        const int pos = out_base + io - cnt_out, kbig = big_base + ib - big;
+        if (npe > 2) {
+            double vm[3] = {0, 0, 0}, xm[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
+            const double inv_w = 1.0 / B.w;
+            for (int i = B.start; i <= B.end; ++i) {
+                const PV v = A.wv[pis[i]];
+                const PX x = A.pos[pis[i]];
+                vm[0] = vm[0] + v.w * v.vx;
+                vm[1] = vm[1] + v.w * v.vy;
+                vm[2] = vm[2] + v.w * v.vz;
+                xm[0] = xm[0] + v.w * x.x;
+                xm[1] = xm[1] + v.w * x.y;
+                xm[2] = xm[2] + v.w * x.z;
+            }
+            for (int k = 0; k < 3; ++k) {
+                vm[k] = vm[k] * inv_w;
+                xm[k] = xm[k] * inv_w;
+            }
+            for (int i = B.start; i <= B.end; ++i) {
+                const PV v = A.wv[pis[i]];
+                const PX x = A.pos[pis[i]];
+                const double dv[3] = {v.vx - vm[0], v.vy - vm[1], v.vz - vm[2]};
+                const double dx[3] = {x.x - xm[0], x.y - xm[1], x.z - xm[2]};
+                for (int k = 0; k < 3; ++k) {
+                    vs[k] = vs[k] + v.w * (dv[k] * dv[k]);
+                    xs[k] = xs[k] + v.w * (dx[k] * dx[k]);
+                }
+            }
+            double sv[3], sx[3];
+            for (int k = 0; k < 3; ++k) {
+                sv[k] = sqrt(vs[k] * inv_w);
+                sx[k] = sqrt(xs[k] * inv_w);
+            }
+            Stream r = st;
+            r.n = 6u * (uint32_t)kbig;
+            double dvs[3], dxs[3];
+            for (int k = 0; k < 3; ++k) dvs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
+            for (int k = 0; k < 3; ++k) dxs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
+            const double w1 = 0.5 * B.w;
+            double x1[3], x2[3];
+            for (int k = 0; k < 3; ++k) {
+                x1[k] = xm[k] + dxs[k] * sx[k];
+                x2[k] = xm[k] - dxs[k] * sx[k];
+            }
+            if (a.clamp) {
+                x1[0] = x1[0] < a.min_x ? a.min_x : (x1[0] > a.max_x ? a.max_x : x1[0]);
+                x2[0] = x2[0] < a.min_x ? a.min_x : (x2[0] > a.max_x ? a.max_x : x2[0]);
+            }
+            ov[pos] = PV{w1, vm[0] + dvs[0] * sv[0], vm[1] + dvs[1] * sv[1], vm[2] + dvs[2] * sv[2]};
+            ov[pos + 1] = PV{w1, vm[0] - dvs[0] * sv[0], vm[1] - dvs[1] * sv[1], vm[2] - dvs[2] * sv[2]};
+            ox[pos] = PX{x1[0], x1[1], x1[2], 0.0};
+            ox[pos + 1] = PX{x2[0], x2[1], x2[2], 0.0};
+        } else if (npe >= 1) {
+            // np == 1 or 2: the bin's particles are kept as they are
+            for (int q = 0; q < npe; ++q) {
+                ov[pos + q] = A.wv[pis[B.start + q]];
+                ox[pos + q] = A.pos[pis[B.start + q]];
+            }
+        }
+        out_base += __shfl_sync(0xFFFFFFFFu, io, 31);
+        big_base += __shfl_sync(0xFFFFFFFFu, ib, 31);
+    }
+    __syncwarp();
+    const int cur = out_base;
+    for (int j = lane; j < cur; j += 32) {
+        const int32_t slot = map_slot(p, j);
+        A.wv[slot] = ov[j];
+        A.pos[slot] = ox[j];
+    }
+    for (int j = cur + lane; j < n; j += 32) {
+        const int32_t slot = map_slot(p, j);
+        A.wv[slot].w = 0.0;
+        S.cell[slot] = -1;
+    }
+    if (lane == 0) {
+        Indexer q = p;
+        if (cur <= p.n1) {
+            q.n1 = cur;
+            q.n2 = 0;
+            q.start2 = 0;
+            if (cur == 0) q.start1 = 0;
+        } else {
+            q.n2 = cur - p.n1;
+        }
+        S.ind[c] = q;
+        if (n > cur) atomicAdd((unsigned long long*)a.deleted, (unsigned long long)(n - cur));
+        atomicAdd((unsigned long long*)a.merged, 1ull);
+        atomicAdd(&d.counters->merges, 1ull);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    char* base = a.scratch + (size_t)warp * a.stride;
+    for (int c = a.cb + warp; c < a.ce; c += nwarps) {
+        const Indexer p = d.sp[a.s].ind[c];
+        const int n = p.n1 + p.n2;
+        if (n == 0 || (a.threshold >= 0 && n <= a.threshold)) continue;
+        merge_cell(d, a, c, base);
+        __syncwarp();
+    }
+}
+
+// largest particle count of the selected cells
+__global__ void k_merge_sizes(DomainView d, int s, int cb, int ce, int64_t threshold, int64_t* out)
+{
+    int best = 0, cnt = 0;
+    for (int c = cb + blockIdx.x * blockDim.x + threadIdx.x; c < ce; c += gridDim.x * blockDim.x) {
+        const Indexer p = d.sp[s].ind[c];
+        const int n = p.n1 + p.n2;
+        if (n > 0 && (threshold < 0 || n > threshold)) {
+            best = max(best, n);
+            ++cnt;
+        }
+    }
+    best = __reduce_max_sync(0xFFFFFFFFu, best);
+    cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax((unsigned long long*)out, (unsigned long long)best);
+        atomicAdd((unsigned long long*)(out + 1), (unsigned long long)cnt);
+    }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
+                  const mz_octree_params* prm, const mz_grid1d* g, uint64_t step, int64_t* n_merged)
+{
+    mz_ctx* c = d->ctx;
+    MZ_REQUIRE(prm->split == 1, "mz_merge_octree_n2: only OctreeBinMidSplit (split = 1) is implemented");
+    MZ_REQUIRE(prm->init_bin_bounds >= 1 && prm->init_bin_bounds <= 3, "mz_merge_octree_n2: bad init_bin_bounds");
+    MZ_REQUIRE(prm->bin_bounds_compute == 1 || prm->bin_bounds_compute == 2,
+               "mz_merge_octree_n2: bad bin_bounds_compute");
+    MZ_REQUIRE(prm->max_Nbins >= 8, "mz_merge_octree_n2: max_Nbins must be at least 8 (one split)");
+    MZ_REQUIRE(target <= (1 << 30), "mz_merge_octree_n2: target_np too large");
+    if (n_merged) *n_merged = 0;
+    if (ce <= cb) return;
+    DomainView v = make_view(d);
+    // sizes of the selected cells decide the scratch per warp
+    MZ_CK(cudaMemsetAsync(d->d_scalar, 0, 4 * sizeof(int64_t), c->stream));
+    const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(ce - cb, 256), (int64_t)c->num_sms * 4));
+    MZ_LAUNCH(c, "merge_sizes", k_merge_sizes, sb, 256, 0, v, s, (int)cb, (int)ce, threshold, d->d_scalar);
+    MZ_CK(cudaMemcpyAsync(d->h_scalar, d->d_scalar, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    MZ_CK(cudaStreamSynchronize(c->stream));
+    const int64_t nmax = d->h_scalar[0], ncells = d->h_scalar[1];
+    if (ncells == 0) return;
+
+    MergeArgs a;
+    memset(&a, 0, sizeof a);
+    a.s = s;
+    a.cb = (int)cb;
+    a.ce = (int)ce;
+    a.threshold = threshold;
+    a.target = (int32_t)target;
+    a.prm = *prm;
+    a.clamp = g != nullptr;
+    if (g) {
+        a.min_x = g->min_x;
+        a.max_x = g->max_x;
+    }
+    a.step = (uint32_t)step;
+    const int64_t outmax = std::max<int64_t>(target, 2);
+    size_t off = align256((size_t)prm->max_Nbins * sizeof(MergeBin));
+    a.off_pis = off;
+    off += align256(nmax * sizeof(int32_t));
+    a.off_tmp = off;
+    off += align256(nmax * sizeof(int32_t));
+    a.off_w = off;
+    off += align256(nmax * sizeof(double));
+    a.off_oct = off;
+    off += align256(nmax);
+    a.off_ov = off;
+    off += align256(outmax * sizeof(PV));
+    a.off_ox = off;
+    off += align256(outmax * sizeof(PX));
+    a.stride = off;
+    const int warps_wanted = (int)std::min<int64_t>(ncells, (int64_t)c->num_sms * 16);
+    const int blocks = (int)std::max<int64_t>(1, div_up(warps_wanted, 8));
+    const size_t need = (size_t)blocks * 8 * a.stride;
+    if (need > d->merge_scratch_bytes) {
+        cudaFree(d->d_merge_scratch);
+        d->d_merge_scratch = nullptr;
+        d->merge_scratch_bytes = 0;
+        MZ_CK(cudaMalloc(&d->d_merge_scratch, need));
+        d->merge_scratch_bytes = need;
+    }
+    a.scratch = static_cast<char*>(d->d_merge_scratch);
+    a.deleted = d->d_scalar + 2;
+    a.merged = d->d_scalar + 3;
+    MZ_LAUNCH(c, "merge", k_merge, blocks, 256, 0, v, a);
+    MZ_CK(cudaMemcpyAsync(d->h_scalar + 2, d->d_scalar + 2, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    MZ_CK(cudaStreamSynchronize(c->stream));
+    SpeciesHost& S = d->sp[s];
+    const int64_t deleted = d->h_scalar[2];
+    S.n_total -= deleted;
+    if (deleted > 0) S.compact = false;
+    if (n_merged) *n_merged = d->h_scalar[3];
+}
