@@ -419,6 +419,7 @@ int mz_domain_destroy(mz_domain* d)
     cudaFree(d->d_merge_scratch);
     cudaFree(d->d_step);
     cudaFree(d->d_done);
+    cudaFree(d->d_hitq);
     cudaFreeHost(d->h_scalar);
     delete d;
     return MZ_OK;

@@ -331,6 +331,7 @@ __device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& 
 
 // ------------------------------------------------------------------ convection
 struct WallView {
+    const double2* trig;  // sector table of sincos_2pi_u52
     double L, min_x, max_x, inv_dx;
     long long bits_L, bits_min, bits_max;  // bit patterns of L, min_x, max_x (positive doubles order like integers)
     double vsq[2][MZ_MAX_SPECIES];
@@ -338,16 +339,16 @@ struct WallView {
     double acc[2];
 };
 
-__device__ __forceinline__ void diffuse_reflect(Stream& st, double& vx, double& vy, double& vz, double vsq,
-                                                double normal, const double* wv)
-{   // diffuse_reflection_x! (boundary_conditions.jl:79-93)
+__device__ __forceinline__ void diffuse_reflect(Stream& st, const double2* trig, double& vx, double& vy, double& vz,
+                                                double vsq, double normal, const double* wv)
+{   // diffuse_reflection_x! (boundary_conditions.jl:79-93); the angle 2 pi rand()
+    // through the scattering's table-driven sine and cosine
     double R = fmax(1e-50, st.uniform());
     const double vn = normal * sqrt(-vsq * log(R));
     R = fmax(1e-50, st.uniform());
     const double vt = sqrt(-vsq * log(R));
-    R = TWOPI * st.uniform();
     double sR, cR;
-    sincos(R, &sR, &cR);
+    sincos_2pi_u52(trig, st.u52(), sR, cR);
     vx = vn + wv[0];
     vy = sR * vt + wv[1];
     vz = cR * vt + wv[2];
@@ -385,10 +386,10 @@ __device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int 
         if (acc == 0.0) {
             vx = -vx;
         } else if (acc == 1.0) {
-            diffuse_reflect(st, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
+            diffuse_reflect(st, W.trig, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
         } else {
             if (st.uniform() < acc)
-                diffuse_reflect(st, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
+                diffuse_reflect(st, W.trig, vx, vy, vz, W.vsq[bc][s], normal, W.wv[bc]);
             else
                 vx = -vx;
         }

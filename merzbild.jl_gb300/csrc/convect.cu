@@ -60,6 +60,7 @@ void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w
     W.min_x = g->min_x;
     W.max_x = g->max_x;
     W.inv_dx = g->inv_dx;
+    W.trig = c->d_trig;
     wall_bits(W);
     for (int b = 0; b < 2; ++b) {
         for (int q = 0; q < MZ_MAX_SPECIES; ++q) W.vsq[b][q] = w->reflection_v_sq[b][q];

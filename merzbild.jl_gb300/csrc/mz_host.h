@@ -100,7 +100,9 @@ struct mz_domain_s {
     std::vector<mz_props*> props;
     // fused step: RNG step index and last-block counter
     uint32_t* d_step = nullptr;
-    unsigned int* d_done = nullptr;
+    unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block}
+    void* d_hitq = nullptr;          // fused step: wall-hit queue (int4 entries)
+    int64_t hitq_cap = 0;
 };
 
 struct mz_props_s {

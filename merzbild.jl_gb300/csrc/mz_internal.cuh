@@ -96,7 +96,9 @@ struct Stream {
             blk = bk;
         }
         ++n;
-        return (uint64_t)buf[2 * e] | ((uint64_t)buf[2 * e + 1] << 32);
+        // constant indices keep buf in registers
+        const uint32_t lo = e ? buf[2] : buf[0], hi = e ? buf[3] : buf[1];
+        return (uint64_t)lo | ((uint64_t)hi << 32);
     }
     // the 52-bit integer m of the next uniform U = m * 2^-52
     __host__ __device__ inline uint64_t u52() { return bits() >> 12; }

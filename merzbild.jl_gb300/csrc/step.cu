@@ -47,6 +47,10 @@ struct StepArgs {
     uint32_t* step_ptr;   // RNG step of the NTC / convection done by this launch
     unsigned int* done;   // last-block counter
     unsigned int* next;   // next cell to hand out (cells are taken CPW at a time)
+    int4* hitq;           // particles that reach a wall: {slot, cell, position in cell, species}
+    unsigned int* hit_n;  // entries in hitq
+    unsigned int* hit_done;  // last-block counter of k_wall_hits
+    unsigned int hitq_cap;
 };
 
 __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const CellMoments& r, int32_t np,
@@ -172,26 +176,47 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                 for (int j0 = 0; j0 < n1; j0 += 32) {
                     const int j = j0 + lane;
                     const bool in = j < n1;
+                    const int64_t qq = (int64_t)st1 + j;
                     int32_t key = 0;
+                    bool counted = false, hit = false;
                     if (in) {
-                        const int64_t qq = (int64_t)st1 + j;
                         double x = Q.pos[qq].x;
-                        double vx = Q.wv[qq].vx;
-                        const double xn = fma(vx, a.dt, x);
-                        if (!move_free(a.W, xn, x)) {
+                        const double xn = fma(Q.wv[qq].vx, a.dt, x);
+                        if (move_free(a.W, xn, x)) {
+                            Q.pos[qq].x = x;
+                            key = cell_of(d, x, a.W.inv_dx);
+                            S.key[qq] = key;
+                            counted = true;
+                        } else {
+                            hit = true;
+                        }
+                    }
+                    // particles that reach a wall finish in k_wall_hits, packed
+                    // into full warps; a full queue falls back to this warp
+                    const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
+                    if (hm) {
+                        const int leader = __ffs(hm) - 1;
+                        unsigned base = 0;
+                        if (lane == leader) base = atomicAdd(a.hit_n, (unsigned)__popc(hm));
+                        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                        const unsigned k = base + __popc(hm & lanemask_lt());
+                        if (hit && k < a.hitq_cap) {
+                            a.hitq[k] = make_int4((int)qq, cq, j, s);
+                        } else if (hit) {
                             Stream rs;
                             rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
                             const PV r = Q.wv[qq];
-                            double vy = r.vy, vz = r.vz;
+                            double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
                             hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
                             Q.wv[qq] = PV{r.w, vx, vy, vz};
+                            Q.pos[qq].x = x;
+                            key = cell_of(d, x, a.W.inv_dx);
+                            S.key[qq] = key;
+                            counted = true;
                         }
-                        Q.pos[qq].x = x;
-                        key = cell_of(d, x, a.W.inv_dx);
-                        S.key[qq] = key;
                     }
-                    const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
-                    if (in) warp_agg_add(S.counts, key, m);
+                    const unsigned m = __ballot_sync(0xFFFFFFFFu, counted);
+                    if (counted) warp_agg_add(S.counts, key, m);
                 }
             }
         }
@@ -217,6 +242,49 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
             *a.done = 0;
             *a.next = 0;
             *a.step_ptr = step + 1;
+            __threadfence();
+        }
+    }
+}
+
+// The wall-hit loop of convect_particles! (convection_1D.jl:22-46) for the
+// particles k_cell queued, one thread each, with the particle's own stream:
+// the same arithmetic and draws as in k_cell, but the FP64 work of diffuse
+// reflections (log, sqrt, sine and cosine) runs on full warps.
+__global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
+{
+    const uint32_t step = *a.step_ptr - 1;  // k_cell advanced it
+    const unsigned n = min(*a.hit_n, a.hitq_cap);
+    unsigned long long hits = 0;
+    bool cap = false;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 h = a.hitq[i];
+        const int64_t qq = h.x;
+        const int c = h.y, j = h.z, s = h.w;
+        const SpeciesView& S = d.sp[s];
+        const Cols& Q = a.gather ? S.B : S.A;
+        Stream rs;
+        rs.init(cell_seed(d, c), TAG_CONVECT, (uint32_t)s, cell_step(d, c, step), cell_rid(d, c), (uint32_t)j);
+        const PV r = Q.wv[qq];
+        double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
+        hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
+        Q.wv[qq] = PV{r.w, vx, vy, vz};
+        Q.pos[qq].x = x;
+        const int32_t key = cell_of(d, x, a.W.inv_dx);
+        S.key[qq] = key;
+        atomicAdd(&S.counts[key], 1);
+    }
+    if (cap) set_status(d, ST_WALL_HITS);
+    hits = __reduce_add_sync(0xFFFFFFFFu, (unsigned)hits);
+    if ((threadIdx.x & 31) == 0 && hits) atomicAdd(&d.counters->wall_hits, hits);
+    // the last block empties the queue for the next step
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(a.hit_done, 1u);
+        if (prev == gridDim.x - 1) {
+            *a.hit_done = 0;
+            *a.hit_n = 0;
             __threadfence();
         }
     }
@@ -248,8 +316,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     for (int s = 0; s < d->ns; ++s) launch_compact(d, s);
     if (!d->d_step) {
         MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
-        MZ_CK(cudaMalloc(&d->d_done, 2 * sizeof(unsigned int)));
-        MZ_CK(cudaMemsetAsync(d->d_done, 0, 2 * sizeof(unsigned int), c->stream));
+        MZ_CK(cudaMalloc(&d->d_done, 4 * sizeof(unsigned int)));
+        MZ_CK(cudaMemsetAsync(d->d_done, 0, 4 * sizeof(unsigned int), c->stream));
     }
     const uint32_t first = (uint32_t)(plan->step0 + 1);
     MZ_CK(cudaMemcpyAsync(d->d_step, &first, sizeof first, cudaMemcpyHostToDevice, c->stream));
@@ -260,6 +328,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.W.min_x = plan->grid.min_x;
     a.W.max_x = plan->grid.max_x;
     a.W.inv_dx = plan->grid.inv_dx;
+    a.W.trig = c->d_trig;
     wall_bits(a.W);
     for (int b = 0; b < 2; ++b) {
         for (int q = 0; q < MZ_MAX_SPECIES; ++q) a.W.vsq[b][q] = plan->walls.reflection_v_sq[b][q];
@@ -279,6 +348,23 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.step_ptr = d->d_step;
     a.done = d->d_done;
     a.next = d->d_done + 1;
+    a.hit_n = d->d_done + 2;
+    a.hit_done = d->d_done + 3;
+    {
+        // wall-hit queue: a fraction of the particles; overflow is handled inline
+        int64_t n_all = 0;
+        for (int s = 0; s < d->ns; ++s) n_all += d->sp[s].n_total;
+        const int64_t want = std::max<int64_t>(4096, n_all / 16);
+        if (want > d->hitq_cap) {
+            cudaFree(d->d_hitq);
+            d->d_hitq = nullptr;
+            d->hitq_cap = 0;
+            MZ_CK(cudaMalloc(&d->d_hitq, want * sizeof(int4)));
+            d->hitq_cap = want;
+        }
+        a.hitq = static_cast<int4*>(d->d_hitq);
+        a.hitq_cap = (unsigned)std::min<int64_t>(d->hitq_cap, 0x7FFFFFFF);
+    }
     const bool want_props = plan->props && (inst || a.has_avg);
     const int G = ntc_group_width(d->n_cells);
     void (*kern)(DomainView, StepArgs) = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
@@ -297,6 +383,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
         MZ_LAUNCH(c, name, kern, blocks, 256, 0, v, b);
+        if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
     };
     // one sort of every species from the keys k_cell wrote, gather in k_cell
     auto sort_launch = [&](int props, int physics) {

@@ -1,0 +1,335 @@
+"""
+    MerzbildGPU
+
+Julia binding of libmerzgpu.so (include/merzgpu.h): the per-step DSMC path of
+Merzbild.jl (NTC collisions, 1-D convection, grid sorting, cell properties,
+octree merging, sampling) on a GB300 GPU.
+
+The module adds methods to Merzbild's own functions for a device-resident
+particle type, so a time loop written against Merzbild keeps its calls and
+swaps its particle containers:
+
+    ctx = DeviceContext(0)
+    dp  = DeviceParticles(ctx, n_cells, species_data, interactions, capacity)
+    for t in 1:n_timesteps
+        rng.step = t
+        ntc_equal_weight!(rng, dp, (1, n_cells), 1, Δt)
+        convect_particles!(rng, grid, walls, dp, 1, Δt)
+        sort_particles!(grid, dp, 1)
+        compute_props_sorted!(dp, props)
+    end
+
+Conventions at the boundary: the C ABI is 0-based (cells, slots); this
+module takes and returns Merzbild's 1-based cells.  Random numbers come from
+counter-based streams keyed on (seed, step, cell, particle), so `DeviceRNG`
+carries a seed and the time-step index instead of a generator state.
+"""
+module MerzbildGPU
+
+export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, DeviceWalls1D, DeviceOctree,
+       upload!, download, ntc!, ntc_equal_weight!, convect_particles!, convect_particles_and_compute_cell!,
+       sort_particles!, squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
+       avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters
+
+const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
+const MZ_MAX_SPECIES = 4
+const MZ_NTC_EQUAL_WEIGHT = Int32(1)
+const MZ_CONVECT_COMPUTE_CELL = Int32(1)
+const MZ_PROPS_ALL, MZ_PROPS_MOMENTS, MZ_PROPS_SORTED = Int32(0), Int32(1), Int32(2)
+
+# ------------------------------------------------------------------ C structs
+struct MzInteraction          # Interaction (collision_utils.jl:73-82)
+    m_r::Float64; μ1::Float64; μ2::Float64; vhs_d::Float64; vhs_o::Float64
+    vhs_Tref::Float64; vhs_muref::Float64; vhs_factor::Float64
+end
+
+struct MzParticleIndexer      # ParticleIndexer, 0-based slots
+    n_local::Int64; start1::Int64; end1::Int64; n_group1::Int64
+    start2::Int64; end2::Int64; n_group2::Int64
+end
+
+struct MzCollisionFactors
+    n1::Int64; n2::Int64; sigma_g_w_max::Float64
+    n_coll::Int64; n_coll_performed::Int64; n_eq_w_coll_performed::Int64
+end
+
+struct DeviceGrid1D           # Grid1DUniform (grid_uniform1D.jl:49-86)
+    L::Float64; n_cells::Int64; dx::Float64; inv_dx::Float64; min_x::Float64; max_x::Float64
+end
+DeviceGrid1D(grid) = DeviceGrid1D(grid.L, grid.n_cells, grid.Δx, grid.inv_Δx, grid.min_x, grid.max_x)
+
+struct DeviceWalls1D          # MaxwellWalls1D (boundary_conditions.jl:29-53), left then right
+    T::NTuple{2,Float64}
+    v::NTuple{6,Float64}
+    accommodation::NTuple{2,Float64}
+    reflection_v_sq::NTuple{2 * MZ_MAX_SPECIES,Float64}
+end
+function DeviceWalls1D(walls)
+    ns = size(walls.reflection_velocities_sq, 2)   # (wall, species)
+    vsq = ntuple(i -> begin
+                     w, s = divrem(i - 1, MZ_MAX_SPECIES)
+                     s < ns ? walls.reflection_velocities_sq[w + 1, s + 1] : 0.0
+                 end, 2 * MZ_MAX_SPECIES)
+    DeviceWalls1D((walls.boundaries[1].T, walls.boundaries[2].T),
+                  (walls.boundaries[1].v..., walls.boundaries[2].v...),
+                  (walls.boundaries[1].accommodation, walls.boundaries[2].accommodation), vsq)
+end
+
+struct DeviceOctree           # OctreeN2Merge options (merging_octree_N2.jl:235-246)
+    split::Int32; init_bin_bounds::Int32; bin_bounds_compute::Int32; max_Nbins::Int32; max_depth::Int32
+end
+DeviceOctree(; init_bin_bounds=1, bin_bounds_compute=1, max_Nbins=4096, max_depth=10) =
+    DeviceOctree(1, init_bin_bounds, bin_bounds_compute, max_Nbins, max_depth)
+
+struct MzCounters
+    candidates::UInt64; accepted::UInt64; splits::UInt64; merges::UInt64; wall_hits::UInt64
+end
+
+struct MzStepPlan
+    dims::Int32; collide::Int32; equal_weight::Int32; props::Int32
+    avg_start::Int64; n_avg::Int64; dt::Float64; dw_tol::Float64; step0::UInt64
+    use_graph::Int32; reserved::Int32
+    grid::DeviceGrid1D; walls::DeviceWalls1D
+end
+
+# ------------------------------------------------------------------ handles
+mutable struct DeviceContext
+    ptr::Ptr{Cvoid}
+    function DeviceContext(device::Integer=0)
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:mz_ctx_create, libmz), Cint, (Cint, Ref{Ptr{Cvoid}}), device, r), C_NULL)
+        c = new(r[])
+        finalizer(c -> ccall((:mz_ctx_destroy, libmz), Cint, (Ptr{Cvoid},), c.ptr), c)
+        c
+    end
+end
+
+mutable struct DeviceParticles
+    ctx::DeviceContext
+    ptr::Ptr{Cvoid}
+    n_cells::Int
+    n_species::Int
+end
+
+"""
+    DeviceParticles(ctx, n_cells, species_data, interactions, capacity; seed=1234)
+
+Device counterpart of `particles::Vector{ParticleVector}`, `pia` and the
+collision factors of all species pairs.
+"""
+function DeviceParticles(ctx::DeviceContext, n_cells, species_data, interactions, capacity; seed=1234)
+    ns = length(species_data)
+    cap = fill(Int64(capacity), ns)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mz_domain_create, libmz), Cint, (Ptr{Cvoid}, Int64, Int32, Ptr{Int64}, Ref{Ptr{Cvoid}}),
+                ctx.ptr, n_cells, ns, cap, r), ctx)
+    dp = DeviceParticles(ctx, r[], n_cells, ns)
+    finalizer(d -> ccall((:mz_domain_destroy, libmz), Cint, (Ptr{Cvoid},), d.ptr), dp)
+    check(ccall((:mz_set_species, libmz), Cint, (Ptr{Cvoid}, Ptr{Float64}), dp.ptr, [s.mass for s in species_data]), ctx)
+    tab = [MzInteraction(interactions[s1, s2].m_r, interactions[s1, s2].μ1, interactions[s1, s2].μ2,
+                         interactions[s1, s2].vhs_d, interactions[s1, s2].vhs_o, interactions[s1, s2].vhs_Tref,
+                         interactions[s1, s2].vhs_muref, interactions[s1, s2].vhs_factor) for s1 in 1:ns, s2 in 1:ns]
+    check(ccall((:mz_set_interactions, libmz), Cint, (Ptr{Cvoid}, Ptr{MzInteraction}), dp.ptr, tab), ctx)
+    check(ccall((:mz_set_seed, libmz), Cint, (Ptr{Cvoid}, UInt64), dp.ptr, seed), ctx)
+    dp
+end
+
+mutable struct DeviceProps
+    dp::DeviceParticles
+    ptr::Ptr{Cvoid}
+    n_moments::Int
+end
+
+"""
+    DeviceProps(dp; moments_list=Int32[], Tref=300.0, ndens_not_Np=false)
+
+Device counterpart of `PhysProps` (physical_props.jl:24-58); `fetch!` copies
+into a `PhysProps`.
+"""
+function DeviceProps(dp::DeviceParticles; moments_list=Int32[], Tref=300.0, ndens_not_Np=false)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    m = Int32.(moments_list)
+    check(ccall((:mz_props_create, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{Int32}, Float64, Int32, Ref{Ptr{Cvoid}}),
+                dp.ptr, length(m), m, Tref, ndens_not_Np ? 1 : 0, r), dp.ctx)
+    p = DeviceProps(dp, r[], length(m))
+    finalizer(q -> ccall((:mz_props_destroy, libmz), Cint, (Ptr{Cvoid},), q.ptr), p)
+    p
+end
+
+"""Seed and time-step index of the counter-based streams (replaces `rng`)."""
+mutable struct DeviceRNG
+    seed::UInt64
+    step::UInt64
+end
+DeviceRNG(seed::Integer) = DeviceRNG(UInt64(seed), UInt64(0))
+
+function check(rc, ctx)
+    rc == 0 && return nothing
+    msg = ""
+    cp = ctx isa DeviceContext ? ctx.ptr : ctx
+    if cp != C_NULL
+        buf = Vector{UInt8}(undef, 1024)
+        ccall((:mz_last_error, libmz), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), cp, buf, length(buf))
+        msg = unsafe_string(pointer(buf))
+    end
+    throw(ErrorException("merzgpu error $rc: $msg"))
+end
+
+cellrange(cell::Integer) = (Int64(cell - 1), Int64(cell))
+cellrange(cells::Tuple) = (Int64(cells[1] - 1), Int64(cells[2]))
+
+# ------------------------------------------------------------------ particles
+"""Load particles of `species` (w, v as 3×n, x as 3×n, 1-based cells)."""
+function upload!(dp::DeviceParticles, species, w::Vector{Float64}, v::Matrix{Float64}, x::Matrix{Float64},
+                 cells::Vector{<:Integer})
+    c0 = Int32.(cells .- 1)
+    check(ccall((:mz_upload_particles, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
+                dp.ptr, species - 1, length(w), w, v, x, c0), dp.ctx)
+end
+
+"""Particles of `species` in logical order: (w, v 3×n, x 3×n, 1-based cells)."""
+function download(dp::DeviceParticles, species)
+    n = Ref{Int64}(0)
+    check(ccall((:mz_get_indexer, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{MzParticleIndexer}, Ref{Int64}),
+                dp.ptr, species - 1, C_NULL, n), dp.ctx)
+    w = Vector{Float64}(undef, n[]); v = Matrix{Float64}(undef, 3, n[]); x = Matrix{Float64}(undef, 3, n[])
+    cells = Vector{Int32}(undef, n[])
+    check(ccall((:mz_download_particles, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ref{Int64}),
+                dp.ptr, species - 1, n[], w, v, x, cells, n), dp.ctx)
+    w, v, x, cells .+ 1
+end
+
+# ------------------------------------------------------------------ collisions
+"""ntc! (collision_ntc.jl:338, :412) for one cell or a range (first, last) of cells."""
+function ntc!(rng::DeviceRNG, dp::DeviceParticles, cell, species1, species2, Δt; dw_tol=1e-16)
+    cb, ce = cellrange(cell)
+    check(ccall((:mz_ntc, libmz), Cint, (Ptr{Cvoid}, Int32, Int32, Float64, Int64, Int64, UInt64, Int32, Float64),
+                dp.ptr, species1 - 1, species2 - 1, Δt, cb, ce, rng.step, 0, dw_tol), dp.ctx)
+end
+ntc!(rng::DeviceRNG, dp::DeviceParticles, cell, species, Δt; dw_tol=1e-16) =
+    ntc!(rng, dp, cell, species, species, Δt; dw_tol=dw_tol)
+
+"""ntc_equal_weight! (collision_ntc.jl:479, :554)."""
+function ntc_equal_weight!(rng::DeviceRNG, dp::DeviceParticles, cell, species1, species2, Δt)
+    cb, ce = cellrange(cell)
+    check(ccall((:mz_ntc, libmz), Cint, (Ptr{Cvoid}, Int32, Int32, Float64, Int64, Int64, UInt64, Int32, Float64),
+                dp.ptr, species1 - 1, species2 - 1, Δt, cb, ce, rng.step, MZ_NTC_EQUAL_WEIGHT, 1e-16), dp.ctx)
+end
+ntc_equal_weight!(rng::DeviceRNG, dp::DeviceParticles, cell, species, Δt) =
+    ntc_equal_weight!(rng, dp, cell, species, species, Δt)
+
+"""Set (σ g w)_max of a species pair for every cell (create_collision_factors_array)."""
+function set_sigma_g_w_max!(dp::DeviceParticles, species1, species2, values::Vector{Float64})
+    check(ccall((:mz_set_collision_factors, libmz), Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}),
+                dp.ptr, species1 - 1, species2 - 1, values), dp.ctx)
+end
+
+set_cell_volumes!(dp::DeviceParticles, V::Vector{Float64}) =
+    check(ccall((:mz_set_cell_volumes, libmz), Cint, (Ptr{Cvoid}, Ptr{Float64}), dp.ptr, V), dp.ctx)
+
+# ------------------------------------------------------------------ convection and sorting
+"""convect_particles! (convection_1D.jl:130-157)."""
+convect_particles!(rng::DeviceRNG, grid::DeviceGrid1D, walls::DeviceWalls1D, dp::DeviceParticles, species, Δt) =
+    check(ccall((:mz_convect_1d, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ref{DeviceWalls1D}, Float64, UInt64, Int32),
+                dp.ptr, species - 1, grid, walls, Δt, rng.step, 0), dp.ctx)
+
+"""convect_particles_and_compute_cell! (convection_1D.jl:225-255)."""
+convect_particles_and_compute_cell!(rng::DeviceRNG, grid::DeviceGrid1D, walls::DeviceWalls1D, dp::DeviceParticles,
+                                    species, Δt) =
+    check(ccall((:mz_convect_1d, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ref{DeviceWalls1D}, Float64, UInt64, Int32),
+                dp.ptr, species - 1, grid, walls, Δt, rng.step, MZ_CONVECT_COMPUTE_CELL), dp.ctx)
+
+"""sort_particles! with cells from positions (grid_sorting.jl:58-113)."""
+sort_particles!(grid::DeviceGrid1D, dp::DeviceParticles, species) =
+    check(ccall((:mz_sort, libmz), Cint, (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ptr{Int64}),
+                dp.ptr, species - 1, grid, C_NULL), dp.ctx)
+
+"""sort_particles! with cells stored by convection (grid_sorting.jl:128-182)."""
+sort_particles!(dp::DeviceParticles, species) =
+    check(ccall((:mz_sort, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{DeviceGrid1D}, Ptr{Int64}),
+                dp.ptr, species - 1, C_NULL, C_NULL), dp.ctx)
+
+"""squash_pia! (particles.jl:622-701)."""
+squash_pia!(dp::DeviceParticles, species) =
+    check(ccall((:mz_squash, libmz), Cint, (Ptr{Cvoid}, Int32), dp.ptr, species - 1), dp.ctx)
+
+# ------------------------------------------------------------------ properties
+compute_props!(dp::DeviceParticles, p::DeviceProps) =
+    check(ccall((:mz_compute_props, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Int32), dp.ptr, p.ptr, MZ_PROPS_ALL), dp.ctx)
+compute_props_sorted!(dp::DeviceParticles, p::DeviceProps) =
+    check(ccall((:mz_compute_props, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Int32), dp.ptr, p.ptr, MZ_PROPS_SORTED),
+          dp.ctx)
+compute_props_with_total_moments!(dp::DeviceParticles, p::DeviceProps) =
+    check(ccall((:mz_compute_props, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Int32), dp.ptr, p.ptr, MZ_PROPS_MOMENTS),
+          dp.ctx)
+avg_props!(avg::DeviceProps, inst::DeviceProps, n_avg_timesteps) =
+    check(ccall((:mz_avg_props, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64), avg.ptr, inst.ptr, n_avg_timesteps),
+          avg.dp.ctx)
+clear_props!(p::DeviceProps) = check(ccall((:mz_clear_props, libmz), Cint, (Ptr{Cvoid},), p.ptr), p.dp.ctx)
+
+"""Copy device properties into a Merzbild `PhysProps` (same array layouts)."""
+function fetch!(phys_props, p::DeviceProps)
+    lpa = Vector{Float64}(undef, p.dp.n_species)
+    mom = p.n_moments > 0 ? phys_props.moments : C_NULL
+    check(ccall((:mz_props_download, libmz), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                p.ptr, lpa, phys_props.np, phys_props.n, phys_props.v, phys_props.T, mom), p.dp.ctx)
+    phys_props.lpa .= lpa
+    phys_props
+end
+
+# ------------------------------------------------------------------ merging and sampling
+"""merge_octree_N2_based! (merging_octree_N2.jl:1060, :1088) for a cell or a
+range of cells; `threshold` merges only cells with more particles."""
+function merge_octree_N2_based!(rng::DeviceRNG, octree::DeviceOctree, dp::DeviceParticles, cell, species, target_np;
+                                grid::Union{Nothing,DeviceGrid1D}=nothing, threshold=-1)
+    cb, ce = cellrange(cell)
+    n = Ref{Int64}(0)
+    if grid === nothing
+        check(ccall((:mz_merge_octree_n2, libmz), Cint,
+                    (Ptr{Cvoid}, Int32, Int64, Int64, Int64, Int64, Ref{DeviceOctree}, Ptr{DeviceGrid1D}, UInt64,
+                     Ref{Int64}), dp.ptr, species - 1, cb, ce, threshold, target_np, octree, C_NULL, rng.step, n),
+              dp.ctx)
+    else
+        check(ccall((:mz_merge_octree_n2, libmz), Cint,
+                    (Ptr{Cvoid}, Int32, Int64, Int64, Int64, Int64, Ref{DeviceOctree}, Ref{DeviceGrid1D}, UInt64,
+                     Ref{Int64}), dp.ptr, species - 1, cb, ce, threshold, target_np, octree, grid, rng.step, n),
+              dp.ctx)
+    end
+    n[]
+end
+
+"""sample_particles_equal_weight!(rng, grid, ..., ndens, T, Fnum) (grid_uniform1D.jl:198-219)."""
+sample_particles_equal_weight!(rng::DeviceRNG, grid::DeviceGrid1D, dp::DeviceParticles, species, ndens, T, Fnum) =
+    check(ccall((:mz_sample_grid_ndens, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Float64, Float64, Float64, UInt64),
+                dp.ptr, species - 1, grid, ndens, T, Fnum, rng.step), dp.ctx)
+
+# ------------------------------------------------------------------ fused steps
+"""
+    step!(dp, n_steps; grid, walls, Δt, step0, inst, avg, avg_start, n_avg)
+
+`n_steps` fused steps (ntc_equal_weight! -> convect -> sort -> props ->
+avg_props!), replayed from a CUDA graph: the loop body of
+simulations/1D/couette_benchmarking.jl:58-85 in one call.
+"""
+function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D, walls::DeviceWalls1D, Δt, step0=0,
+               inst::Union{Nothing,DeviceProps}=nothing, avg::Union{Nothing,DeviceProps}=nothing,
+               avg_start=0, n_avg=1, dims=1)
+    plan = MzStepPlan(dims, 1, 1, 1, avg_start, n_avg, Δt, 1e-16, step0, 1, 0, grid, walls)
+    check(ccall((:mz_step, libmz), Cint, (Ptr{Cvoid}, Ref{MzStepPlan}, Int64, Ptr{Cvoid}, Ptr{Cvoid}),
+                dp.ptr, plan, n_steps, inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr),
+          dp.ctx)
+end
+
+function counters(dp::DeviceParticles; reset=false)
+    c = Ref{MzCounters}()
+    check(ccall((:mz_get_counters, libmz), Cint, (Ptr{Cvoid}, Ref{MzCounters}, Int32), dp.ptr, c, reset), dp.ctx)
+    c[]
+end
+
+end # module
