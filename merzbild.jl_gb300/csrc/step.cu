@@ -53,6 +53,10 @@ struct StepArgs {
     unsigned int hitq_cap;
 };
 
+// cells of the per-warp destination histogram of k_cell (48 KB per block)
+constexpr int CELL_WINDOW = 1536;
+constexpr size_t CELL_SMEM = (size_t)8 * CELL_WINDOW * sizeof(int32_t);
+
 __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const CellMoments& r, int32_t np,
                                             uint32_t step)
 {
@@ -84,8 +88,12 @@ template <int G>
 __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
 {
     constexpr int CPW = 32 / G;
+    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
     const uint32_t step = *a.step_ptr;
     const int lane = threadIdx.x & 31;
+    int32_t* wh = cell_hist + (threadIdx.x >> 5) * CELL_WINDOW;
+    for (int bin = lane; bin < CELL_WINDOW; bin += 32) wh[bin] = 0;
+    __syncwarp();
     const WarpGroup<G> grp;
     const int gi = lane / G;
     const int ns = d.n_species;
@@ -153,10 +161,10 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
             }
         }
         __syncwarp();
-        for (int q = 0; q < nq; ++q) {
-            const int cq = c0 + q;
-            // 0-D: compute_props! after the collisions of this step
-            if (a.props && a.props_lag == 0) {
+        // 0-D: compute_props! after the collisions of this step
+        if (a.props && a.props_lag == 0) {
+            for (int q = 0; q < nq; ++q) {
+                const int cq = c0 + q;
                 for (int s = 0; s < ns; ++s) {
                     const SpeciesView& S = d.sp[s];
                     const Indexer p = S.ind[cq];
@@ -164,13 +172,20 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                     if (lane == 0) write_props(a, (int64_t)cq + (int64_t)d.n_cells * s, r, p.n1, step);
                 }
             }
-            if (a.dims != 1 || !a.physics) continue;
-            // convect_particles! + get_cell for the next sort
-            const uint64_t seed = cell_seed(d, cq);
-            const uint32_t rid = cell_rid(d, cq), stp = cell_step(d, cq, step);
-            for (int s = 0; s < ns; ++s) {
-                const SpeciesView& S = d.sp[s];
-                const Cols& Q = a.gather ? S.B : S.A;
+        }
+        if (a.dims != 1 || !a.physics) continue;
+        // convect_particles! + get_cell for the next sort.  Destination counts
+        // go to a per-warp histogram over a window of cells around the warp's
+        // cells, flushed with one atomic per non-empty cell (consecutive
+        // addresses); destinations outside the window count directly.
+        const int kb = c0 + CPW / 2 - CELL_WINDOW / 2;
+        for (int s = 0; s < ns; ++s) {
+            const SpeciesView& S = d.sp[s];
+            const Cols& Q = a.gather ? S.B : S.A;
+            for (int q = 0; q < nq; ++q) {
+                const int cq = c0 + q;
+                const uint64_t seed = cell_seed(d, cq);
+                const uint32_t rid = cell_rid(d, cq), stp = cell_step(d, cq, step);
                 const Indexer p = S.ind[cq];
                 const int32_t n1 = p.n1, st1 = p.start1;
                 for (int j0 = 0; j0 < n1; j0 += 32) {
@@ -215,10 +230,24 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                             counted = true;
                         }
                     }
-                    const unsigned m = __ballot_sync(0xFFFFFFFFu, counted);
-                    if (counted) warp_agg_add(S.counts, key, m);
+                    if (counted) {
+                        const int bin = key - kb;
+                        if ((unsigned)bin < (unsigned)CELL_WINDOW)
+                            atomicAdd(&wh[bin], 1);
+                        else
+                            atomicAdd(&S.counts[key], 1);
+                    }
                 }
             }
+            __syncwarp();
+            for (int bin = lane; bin < CELL_WINDOW; bin += 32) {
+                const int v = wh[bin];
+                if (v) {
+                    atomicAdd(&S.counts[kb + bin], v);
+                    wh[bin] = 0;
+                }
+            }
+            __syncwarp();
         }
     }
     if (cap) set_status(d, ST_WALL_HITS);
@@ -290,19 +319,53 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
     }
 }
 
-__global__ void __launch_bounds__(256) k_step_scatter(DomainView d, int s, int64_t n)
+// Tickets of the counting sort: each block takes tiles of SCATTER_TILE
+// consecutive slots; slots whose destination lies within SCATTER_WINDOW cells
+// of the tile's middle cell take a rank from a shared-memory histogram, and
+// each non-empty destination then reserves its run of the cell's segment
+// with one global atomic (consecutive addresses).  Other slots take a ticket
+// directly.  The order inside a segment is arbitrary; k_cell sorts it.
+constexpr int SCATTER_TILE = 2048, SCATTER_WINDOW = 2048;
+
+__global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, int64_t n)
 {
+    __shared__ int32_t hist[SCATTER_WINDOW];
+    constexpr int PER = SCATTER_TILE / 256;
     const SpeciesView& S = d.sp[s];
-    const int lane = threadIdx.x & 31;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
-        const int64_t slot = base + lane;
-        const bool in = slot < n;
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
-        if (!in) continue;
-        const int32_t key = S.key[slot];
-        const int32_t pos = S.ind[key].start1 + warp_agg_ticket(S.fill, key, m);
-        S.idx[pos] = (int32_t)slot;
+    for (int64_t t0 = (int64_t)blockIdx.x * SCATTER_TILE; t0 < n; t0 += (int64_t)gridDim.x * SCATTER_TILE) {
+        const int64_t t1 = min(n, t0 + (int64_t)SCATTER_TILE);
+        const int32_t cmid = S.cell[(t0 + t1 - 1) / 2];
+        const int kb = (cmid >= 0 ? cmid : S.key[(t0 + t1 - 1) / 2]) - SCATTER_WINDOW / 2;
+        for (int b = threadIdx.x; b < SCATTER_WINDOW; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        int32_t key[PER], rank[PER];
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const int64_t slot = t0 + threadIdx.x + 256 * r;
+            rank[r] = -1;
+            key[r] = 0;
+            if (slot < t1) {
+                const int32_t k = S.key[slot];
+                key[r] = k;
+                const int b = k - kb;
+                if ((unsigned)b < (unsigned)SCATTER_WINDOW) {
+                    rank[r] = atomicAdd(&hist[b], 1);
+                } else {
+                    const int32_t pos = S.ind[k].start1 + atomicAdd(&S.fill[k], 1);
+                    S.idx[pos] = (int32_t)slot;
+                }
+            }
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < SCATTER_WINDOW; b += blockDim.x) {
+            const int cnt = hist[b];
+            if (cnt) hist[b] = S.ind[kb + b].start1 + atomicAdd(&S.fill[kb + b], cnt);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PER; ++r)
+            if (rank[r] >= 0) S.idx[hist[key[r] - kb] + rank[r]] = (int32_t)(t0 + threadIdx.x + 256 * r);
+        __syncthreads();
     }
 }
 
@@ -369,7 +432,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     const int G = ntc_group_width(d->n_cells);
     void (*kern)(DomainView, StepArgs) = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
     int per_sm = 0;
-    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, CELL_SMEM));
     const int blocks = (int)std::max<int64_t>(
         1, std::min<int64_t>(div_up(d->n_cells, 8 * (32 / G)), (int64_t)c->num_sms * std::max(per_sm, 1)));
 
@@ -382,7 +445,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
-        MZ_LAUNCH(c, name, kern, blocks, 256, 0, v, b);
+        MZ_LAUNCH(c, name, kern, blocks, 256, CELL_SMEM, v, b);
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
     };
     // one sort of every species from the keys k_cell wrote, gather in k_cell
@@ -391,7 +454,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         for (int s = 0; s < d->ns; ++s) {
             SpeciesHost& S = d->sp[s];
             launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar + s, true, nullptr, 0);
-            const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, 256), (int64_t)c->num_sms * 8));
+            const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, SCATTER_TILE), (int64_t)c->num_sms * 8));
             MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total);
         }
         cell_launch(1, props, physics);
