@@ -329,6 +329,94 @@ __device__ __forceinline__ CellMoments props_cell(const Cols& P, const Indexer& 
     return r;
 }
 
+// Sums of four quantities over the warp in 6 additions instead of 20: the
+// halves exchange two quantities, then quarters one, then a butterfly.
+// Returns, in lanes 8q .. 8q+7, the warp total of a_q.
+__device__ __forceinline__ double warp_sum4(double a0, double a1, double a2, double a3)
+{
+    const int lane = threadIdx.x & 31;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    const double b0 = (h16 ? a2 : a0) + __shfl_xor_sync(0xFFFFFFFFu, h16 ? a0 : a2, 16);
+    const double b1 = (h16 ? a3 : a1) + __shfl_xor_sync(0xFFFFFFFFu, h16 ? a1 : a3, 16);
+    double c = (h8 ? b1 : b0) + __shfl_xor_sync(0xFFFFFFFFu, h8 ? b0 : b1, 8);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 4);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
+    return c;
+}
+
+// n, u, T of the group-1 lists of cells c0 .. c0 + nq - 1 (nq <= 32) of one
+// species, one warp (compute_props_sorted!, physical_props.jl:317-354, and
+// compute_props! for lists without group 2).  The same two passes as
+// props_cell for every cell; the divisions and the final scaling run once for
+// all nq cells, lane q finishing cell c0 + q, which returns its moments.
+// props_cells_finish takes the first-pass sums of cell c0 + q in lane q (from
+// props_pass1_into_lane, or from the sort's gather, which accumulates them in
+// the same order) and runs the second pass.
+__device__ __forceinline__ void props_pass1_into_lane(double n, double sx, double sy, double sz, int q, double& mn,
+                                                      double& msx, double& msy, double& msz)
+{
+    const int lane = threadIdx.x & 31;
+    const double t = warp_sum4(n, sx, sy, sz);
+    const double tn = __shfl_sync(0xFFFFFFFFu, t, 0), tx = __shfl_sync(0xFFFFFFFFu, t, 8);
+    const double ty = __shfl_sync(0xFFFFFFFFu, t, 16), tz = __shfl_sync(0xFFFFFFFFu, t, 24);
+    if (lane == q) {
+        mn = tn;
+        msx = tx;
+        msy = ty;
+        msz = tz;
+    }
+}
+
+__device__ __forceinline__ CellMoments props_cells_finish(const Cols& P, const Indexer* ind, int c0, int nq,
+                                                          double mass, double mn, double msx, double msy, double msz)
+{
+    const int lane = threadIdx.x & 31;
+    CellMoments r;
+    r.n = mn;
+    r.ux = r.uy = r.uz = r.T = 0.0;
+    if (lane < nq && mn > 0.0) {
+        r.ux = msx / mn;
+        r.uy = msy / mn;
+        r.uz = msz / mn;
+    }
+    double mE = 0.0;
+    for (int q = 0; q < nq; ++q) {
+        const Indexer p = ind[c0 + q];
+        const double ux = __shfl_sync(0xFFFFFFFFu, r.ux, q), uy = __shfl_sync(0xFFFFFFFFu, r.uy, q);
+        const double uz = __shfl_sync(0xFFFFFFFFu, r.uz, q);
+        double E = 0.0;
+        for (int j = lane; j < p.n1; j += 32) {
+            const PV u = P.wv[p.start1 + j];
+            const double dx = u.vx - ux, dy = u.vy - uy, dz = u.vz - uz;
+            E = fma(u.w, (dx * dx + dy * dy) + dz * dz, E);
+        }
+        E = warp_sum(E);
+        if (lane == q) mE = E;
+    }
+    if (lane < nq && mn > 0.0) r.T = (2.0 / 3.0) * (mE * (0.5 * mass / (mn * K_B)));
+    return r;
+}
+
+__device__ __forceinline__ CellMoments props_cells(const Cols& P, const Indexer* ind, int c0, int nq, double mass)
+{
+    const int lane = threadIdx.x & 31;
+    double mn = 0.0, msx = 0.0, msy = 0.0, msz = 0.0;
+    for (int q = 0; q < nq; ++q) {
+        const Indexer p = ind[c0 + q];
+        double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int j = lane; j < p.n1; j += 32) {
+            const PV r = P.wv[p.start1 + j];
+            n += r.w;
+            sx += r.vx * r.w;
+            sy += r.vy * r.w;
+            sz += r.vz * r.w;
+        }
+        props_pass1_into_lane(n, sx, sy, sz, q, mn, msx, msy, msz);
+    }
+    return props_cells_finish(P, ind, c0, nq, mass, mn, msx, msy, msz);
+}
+
 // ------------------------------------------------------------------ convection
 struct WallView {
     const double2* trig;  // sector table of sincos_2pi_u52

@@ -85,9 +85,15 @@ __device__ __forceinline__ void copy_particle(const Cols& A, const Cols& B, int3
 // stores: the gather is bound by the latency of these scattered reads, so
 // they must be in flight together.  Plain loads keep each chunk's loads behind
 // the previous chunk's stores, which bounds the registers in flight.
+// Partial sums of the first props pass over one lane's particles
+// (sum w, sum w v), accumulated in the order of props_cell's loop.
+struct Sums4 {
+    double n, sx, sy, sz;
+};
+
 template <int E>
 __device__ __forceinline__ void gather_records(const Cols& A, const Cols& B, const int32_t (&v)[E], int32_t start,
-                                               int32_t N)
+                                               int32_t N, Sums4& acc)
 {
     constexpr int CH = E < 2 ? E : 2;
     const int lane = threadIdx.x & 31;
@@ -114,13 +120,18 @@ __device__ __forceinline__ void gather_records(const Cols& A, const Cols& B, con
                 ov[1] = t[r][1];
                 ox[0] = t[r][2];
                 ox[1] = t[r][3];
+                const double w = t[r][0].x;
+                acc.n += w;
+                acc.sx += t[r][0].y * w;
+                acc.sy += t[r][1].x * w;
+                acc.sz += t[r][1].y * w;
             }
         }
     }
 }
 
 template <int E>
-__device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+__device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c, int32_t start, int32_t N, Sums4& acc)
 {
     const int lane = threadIdx.x & 31;
     int32_t v[E];
@@ -130,7 +141,7 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
         v[r] = q < N ? S.idx[start + q] : INT_MAX;
     }
     warp_bitonic<E>(v);
-    gather_records<E>(S.A, S.B, v, start, N);
+    gather_records<E>(S.A, S.B, v, start, N, acc);
 #pragma unroll
     for (int r = 0; r < E; ++r) {
         const int q = r * 32 + lane;
@@ -143,22 +154,25 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
 
 // Segments above 512 particles take an out-of-line call, so the registers
 // their 32-row sort needs do not raise the register count of every caller.
-static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
+                                                        Sums4& acc)
 {
-    sort_gather_regs<32>(S, c, start, N);
+    sort_gather_regs<32>(S, c, start, N, acc);
 }
 
 // Sort the source slots of cell c's segment [start, start + N) and gather the
 // particles from buffer A into the same positions of buffer B (one warp).
-__device__ __forceinline__ void sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+// Returns this lane's first-pass props sums of the gathered particles.
+__device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
 {
-    if (N <= 0) return;
-    if (N <= 32) sort_gather_regs<1>(S, c, start, N);
-    else if (N <= 64) sort_gather_regs<2>(S, c, start, N);
-    else if (N <= 128) sort_gather_regs<4>(S, c, start, N);
-    else if (N <= 256) sort_gather_regs<8>(S, c, start, N);
-    else if (N <= 512) sort_gather_regs<16>(S, c, start, N);
-    else if (N <= 1024) sort_gather_regs_32(S, c, start, N);
+    Sums4 acc{0.0, 0.0, 0.0, 0.0};
+    if (N <= 0) return acc;
+    if (N <= 32) sort_gather_regs<1>(S, c, start, N, acc);
+    else if (N <= 64) sort_gather_regs<2>(S, c, start, N, acc);
+    else if (N <= 128) sort_gather_regs<4>(S, c, start, N, acc);
+    else if (N <= 256) sort_gather_regs<8>(S, c, start, N, acc);
+    else if (N <= 512) sort_gather_regs<16>(S, c, start, N, acc);
+    else if (N <= 1024) sort_gather_regs_32(S, c, start, N, acc);
     else {
         warp_oddeven_sort(S.idx + start, N);
         for (int q = (threadIdx.x & 31); q < N; q += 32) {
@@ -166,8 +180,14 @@ __device__ __forceinline__ void sort_gather_segment(const SpeciesView& S, int32_
             copy_particle(S.A, S.B, S.idx[dst], dst);
             S.cellB[dst] = c;
             S.key[dst] = c;
+            const PV r = S.B.wv[dst];
+            acc.n += r.w;
+            acc.sx += r.vx * r.w;
+            acc.sy += r.vy * r.w;
+            acc.sz += r.vz * r.w;
         }
     }
+    return acc;
 }
 
 }  // namespace mz

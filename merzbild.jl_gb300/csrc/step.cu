@@ -107,23 +107,30 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         if (c0 >= d.n_cells) break;
         const int nq = min(CPW, d.n_cells - c0);
         // sort + gather (A -> B), then 1-D props of the freshly sorted state
-        for (int q = 0; q < nq; ++q) {
-            const int c = c0 + q;
-            for (int s = 0; s < ns; ++s) {
-                const SpeciesView& S = d.sp[s];
-                const Indexer p = S.ind[c];
-                if (a.gather) sort_gather_segment(S, c, p.start1, p.n1);
-            }
-            __syncwarp();
-            if (a.props && a.props_lag == 1) {
-                for (int s = 0; s < ns; ++s) {
-                    const SpeciesView& S = d.sp[s];
-                    const Indexer p = S.ind[c];
-                    const CellMoments r = props_cell(a.gather ? S.B : S.A, p, p.n1, S.mass);
-                    if (lane == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p.n1, step);
+        // (the gather accumulates the first props pass)
+        for (int s = 0; s < ns; ++s) {
+            const SpeciesView& S = d.sp[s];
+            const bool props1 = a.props && a.props_lag == 1;
+            double mn = 0.0, msx = 0.0, msy = 0.0, msz = 0.0;
+            if (a.gather) {
+                for (int q = 0; q < nq; ++q) {
+                    const Indexer p = S.ind[c0 + q];
+                    const Sums4 t = sort_gather_segment(S, c0 + q, p.start1, p.n1);
+                    if (props1) props_pass1_into_lane(t.n, t.sx, t.sy, t.sz, q, mn, msx, msy, msz);
                 }
+                __syncwarp();
+                if (props1) {
+                    const CellMoments r = props_cells_finish(S.B, S.ind, c0, nq, S.mass, mn, msx, msy, msz);
+                    if (lane < nq)
+                        write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
+                }
+            } else if (props1) {
+                const CellMoments r = props_cells(S.A, S.ind, c0, nq, S.mass);
+                if (lane < nq)
+                    write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
             }
         }
+        __syncwarp();
         if (!a.physics && !(a.props && a.props_lag == 0)) continue;
         // ntc_equal_weight! for every pair in the reference's order, one
         // group per cell
@@ -163,14 +170,10 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         __syncwarp();
         // 0-D: compute_props! after the collisions of this step
         if (a.props && a.props_lag == 0) {
-            for (int q = 0; q < nq; ++q) {
-                const int cq = c0 + q;
-                for (int s = 0; s < ns; ++s) {
-                    const SpeciesView& S = d.sp[s];
-                    const Indexer p = S.ind[cq];
-                    const CellMoments r = props_cell(a.gather ? S.B : S.A, p, p.n1, S.mass);
-                    if (lane == 0) write_props(a, (int64_t)cq + (int64_t)d.n_cells * s, r, p.n1, step);
-                }
+            for (int s = 0; s < ns; ++s) {
+                const SpeciesView& S = d.sp[s];
+                const CellMoments r = props_cells(a.gather ? S.B : S.A, S.ind, c0, nq, S.mass);
+                if (lane < nq) write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
             }
         }
         if (a.dims != 1 || !a.physics) continue;
