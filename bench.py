@@ -9,7 +9,7 @@ T0 = T_wall = 273 K, diffuse walls moving at -/+500 m/s, dt = 0.2 / nu
 convect + wall reflection -> counting sort -> compute_props_sorted! ->
 avg_props! (the averaging phase of simulations/1D/couette_benchmarking.jl).
 Synthetic, seeded initial state sampled on the device.  The particle state
-(2.5 GB) is larger than L2, so no flush is needed between steps.
+(2.9 GB) is larger than L2, so no flush is needed between steps.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl merzgpu|reference]
 Prints one JSON line (rank 0).
@@ -19,6 +19,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -35,7 +36,7 @@ ALG_BYTES = 112  # per particle-step: every particle read once and written once 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=500)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="merzgpu", choices=["merzgpu", "reference"])
     p.add_argument("--cells", type=int, default=50000)
@@ -162,7 +163,7 @@ def workload(args):
                         f"{args.cells} cells x {args.ppc} ppc",
             "cells": args.cells, "ppc": args.ppc, "particles": args.cells * args.ppc,
             "step": "ntc_equal_weight -> convect -> sort -> compute_props_sorted -> avg_props",
-            "l2": "inputs larger than L2 (particle state %.1f GB)" % (args.cells * args.ppc * 124 / 1e9)}
+            "l2": "inputs larger than L2 (particle state %.1f GB)" % (args.cells * args.ppc * 144 / 1e9)}
 
 
 def setup_device(mz, ctx, args, seed):
@@ -325,13 +326,15 @@ def run_gpu(args):
     avg_launch_s = kms / klaunch / 1e3
     peak, peak_kind = measured_peaks()
     achieved = ALG_BYTES * n / avg_launch_s / 1e9
+    # DRAM bytes per particle of the full-step launch from the committed ncu
+    # summary (captured on a smaller case; traffic scales with particles)
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "step_cell_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "step_cell_traffic.md")
     if os.path.exists(tfile):
         with open(tfile) as f:
-            traffic = json.load(f).get("dram_bytes_per_particle")
-        if traffic is not None:
-            traffic = traffic * n
+            m = re.search(r"^dram_bytes_per_particle:\s*([0-9.eE+-]+)", f.read(), re.M)
+        if m:
+            traffic = float(m.group(1)) * n
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": ALG_BYTES * n,

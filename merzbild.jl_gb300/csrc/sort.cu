@@ -5,15 +5,16 @@
 // Pipeline (all on the context stream):
 //   count   : per live slot, the destination cell (stored key or floor(x/dx));
 //             warp-aggregated atomicAdd into counts[cell]
-//   scan    : one block, exclusive scan of counts -> indexer start1/n_group1,
-//             group 2 cleared, cursors zeroed, counts zeroed for reuse
+//   scan    : two passes over tiles of cells (launch_scan_cells): exclusive
+//             scan of counts -> indexer start1/n_group1, group 2 cleared,
+//             cursors zeroed, counts zeroed for reuse
 //   scatter : per live slot, position = start1[cell] + ticket (warp-aggregated
 //             atomic); idx[position] = slot.  Tickets arrive in any order.
 //   gather  : one warp per cell sorts its idx segment ascending (a bitonic
 //             network held in registers) -- this restores the reference's
-//             stable order exactly -- then moves the 7 FP64 columns of every
+//             stable order exactly -- then moves both 32-byte records of every
 //             particle into the other buffer, coalesced on the write side.
-// Algorithmic bytes per particle: 56 read + 56 written (+ 16 B of keys/idx).
+// Algorithmic bytes per particle: 64 read + 64 written (+ 16 B of keys/idx).
 #include "mz_host.h"
 #include "sortnet.cuh"
 
