@@ -137,3 +137,72 @@ def test_two_species_relaxation_ensemble_matches_the_oracle(ctx, orc):
             assert abs(a.mean() - b.mean()) <= 3 * se, (tt, s, a.mean(), b.mean(), se)
     for s in range(2):
         assert abs(dev[800][s].mean() - 600.0) / 600.0 < 0.12
+
+
+def test_couette_profiles_ensemble_matches_the_oracle(ctx, orc):
+    """Couette flow (simulations/1D/couette_benchmarking.jl:58-85 at a small
+    size): time-averaged velocity and temperature profiles of 16 device runs
+    (the fused graph step with avg_props!) against 16 oracle runs of the
+    reference loop, other seeds; per cell and quantity z = difference of the
+    ensemble means over its standard error, sum of z^2 below the chi-square
+    99.9 % quantile."""
+    scipy_stats = pytest.importorskip("scipy.stats")
+    sp = species(["Ar"])
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    nx, ppc, L, ndens, T = 20, 200, 5e-4, 1e23, 273.0
+    n_steps, avg_from, runs = 400, 201, 16
+    grid = mz.Grid1DUniform(L, nx)
+    Fnum = grid.dx * ndens / ppc
+    walls = mz.MaxwellWalls1D(sp, T, T, -500.0, 500.0, 1.0, 1.0)
+    dt = 0.2 / mz.mean_collision_frequency(inter, sp, 0, ndens, T)
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], T, T, Fnum)
+    n_avg = n_steps - avg_from + 1
+
+    dev_v, dev_T = [], []
+    for r in range(runs):
+        dom = mz.Domain(ctx, nx, sp, 3 * ppc * nx, interactions=inter, seed=500 + r)
+        dom.set_cell_volumes(grid.V)
+        dom.sample_grid_ndens(0, grid, ndens, T, Fnum, step=0)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        plan = mz._lib.StepPlan()
+        plan.dims, plan.collide, plan.equal_weight, plan.props = 1, 1, 1, 1
+        plan.avg_start, plan.n_avg, plan.dt, plan.dw_tol = avg_from, n_avg, dt, 1e-16
+        plan.step0, plan.use_graph = 0, 1
+        plan.grid, plan.walls = grid.c_struct(), walls.c_struct()
+        avg = mz.PhysProps(dom)
+        dom.step(plan, n_steps, None, avg)
+        a = avg.fetch()
+        dev_v.append(a["v"][1, :, 0].copy())
+        dev_T.append(a["T"][:, 0].copy())
+        dom.close()
+
+    ora_v, ora_T = [], []
+    for r in range(runs):
+        seed = 900 + r
+        o = orc.Oracle(nx, 1, [sp[0].mass])
+        o.load_interactions(*mz.VHS["Ar,Ar"])
+        o.pv_create(0, 3 * ppc * nx)
+        o.sample_grid_ndens(0, L, nx, ndens, T, Fnum, seed=seed, step=0)
+        o.cf_set_smax(0, 0, smax)
+        sv, sT = np.zeros(nx), np.zeros(nx)
+        for step in range(1, n_steps + 1):
+            o.ntc_cells(0, 0, dt, grid.V, seed, step, equal_weight=True)
+            o.convect(0, L, nx, walls.as_flat_array(), dt, seed, step)
+            o.sort(0, L=L, nx=nx)
+            if step >= avg_from:
+                pr = o.compute_props(mode=2)
+                sv += pr["v"][0, :, 1] / n_avg
+                sT += pr["T"][0] / n_avg
+        ora_v.append(sv)
+        ora_T.append(sT)
+
+    chi2 = 0.0
+    for dev, ora in ((np.array(dev_v), np.array(ora_v)), (np.array(dev_T), np.array(ora_T))):
+        se = np.sqrt(dev.var(axis=0, ddof=1) / runs + ora.var(axis=0, ddof=1) / runs)
+        chi2 += float(np.sum(((dev.mean(axis=0) - ora.mean(axis=0)) / se) ** 2))
+    limit = scipy_stats.chi2.ppf(0.999, 2 * nx)
+    assert chi2 < limit, f"chi2 {chi2:.1f} over {2 * nx} cells x quantities, limit {limit:.1f}"
+    # the profiles are Couette profiles: the averaged velocity runs from the
+    # left wall's -500 m/s towards the right wall's +500 m/s
+    vmean = np.array(dev_v).mean(axis=0)
+    assert vmean[0] < -100.0 and vmean[-1] > 100.0 and np.all(np.diff(vmean) > -30.0)
