@@ -253,6 +253,57 @@ int mz_sample_grid_ndens(mz_domain* dom, int32_t species, const mz_grid1d* grid,
  * step, avg accumulates avg_props! from plan->avg_start (either may be NULL) */
 int mz_step(mz_domain* dom, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
 
+/* ---------------------------------------------------------------- serving */
+/* No counterpart in the reference (its drivers run one simulation per
+ * process).  A continuous-batching server of independent 0-D solves -- the
+ * README's relaxation problem (README.md:91-106) as a request: particles of
+ * each species sampled Maxwellian at their temperature in a cell of volume V,
+ * then n_steps of ntc! for every species pair and compute_props!.  Each
+ * request occupies one cell of a server domain while it runs; requests are
+ * admitted first come first served while a cell and the per-species particle
+ * budget (capacity) are free, all running requests advance together in one
+ * fused step per mz_server_step, and a request's result depends only on the
+ * request (its seed), not on the requests beside it or its cell. */
+typedef struct mz_server_s mz_server;
+
+enum { MZ_REQ_QUEUED = 0, MZ_REQ_RUNNING = 1, MZ_REQ_DONE = 2 };
+
+typedef struct {
+    int64_t count[MZ_MAX_SPECIES]; /* particles per species (0: species absent) */
+    double T[MZ_MAX_SPECIES];      /* initial temperature per species, K */
+    double Fnum;                   /* particle weight */
+    double V;                      /* cell volume */
+    int64_t n_steps;               /* time steps, >= 1 */
+    uint64_t seed;                 /* key of all of the request's random streams */
+} mz_request;
+
+typedef struct {
+    int64_t id;
+    int32_t state;       /* MZ_REQ_* */
+    int32_t reserved;
+    int64_t steps_done;
+    int64_t np[MZ_MAX_SPECIES];          /* after the last step */
+    double n[MZ_MAX_SPECIES];
+    double v[MZ_MAX_SPECIES][3];
+    double T[MZ_MAX_SPECIES];
+} mz_request_result;
+
+/* a server for up to max_requests concurrent requests of n_species species
+ * (masses, interactions [s1 + n_species * s2] as mz_set_interactions), time
+ * step dt, capacity[s] particles of each species in HBM */
+int mz_server_create(mz_ctx* ctx, int32_t n_species, const double* mass, const mz_interaction* inter, double dt,
+                     int64_t max_requests, const int64_t* capacity, mz_server** out);
+int mz_server_destroy(mz_server* server);
+/* queue a request; *id identifies it */
+int mz_server_submit(mz_server* server, const mz_request* request, int64_t* id);
+/* admit what fits, advance every running request by one step, retire the
+ * finished ones; counts after the step */
+int mz_server_step(mz_server* server, int64_t* n_running, int64_t* n_queued, int64_t* n_retired);
+/* state of a request and, once done, its final properties */
+int mz_server_result(mz_server* server, int64_t id, mz_request_result* out);
+/* server steps run and particle-steps done so far */
+int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_steps);
+
 /* ---------------------------------------------------------------- counters */
 int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
 

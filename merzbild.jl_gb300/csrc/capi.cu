@@ -70,25 +70,10 @@ void mz_ctx_s::resolve_timings()
 
 int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-static void set_err(const mz_ctx* c, const std::string& m)
+void set_err(const mz_ctx* c, const std::string& m)
 {
     if (c) const_cast<mz_ctx*>(c)->last_error = m;
 }
-
-#define API_TRY try {
-#define API_CATCH(ctxp)                                                                                \
-    }                                                                                                  \
-    catch (MzError & e)                                                                                \
-    {                                                                                                  \
-        set_err(ctxp, e.what());                                                                       \
-        return e.code;                                                                                 \
-    }                                                                                                  \
-    catch (std::exception & e)                                                                         \
-    {                                                                                                  \
-        set_err(ctxp, e.what());                                                                       \
-        return MZ_E_ARG;                                                                               \
-    }                                                                                                  \
-    return MZ_OK;
 
 // ------------------------------------------------------------------ domain helpers
 mz::DomainView make_view(mz_domain* d)
@@ -606,6 +591,7 @@ int mz_upload_particles_indexed(mz_domain* d, int32_t s, int64_t n_slots, const 
     S.hw = n_slots;
     S.n_total = total;
     S.compact = false;
+    S.group2 = true;
     API_CATCH(d->ctx)
 }
 

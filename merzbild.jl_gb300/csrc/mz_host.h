@@ -63,6 +63,7 @@ struct SpeciesHost {
     int64_t hw = 0;        // high water: slots [0, hw) in use (live or dead)
     int64_t n_total = 0;   // live particles
     bool compact = true;   // every cell's list lies in group 1 and no dead slot below hw
+    bool group2 = false;   // some cell may hold group-2 (split) particles
     mz::PV* wv[2] = {nullptr, nullptr};   // [buffer A/B] weight + velocity records
     mz::PX* pos[2] = {nullptr, nullptr};  // [buffer A/B] position records
     int cur = 0;           // which buffer is A
@@ -125,6 +126,24 @@ mz::DomainView make_view(mz_domain* d);
 void ensure_compact(mz_domain* d, int s);
 void swap_buffers(mz_domain* d, int s);
 void check_status(mz_domain* d);
+// last-error text of a context, and the try / catch that turns MzError and
+// other exceptions into a status code at every C entry point
+void set_err(const mz_ctx* c, const std::string& m);
+#define API_TRY try {
+#define API_CATCH(ctxp)                                                                                \
+    }                                                                                                  \
+    catch (MzError & e)                                                                                \
+    {                                                                                                  \
+        set_err(ctxp, e.what());                                                                       \
+        return e.code;                                                                                 \
+    }                                                                                                  \
+    catch (std::exception & e)                                                                         \
+    {                                                                                                  \
+        set_err(ctxp, e.what());                                                                       \
+        return MZ_E_ARG;                                                                               \
+    }                                                                                                  \
+    return MZ_OK;
+
 int64_t div_up(int64_t a, int64_t b);
 
 // launchers (one per translation unit)

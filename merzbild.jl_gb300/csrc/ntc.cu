@@ -165,9 +165,11 @@ void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce,
         // splits land in one species per event; recount per species from the indexers
         A.hw += tot1;
         A.compact = false;
+        A.group2 = true;
         if (!single) {
             B.hw += tot2;
             B.compact = false;
+            B.group2 = true;
         }
         // exact per-species totals from the indexers
         for (int s : {s1, s2}) {

@@ -1,0 +1,377 @@
+// Serving loop: continuous batching of independent 0-D solves (the README's
+// relaxation problem, README.md:91-106, as a request) on one domain.
+//
+// Every request owns one cell (a slot) of a server domain for its lifetime.
+// Its particles, (sigma g w)_max and random streams live in that slot only:
+// the streams are keyed on the request's seed and its own step count (per-cell
+// RNG keys with a step offset), and every kernel works per cell, so a
+// request's result does not depend on which slot it gets or on what runs
+// beside it.  One server step admits queued requests while slots and the
+// particle budget allow (compacting storage when dead slots block an
+// admission), runs one fused 0-D step (ntc! for every species pair, then
+// compute_props!) for all running requests at once, and retires requests that
+// reached their step count, keeping their final properties.
+#include "mz_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <deque>
+#include <unordered_map>
+
+using namespace mz;
+
+namespace {
+
+struct ReqRec {
+    mz_request r;
+    int32_t state = MZ_REQ_QUEUED;
+    int32_t slot = -1;
+    int64_t start_step = 0;  // server step before the request's first step
+    mz_request_result res{};
+};
+
+// per-slot set-up of admitted requests: RNG keys, volume, (sigma g w)_max
+struct AdmitArgs {
+    const int32_t* cells;
+    int n;
+    const uint64_t* seed;
+    const uint32_t* offset;
+    const double* V;
+    const double* smax;  // n x (ns * ns), pair index s1 + ns * s2
+};
+
+__global__ void k_admit(DomainView d, AdmitArgs a, uint64_t* cseed, uint32_t* crid, uint32_t* cstep, double* cV)
+{
+    const int ns = d.n_species;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const int c = a.cells[i];
+        cseed[c] = a.seed[i];
+        crid[c] = 0;
+        cstep[c] = a.offset[i];
+        cV[c] = a.V[i];
+        for (int p = 0; p < ns * ns; ++p) {
+            CollisionFactors& cf = d.cf[(size_t)p * d.n_cells + c];
+            cf.smax = a.smax[(size_t)i * ns * ns + p];
+            cf.n1 = cf.n2 = cf.n_coll = cf.n_coll_performed = cf.n_eq_w_coll_performed = cf.n_split = 0;
+        }
+    }
+}
+
+// retire: the slot's particles become dead and its lists empty
+__global__ void k_release(DomainView d, const int32_t* cells, int n)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+        const int c = cells[i];
+        for (int s = 0; s < d.n_species; ++s) {
+            const SpeciesView& S = d.sp[s];
+            const Indexer p = S.ind[c];
+            for (int j = lane; j < p.n1 + p.n2; j += 32) {
+                const int32_t q = map_slot(p, j);
+                S.cell[q] = -1;
+                S.A.wv[q].w = 0.0;
+            }
+            __syncwarp();
+            if (lane == 0) S.ind[c] = Indexer{0, 0, 0, 0};
+        }
+    }
+}
+
+// estimate_sigma_g_w_max (collision_utils.jl:418-423)
+double sigma_g_w_max_estimate(const Interaction& I, double m1, double m2, double T1, double T2, double Fnum)
+{
+    const double g = 0.5 * (std::sqrt(2.0 * T1 * K_B / m1) + std::sqrt(2.0 * T2 * K_B / m2));
+    const double sigma = I.vhs_factor * std::pow(g, std::fma(-2.0, I.vhs_o, 1.0));
+    return sigma * g * Fnum;
+}
+
+}  // namespace
+
+struct mz_server_s {
+    mz_ctx* ctx = nullptr;
+    mz_domain* dom = nullptr;
+    mz_props* props = nullptr;
+    int32_t ns = 0;
+    int64_t slots = 0;
+    double dt = 0.0;
+    int64_t step = 0;  // server steps run
+    int64_t next_id = 1;
+    std::deque<int64_t> queue;
+    std::unordered_map<int64_t, ReqRec> reqs;
+    std::vector<int64_t> slot_req;  // request id per slot, 0 = free
+    std::vector<int64_t> free_slots;
+    std::vector<int64_t> running;   // ids of admitted, unfinished requests
+    // device scratch for admissions / retirements
+    int32_t* d_cells = nullptr;
+    uint64_t* d_seed = nullptr;
+    uint32_t* d_off = nullptr;
+    double* d_V = nullptr;
+    double* d_smax = nullptr;
+    int64_t particle_steps = 0;
+};
+
+namespace {
+
+void ensure_rng_arrays(mz_domain* d)
+{
+    const int64_t n = d->n_cells;
+    if (!d->d_cell_seed) {
+        MZ_CK(cudaMalloc(&d->d_cell_seed, n * sizeof(uint64_t)));
+        MZ_CK(cudaMemsetAsync(d->d_cell_seed, 0, n * sizeof(uint64_t), d->ctx->stream));
+    }
+    if (!d->d_cell_rid) {
+        MZ_CK(cudaMalloc(&d->d_cell_rid, n * sizeof(uint32_t)));
+        MZ_CK(cudaMemsetAsync(d->d_cell_rid, 0, n * sizeof(uint32_t), d->ctx->stream));
+    }
+    if (!d->d_cell_step) {
+        MZ_CK(cudaMalloc(&d->d_cell_step, n * sizeof(uint32_t)));
+        MZ_CK(cudaMemsetAsync(d->d_cell_step, 0, n * sizeof(uint32_t), d->ctx->stream));
+    }
+}
+
+// admit queued requests while slots and storage allow; FIFO, no overtaking
+void admit(mz_server* sv)
+{
+    mz_domain* d = sv->dom;
+    const int ns = sv->ns;
+    std::vector<int32_t> cells;
+    std::vector<uint64_t> seeds;
+    std::vector<uint32_t> offs;
+    std::vector<double> Vs, smax;
+    std::vector<std::vector<int64_t>> counts(ns, std::vector<int64_t>(d->n_cells, 0));
+    std::vector<double> T3(3 * d->n_cells * ns, 0.0), F(d->n_cells * ns, 0.0);
+    int64_t need[MZ_MAX_SPECIES] = {0, 0, 0, 0};
+    while (!sv->queue.empty() && !sv->free_slots.empty()) {
+        const int64_t id = sv->queue.front();
+        ReqRec& q = sv->reqs.at(id);
+        bool fits = true;
+        for (int s = 0; s < ns && fits; ++s) {
+            SpeciesHost& S = d->sp[s];
+            const int64_t want = need[s] + q.r.count[s];
+            if (S.hw + want > S.capacity) {
+                // dead slots of retired requests block the admission: compact
+                if (S.n_total + want <= S.capacity && need[s] == 0 && !S.compact) launch_compact(d, s);
+                if (S.hw + want > S.capacity) fits = false;
+            }
+        }
+        if (!fits) break;
+        sv->queue.pop_front();
+        const int32_t slot = (int32_t)sv->free_slots.back();
+        sv->free_slots.pop_back();
+        q.state = MZ_REQ_RUNNING;
+        q.slot = slot;
+        q.start_step = sv->step;
+        sv->slot_req[slot] = id;
+        sv->running.push_back(id);
+        cells.push_back(slot);
+        seeds.push_back(q.r.seed);
+        offs.push_back((uint32_t)sv->step);
+        Vs.push_back(q.r.V);
+        for (int s2 = 0; s2 < ns; ++s2)
+            for (int s1 = 0; s1 < ns; ++s1) {
+                const double T1 = q.r.T[s1] > 0 ? q.r.T[s1] : 300.0, T2 = q.r.T[s2] > 0 ? q.r.T[s2] : 300.0;
+                smax.push_back(sigma_g_w_max_estimate(d->inter[s1 + ns * s2], d->mass[s1], d->mass[s2], T1, T2,
+                                                      q.r.Fnum));
+            }
+        for (int s = 0; s < ns; ++s) {
+            counts[s][slot] = q.r.count[s];
+            need[s] += q.r.count[s];
+            for (int k = 0; k < 3; ++k) T3[(size_t)s * 3 * d->n_cells + 3 * slot + k] = q.r.T[s];
+            F[(size_t)s * d->n_cells + slot] = q.r.Fnum;
+        }
+    }
+    if (cells.empty()) return;
+    const int n = (int)cells.size();
+    mz_ctx* c = sv->ctx;
+    MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sv->d_seed, seeds.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sv->d_off, offs.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sv->d_V, Vs.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(sv->d_smax, smax.data(), smax.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AdmitArgs a{sv->d_cells, n, sv->d_seed, sv->d_off, sv->d_V, sv->d_smax};
+    DomainView v = make_view(d);
+    MZ_LAUNCH(c, "server_admit", k_admit, (int)div_up(n, 128), 128, 0, v, a, d->d_cell_seed, d->d_cell_rid,
+              d->d_cell_step, d->d_V);
+    // initial particles of the admitted requests (streams of step 0 of each)
+    for (int s = 0; s < ns; ++s) {
+        if (need[s] == 0) continue;
+        launch_sample_cells(d, s, counts[s].data(), nullptr, T3.data() + (size_t)s * 3 * d->n_cells, nullptr,
+                            F.data() + (size_t)s * d->n_cells, 0.0, nullptr, 0, (uint64_t)sv->step);
+        d->sp[s].compact = false;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mz_server_create(mz_ctx* c, int32_t n_species, const double* mass, const mz_interaction* inter, double dt,
+                     int64_t max_requests, const int64_t* capacity, mz_server** out)
+{
+    mz_server* sv = nullptr;
+    API_TRY
+    MZ_REQUIRE(c && out && mass && inter && capacity, "mz_server_create: NULL argument");
+    MZ_REQUIRE(n_species >= 1 && n_species <= MZ_MAX_SPECIES, "mz_server_create: bad species count");
+    MZ_REQUIRE(max_requests >= 1 && max_requests < (1 << 24), "mz_server_create: bad max_requests");
+    MZ_REQUIRE(dt > 0.0, "mz_server_create: dt must be positive");
+    sv = new mz_server_s();
+    sv->ctx = c;
+    sv->ns = n_species;
+    sv->slots = max_requests;
+    sv->dt = dt;
+    int rc = mz_domain_create(c, max_requests, n_species, capacity, &sv->dom);
+    if (rc != MZ_OK) throw MzError(rc, "mz_server_create: domain");
+    rc = mz_set_species(sv->dom, mass);
+    if (rc == MZ_OK) rc = mz_set_interactions(sv->dom, inter);
+    if (rc == MZ_OK) rc = mz_props_create(sv->dom, 0, nullptr, 300.0, 0, &sv->props);
+    if (rc != MZ_OK) throw MzError(rc, "mz_server_create: set-up");
+    ensure_rng_arrays(sv->dom);
+    sv->slot_req.assign(max_requests, 0);
+    for (int64_t s = max_requests - 1; s >= 0; --s) sv->free_slots.push_back(s);
+    MZ_CK(cudaMalloc(&sv->d_cells, max_requests * sizeof(int32_t)));
+    MZ_CK(cudaMalloc(&sv->d_seed, max_requests * sizeof(uint64_t)));
+    MZ_CK(cudaMalloc(&sv->d_off, max_requests * sizeof(uint32_t)));
+    MZ_CK(cudaMalloc(&sv->d_V, max_requests * sizeof(double)));
+    MZ_CK(cudaMalloc(&sv->d_smax, max_requests * n_species * n_species * sizeof(double)));
+    *out = sv;
+    sv = nullptr;
+    API_CATCH(c)
+}
+
+int mz_server_destroy(mz_server* sv)
+{
+    if (!sv) return MZ_OK;
+    cudaSetDevice(sv->ctx->device);
+    cudaStreamSynchronize(sv->ctx->stream);
+    cudaFree(sv->d_cells);
+    cudaFree(sv->d_seed);
+    cudaFree(sv->d_off);
+    cudaFree(sv->d_V);
+    cudaFree(sv->d_smax);
+    if (sv->dom) mz_domain_destroy(sv->dom);  // frees its props too
+    delete sv;
+    return MZ_OK;
+}
+
+int mz_server_submit(mz_server* sv, const mz_request* r, int64_t* id)
+{
+    API_TRY
+    MZ_REQUIRE(sv && r && id, "mz_server_submit: NULL argument");
+    MZ_REQUIRE(r->n_steps >= 1 && r->Fnum > 0.0 && r->V > 0.0, "mz_server_submit: bad request");
+    for (int s = 0; s < sv->ns; ++s) {
+        MZ_REQUIRE(r->count[s] >= 0 && r->count[s] <= sv->dom->sp[s].capacity,
+                   "mz_server_submit: request larger than the particle budget");
+        MZ_REQUIRE(r->count[s] == 0 || r->T[s] > 0.0, "mz_server_submit: temperature must be positive");
+    }
+    ReqRec q;
+    q.r = *r;
+    q.res.id = sv->next_id;
+    const int64_t k = sv->next_id++;
+    sv->reqs.emplace(k, q);
+    sv->queue.push_back(k);
+    *id = k;
+    API_CATCH(sv->ctx)
+}
+
+int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t* n_retired)
+{
+    API_TRY
+    MZ_REQUIRE(sv, "mz_server_step: NULL server");
+    MZ_CK(cudaSetDevice(sv->ctx->device));
+    mz_domain* d = sv->dom;
+    admit(sv);
+    int64_t running = (int64_t)sv->running.size(), retired = 0;
+    if (running > 0) {
+        mz_step_plan plan;
+        memset(&plan, 0, sizeof plan);
+        plan.dims = 0;
+        plan.collide = 1;
+        plan.equal_weight = 1;
+        plan.props = 1;
+        plan.dt = sv->dt;
+        plan.dw_tol = 1e-16;
+        plan.step0 = (uint64_t)sv->step;
+        plan.use_graph = 0;
+        std::vector<int64_t> done;
+        launch_step(d, &plan, 1, sv->props, nullptr);
+        ++sv->step;
+        for (int64_t k : sv->running) {
+            ReqRec& q = sv->reqs.at(k);
+            q.res.steps_done = sv->step - q.start_step;
+            for (int s = 0; s < sv->ns; ++s) sv->particle_steps += q.r.count[s];
+            if (q.res.steps_done >= q.r.n_steps) done.push_back(k);
+        }
+        if (!done.empty()) {
+            // final properties of the finished requests: props of their last step
+            const int64_t nc = d->n_cells, ns = sv->ns;
+            std::vector<double> np(nc * ns), n(nc * ns), v(3 * nc * ns), T(nc * ns);
+            MZ_CK(cudaMemcpyAsync(np.data(), sv->props->np, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
+                                  sv->ctx->stream));
+            MZ_CK(cudaMemcpyAsync(n.data(), sv->props->n, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
+                                  sv->ctx->stream));
+            MZ_CK(cudaMemcpyAsync(v.data(), sv->props->v, 3 * nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
+                                  sv->ctx->stream));
+            MZ_CK(cudaMemcpyAsync(T.data(), sv->props->T, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
+                                  sv->ctx->stream));
+            MZ_CK(cudaStreamSynchronize(sv->ctx->stream));
+            std::vector<int32_t> cells;
+            for (int64_t k : done) {
+                ReqRec& q = sv->reqs.at(k);
+                const int64_t c = q.slot;
+                for (int s = 0; s < ns; ++s) {
+                    q.res.np[s] = (int64_t)np[c + nc * s];
+                    q.res.n[s] = n[c + nc * s];
+                    for (int a = 0; a < 3; ++a) q.res.v[s][a] = v[a + 3 * (c + nc * s)];
+                    q.res.T[s] = T[c + nc * s];
+                }
+                q.res.steps_done = q.r.n_steps;
+                q.state = MZ_REQ_DONE;
+                cells.push_back((int32_t)c);
+                sv->slot_req[c] = 0;
+                sv->free_slots.push_back(c);
+                for (int s = 0; s < ns; ++s) d->sp[s].n_total -= q.r.count[s];
+                ++retired;
+            }
+            MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), cells.size() * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, sv->ctx->stream));
+            DomainView vv = make_view(d);
+            MZ_LAUNCH(sv->ctx, "server_release", k_release, (int)div_up((int64_t)cells.size() * 32, 256), 256, 0, vv,
+                      sv->d_cells, (int)cells.size());
+            for (int s = 0; s < ns; ++s) d->sp[s].compact = false;
+            sv->running.erase(std::remove_if(sv->running.begin(), sv->running.end(),
+                                             [&](int64_t k) { return sv->reqs.at(k).state == MZ_REQ_DONE; }),
+                              sv->running.end());
+            running -= retired;
+        }
+    }
+    if (n_running) *n_running = running;
+    if (n_queued) *n_queued = (int64_t)sv->queue.size();
+    if (n_retired) *n_retired = retired;
+    check_status(d);
+    API_CATCH(sv->ctx)
+}
+
+int mz_server_result(mz_server* sv, int64_t id, mz_request_result* out)
+{
+    API_TRY
+    MZ_REQUIRE(sv && out, "mz_server_result: NULL argument");
+    auto it = sv->reqs.find(id);
+    MZ_REQUIRE(it != sv->reqs.end(), "mz_server_result: unknown request");
+    *out = it->second.res;
+    out->id = id;
+    out->state = it->second.state;
+    if (it->second.state == MZ_REQ_RUNNING) out->steps_done = sv->step - it->second.start_step;
+    API_CATCH(sv->ctx)
+}
+
+int mz_server_info(mz_server* sv, int64_t* steps_run, int64_t* particle_steps)
+{
+    API_TRY
+    MZ_REQUIRE(sv, "mz_server_info: NULL server");
+    if (steps_run) *steps_run = sv->step;
+    if (particle_steps) *particle_steps = sv->particle_steps;
+    API_CATCH(sv->ctx)
+}
+
+}  // extern "C"

@@ -308,6 +308,7 @@ void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index)
     S.hw = n_total;
     S.cur ^= 1;
     S.compact = true;
+    S.group2 = false;
 }
 
 void launch_compact(mz_domain* d, int s)
@@ -324,6 +325,7 @@ void launch_compact(mz_domain* d, int s)
     S.hw = S.n_total;
     S.cur ^= 1;
     S.compact = true;
+    S.group2 = false;
 }
 
 void launch_key_from_cell(mz_domain* d, int s)

@@ -379,7 +379,11 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     mz_ctx* c = d->ctx;
     if (n_steps <= 0) return;
     MZ_REQUIRE(plan->equal_weight, "mz_step: the fused step runs ntc_equal_weight!; use mz_ntc for splitting");
-    for (int s = 0; s < d->ns; ++s) launch_compact(d, s);
+    // the 1-D step's sort runs over slots [0, n_total): close gaps first; the
+    // 0-D step works on each cell's group-1 list in place, so only split
+    // particles in group 2 need a compaction
+    for (int s = 0; s < d->ns; ++s)
+        if (plan->dims == 1 || d->sp[s].group2) launch_compact(d, s);
     if (!d->d_step) {
         MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
         MZ_CK(cudaMalloc(&d->d_done, 4 * sizeof(unsigned int)));
@@ -499,8 +503,9 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     } else {
         for (int64_t t = 0; t < n_steps; ++t) cell_launch(0, want_props, plan->collide);
     }
-    for (int s = 0; s < d->ns; ++s) {
-        d->sp[s].hw = d->sp[s].n_total;
-        d->sp[s].compact = true;
-    }
+    if (plan->dims == 1)
+        for (int s = 0; s < d->ns; ++s) {
+            d->sp[s].hw = d->sp[s].n_total;
+            d->sp[s].compact = true;
+        }
 }

@@ -54,6 +54,19 @@ class Counters(C.Structure):
     _fields_ = [(n, C.c_ulonglong) for n in ("candidates", "accepted", "splits", "merges", "wall_hits")]
 
 
+class Request(C.Structure):
+    _fields_ = [("count", i64 * MZ_MAX_SPECIES), ("T", d * MZ_MAX_SPECIES), ("Fnum", d), ("V", d), ("n_steps", i64),
+                ("seed", u64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", i64), ("state", i32), ("reserved", i32), ("steps_done", i64), ("np", i64 * MZ_MAX_SPECIES),
+                ("n", d * MZ_MAX_SPECIES), ("v", (d * 3) * MZ_MAX_SPECIES), ("T", d * MZ_MAX_SPECIES)]
+
+
+MZ_REQ_QUEUED, MZ_REQ_RUNNING, MZ_REQ_DONE = 0, 1, 2
+
+
 class StepPlan(C.Structure):
     _fields_ = [("dims", i32), ("collide", i32), ("equal_weight", i32), ("props", i32), ("avg_start", i64),
                 ("n_avg", i64), ("dt", d), ("dw_tol", d), ("step0", u64), ("use_graph", i32), ("reserved", i32),
@@ -105,6 +118,12 @@ _SIGS = {
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
     "mz_sort_keys_noalloc": (i32, [vp, vp, i64, i32, vp, vp]),
     "mz_sincos_2pi": (i32, [vp, i64, P(u64), P(d), P(d)]),
+    "mz_server_create": (i32, [vp, i32, P(d), P(Interaction), d, i64, P(i64), P(vp)]),
+    "mz_server_destroy": (i32, [vp]),
+    "mz_server_submit": (i32, [vp, P(Request), P(i64)]),
+    "mz_server_step": (i32, [vp, P(i64), P(i64), P(i64)]),
+    "mz_server_result": (i32, [vp, i64, P(RequestResult)]),
+    "mz_server_info": (i32, [vp, P(i64), P(i64)]),
 }
 NOALLOC_MAX_CELLS = 262144
 

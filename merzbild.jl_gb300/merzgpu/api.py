@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 import tomllib
 import weakref
 from dataclasses import dataclass
@@ -502,6 +503,105 @@ class PhysProps:
         # column-major (Julia) -> numpy [..., cell, species] views
         return dict(lpa=lpa, np=np_.reshape(ns, nc).T, n=n.reshape(ns, nc).T, v=v.reshape(ns, nc, 3).transpose(2, 1, 0),
                     T=T.reshape(ns, nc).T, moments=mom[: nm * nc * ns].reshape(ns, nc, nm).transpose(2, 1, 0))
+
+
+# --------------------------------------------------------------------- serving
+class Server:
+    """Continuous-batching server of independent 0-D solves (mz_server_*).
+
+    Each request is the README relaxation problem for given particle counts
+    and temperatures per species; requests run side by side in one domain,
+    one cell each, and advance together one fused step per `step()`.  A
+    request's result depends only on the request itself (its seed)."""
+
+    def __init__(self, ctx: Context, species_data, interactions, dt, max_requests, capacity):
+        self.ctx = ctx
+        self.ns = len(species_data)
+        mass = f64([sp.mass for sp in species_data])
+        tab = (L.Interaction * (self.ns * self.ns))()
+        for s1 in range(self.ns):
+            for s2 in range(self.ns):
+                tab[s1 + self.ns * s2] = interactions[s1][s2].c_struct()
+        cap = np.ascontiguousarray(np.broadcast_to(np.asarray(capacity, np.int64), (self.ns,)))
+        self.h = C.c_void_p()
+        check(lib().mz_server_create(ctx.h, self.ns, ptr(mass), tab, float(dt), int(max_requests),
+                                     ptr(cap, C.c_int64), C.byref(self.h)), ctx.h)
+        ctx._children.add(self)
+
+    def close(self):
+        if self.h:
+            if self.ctx.h:
+                lib().mz_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        check(rc, self.ctx.h)
+
+    def submit(self, counts, T, Fnum, n_steps, seed, V=1.0):
+        r = L.Request()
+        for s in range(self.ns):
+            r.count[s] = int(counts[s]) if s < len(counts) else 0
+            r.T[s] = float(T[s]) if s < len(T) else 0.0
+        r.Fnum, r.V, r.n_steps, r.seed = float(Fnum), float(V), int(n_steps), int(seed)
+        rid = C.c_int64()
+        self._ck(lib().mz_server_submit(self.h, C.byref(r), C.byref(rid)))
+        return rid.value
+
+    def step(self):
+        run, que, ret = C.c_int64(), C.c_int64(), C.c_int64()
+        self._ck(lib().mz_server_step(self.h, C.byref(run), C.byref(que), C.byref(ret)))
+        return run.value, que.value, ret.value
+
+    def result(self, rid):
+        out = L.RequestResult()
+        self._ck(lib().mz_server_result(self.h, int(rid), C.byref(out)))
+        ns = self.ns
+        return dict(state=out.state, steps_done=out.steps_done, np=[out.np[s] for s in range(ns)],
+                    n=[out.n[s] for s in range(ns)], v=[[out.v[s][k] for k in range(3)] for s in range(ns)],
+                    T=[out.T[s] for s in range(ns)])
+
+    def info(self):
+        steps, ps = C.c_int64(), C.c_int64()
+        self._ck(lib().mz_server_info(self.h, C.byref(steps), C.byref(ps)))
+        return dict(steps=steps.value, particle_steps=ps.value)
+
+    def serve(self, requests, clock=time.perf_counter):
+        """Request loop: `requests` are (arrival_s, kwargs of submit) sorted by
+        arrival.  Requests are submitted when their arrival time has passed
+        (relative to the start), the server steps while work remains, and the
+        latency of each request (completion - arrival) is recorded.  Returns
+        (latencies in s, ids, elapsed s)."""
+        t0 = clock()
+        i, n = 0, len(requests)
+        ids, arrival = [], {}
+        pending = set()
+        lat = {}
+        while i < n or pending:
+            now = clock() - t0
+            while i < n and requests[i][0] <= now:
+                rid = self.submit(**requests[i][1])
+                ids.append(rid)
+                arrival[rid] = requests[i][0]
+                pending.add(rid)
+                i += 1
+            if not pending:
+                # idle until the next arrival
+                time.sleep(max(0.0, min(requests[i][0] - now, 0.002)))
+                continue
+            _, _, retired = self.step()
+            if retired:
+                t = clock() - t0
+                for rid in list(pending):
+                    if self.result(rid)["state"] == L.MZ_REQ_DONE:
+                        lat[rid] = t - arrival[rid]
+                        pending.discard(rid)
+        return [lat[r] for r in ids], ids, clock() - t0
 
 
 # --------------------------------------------------------------------- reference-named functions
