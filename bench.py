@@ -45,6 +45,7 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip the batched 0-D and serving measurements")
     p.add_argument("--seed", type=int, default=1234)
     return p.parse_args()
 
@@ -200,6 +201,102 @@ def make_plan(mz, grid, walls, dt, step0, n_avg, graph=True):
 
 AR_MASS = 66.3e-27                 # data/particles.toml
 AR_VHS = (4.11e-10, 0.81, 273.0)   # data/vhs.toml: vhs_d, vhs_o, vhs_Tref
+
+
+def batched_0d(mz, ctx, seed, steps=20, warmup=2):
+    """Batched 0-D relaxation: 65,536 independent Ar cells with seeded
+    log-uniform particle counts in [50, 4000], bi-Maxwellian velocities (Tx =
+    2000 K, Ty = Tz = 300 K), Fnum = 1e13, V = 1, dt = 1e-6 s; one fused step =
+    ntc_equal_weight! + compute_props! for every cell, graph-replayed.  The
+    plain form launches ntc! cell by cell, then props, for one step."""
+    import numpy as np
+
+    n_cells = 65536
+    rng = np.random.default_rng(seed)
+    counts = np.floor(np.exp(rng.uniform(np.log(50), np.log(4000), n_cells))).astype(np.int64)
+    sp = [mz.Species("Ar", mz.AR_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    dom = mz.Domain(ctx, n_cells, sp, int(counts.sum()) + 1024, interactions=inter, seed=seed)
+    dom.sample_cells(0, counts, [2000.0, 300.0, 300.0], 1e13, step=0)
+    Tm = (2000.0 + 300.0 + 300.0) / 3
+    dom.set_sigma_g_w_max(0, 0, mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], Tm, Tm, 1e13))
+    n = int(counts.sum())
+    dt = 1e-6
+    inst = mz.PhysProps(dom)
+
+    def plan(step0):
+        p = mz._lib.StepPlan()
+        p.dims, p.collide, p.equal_weight, p.props, p.dt, p.step0, p.use_graph = 0, 1, 1, 1, dt, step0, 1
+        return p
+
+    dom.step(plan(0), warmup, inst)
+    dom.counters(reset=True)
+    ctx.synchronize()
+    ctx.timer_start()
+    dom.step(plan(warmup), steps, inst)
+    ms = ctx.timer_stop()
+    cnt = dom.counters(reset=True)
+    # plain: one launch sequence per cell (the reference's call granularity)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for c in range(n_cells):
+        dom.ntc(0, 0, dt, warmup + steps + 1, cells=(c, c + 1), equal_weight=True)
+    mz.compute_props(dom, inst)
+    ctx.synchronize()
+    plain_s = time.perf_counter() - t0
+    value = n * steps / (ms / 1e3)
+    out = {"workload": "0-D Ar relaxation, 65,536 cells, N log-uniform [50, 4000], bi-Maxwellian 2000/300/300 K",
+           "particles": n, "steps": steps, "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+           "collisions_per_s": cnt["accepted"] / (ms / 1e3), "plain_value": n / plain_s,
+           "batched_over_plain": value / (n / plain_s)}
+    dom.close()
+    return out
+
+
+def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
+    """Serving loop: seeded Poisson arrivals (mean `rate` per s over `window_s`)
+    of 0-D relaxation requests, 70 % Ar and 30 % Ar + He, particles
+    log-uniform in [200, 200,000] per species, temperatures uniform in [300,
+    5000] K, steps uniform in [50, 2000]; a common number density (Fnum = n V /
+    N), dt = 2.5e-3 s.  Requests are admitted by slots and a particle budget,
+    co-batched per step; p50 / p99 latency from arrival to result.  The plain
+    form runs requests one at a time on the same GPU."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sp = [mz.Species("Ar", mz.AR_MASS), mz.Species("He", mz.HE_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * window_s * 1.5)))
+    arrivals = arrivals[arrivals < window_s]
+    reqs = []
+    for k, t in enumerate(arrivals):
+        two = rng.random() < 0.3
+        c = [int(np.exp(rng.uniform(np.log(200), np.log(200_000)))),
+             int(np.exp(rng.uniform(np.log(200), np.log(200_000)))) if two else 0]
+        T = [rng.uniform(300.0, 5000.0), rng.uniform(300.0, 5000.0) if two else 0.0]
+        reqs.append((float(t), dict(counts=c, T=T, Fnum=2.2e16 / sum(c), n_steps=int(rng.integers(50, 2001)),
+                                    seed=int(seed) * 100_000 + k)))
+    srv = mz.Server(ctx, sp, inter, 2.5e-3, 1024, [40_000_000, 40_000_000])
+    lat, ids, elapsed = srv.serve(reqs)
+    info = srv.info()
+    srv.close()
+    lat = np.array(lat)
+    # plain: the first requests one at a time (arrival at 0, no overlap)
+    one = mz.Server(ctx, sp, inter, 2.5e-3, 1, [400_000, 400_000])
+    ps = 0
+    t0 = time.perf_counter()
+    for _, kw in reqs[:plain_sample]:
+        one.serve([(0.0, kw)])
+        ps += sum(kw["counts"]) * kw["n_steps"]
+    plain_s = time.perf_counter() - t0
+    one.close()
+    return {"workload": f"Poisson {rate:g}/s over {window_s:g} s, {len(reqs)} requests, 70 % Ar / 30 % Ar+He, "
+                        "N log-uniform [200, 2e5] per species, T [300, 5000] K, steps [50, 2000]",
+            "requests": len(reqs), "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "value": info["particle_steps"] / elapsed,
+            "unit": "particle-steps/s", "elapsed_s": elapsed, "server_steps": info["steps"],
+            "plain_value": ps / plain_s, "plain_sample": f"first {plain_sample} requests one at a time",
+            "batched_over_plain": (info["particle_steps"] / elapsed) / (ps / plain_s)}
 
 
 def cpu_oracle_run(args, steps, time_budget=None, nthreads=None):
@@ -389,8 +486,15 @@ def run_gpu(args):
                "note": f"initial state uploaded once ({h2d} B) inside the timed region, amortised over {K} steps; "
                        "cell properties (np, n, v, T) read back after every step"}
 
-    cpu = None
+    extra_0d = extra_srv = None
     log(f"e2e: {e2e}")
+    if not args.no_extra and rank == 0:
+        extra_0d = batched_0d(mz, ctx, seed)
+        log(f"batched 0-D: {extra_0d}")
+        extra_srv = serving(mz, ctx, seed)
+        log(f"serving: {extra_srv}")
+
+    cpu = None
     if not args.no_cpu_baseline and rank == 0:
         r = cpu_oracle_run(args, 20, time_budget=15.0)
         cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -403,7 +507,7 @@ def run_gpu(args):
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-               "plain": plain}
+               "plain": plain, "batched_0d": extra_0d, "serving": extra_srv}
         print(json.dumps(out), flush=True)
     ctx.close()
 

@@ -301,6 +301,9 @@ int mz_server_submit(mz_server* server, const mz_request* request, int64_t* id);
 int mz_server_step(mz_server* server, int64_t* n_running, int64_t* n_queued, int64_t* n_retired);
 /* state of a request and, once done, its final properties */
 int mz_server_result(mz_server* server, int64_t id, mz_request_result* out);
+/* ids of the requests the last mz_server_step retired (*n of them; up to
+ * max_ids written) */
+int mz_server_retired(mz_server* server, int64_t max_ids, int64_t* ids, int64_t* n);
 /* server steps run and particle-steps done so far */
 int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_steps);
 

@@ -102,6 +102,7 @@ struct mz_server_s {
     std::vector<int64_t> slot_req;  // request id per slot, 0 = free
     std::vector<int64_t> free_slots;
     std::vector<int64_t> running;   // ids of admitted, unfinished requests
+    std::vector<int64_t> retired;   // ids retired by the last mz_server_step
     // device scratch for admissions / retirements
     int32_t* d_cells = nullptr;
     uint64_t* d_seed = nullptr;
@@ -282,6 +283,7 @@ int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t
     mz_domain* d = sv->dom;
     admit(sv);
     int64_t running = (int64_t)sv->running.size(), retired = 0;
+    sv->retired.clear();
     if (running > 0) {
         mz_step_plan plan;
         memset(&plan, 0, sizeof plan);
@@ -327,6 +329,7 @@ int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t
                 }
                 q.res.steps_done = q.r.n_steps;
                 q.state = MZ_REQ_DONE;
+                sv->retired.push_back(k);
                 cells.push_back((int32_t)c);
                 sv->slot_req[c] = 0;
                 sv->free_slots.push_back(c);
@@ -362,6 +365,15 @@ int mz_server_result(mz_server* sv, int64_t id, mz_request_result* out)
     out->id = id;
     out->state = it->second.state;
     if (it->second.state == MZ_REQ_RUNNING) out->steps_done = sv->step - it->second.start_step;
+    API_CATCH(sv->ctx)
+}
+
+int mz_server_retired(mz_server* sv, int64_t max_ids, int64_t* ids, int64_t* n)
+{
+    API_TRY
+    MZ_REQUIRE(sv && n && (max_ids == 0 || ids), "mz_server_retired: NULL argument");
+    *n = (int64_t)sv->retired.size();
+    for (int64_t i = 0; i < std::min<int64_t>(max_ids, *n); ++i) ids[i] = sv->retired[i];
     API_CATCH(sv->ctx)
 }
 

@@ -566,6 +566,14 @@ class Server:
                     n=[out.n[s] for s in range(ns)], v=[[out.v[s][k] for k in range(3)] for s in range(ns)],
                     T=[out.T[s] for s in range(ns)])
 
+    def retired(self):
+        """ids of the requests the last step() retired"""
+        n = C.c_int64()
+        self._ck(lib().mz_server_retired(self.h, 0, None, C.byref(n)))
+        ids = np.zeros(max(1, n.value), np.int64)
+        self._ck(lib().mz_server_retired(self.h, n.value, ptr(ids, C.c_int64), C.byref(n)))
+        return ids[: n.value].tolist()
+
     def info(self):
         steps, ps = C.c_int64(), C.c_int64()
         self._ck(lib().mz_server_info(self.h, C.byref(steps), C.byref(ps)))
@@ -597,10 +605,9 @@ class Server:
             _, _, retired = self.step()
             if retired:
                 t = clock() - t0
-                for rid in list(pending):
-                    if self.result(rid)["state"] == L.MZ_REQ_DONE:
-                        lat[rid] = t - arrival[rid]
-                        pending.discard(rid)
+                for rid in self.retired():
+                    lat[rid] = t - arrival[rid]
+                    pending.discard(rid)
         return [lat[r] for r in ids], ids, clock() - t0
 
 
