@@ -116,7 +116,8 @@ typedef struct {
     double dw_tol;
     uint64_t step0;       /* RNG step index of the first step */
     int32_t use_graph;    /* capture the step in a CUDA graph and replay it */
-    int32_t reserved;
+    int32_t big_cell;     /* 0-D: cells of at least this many particles collide one block per cell
+                             (0: 2,048; < 0: never); results do not depend on it */
     mz_grid1d grid;
     mz_walls1d walls;
 } mz_step_plan;

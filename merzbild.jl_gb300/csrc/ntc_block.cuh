@@ -1,0 +1,211 @@
+// NTC of one large cell by a whole block: the block-per-cell mapping of the
+// equal-weight candidate loop (ntc_equal_weight!, collision_ntc.jl:479-521 and
+// :554-595).
+//
+// ntc_cell evaluates at most G <= 32 candidates of a cell at a time; a cell of
+// N particles offers about sqrt(pi N / 8) conflict-free candidates, so cells of
+// thousands of particles leave most of that parallelism unused and their
+// sequential chain of batches sets the length of a step.  Here a block of
+// NTC_BLOCK threads evaluates up to NTC_BLOCK candidates per batch with the
+// same semantics:
+//   * the batch ends before the first candidate that touches a particle of an
+//     earlier candidate in the batch: every particle of the batch goes into a
+//     shared-memory hash table that keeps the smallest candidate index using
+//     it (open addressing, at most 2 NTC_BLOCK keys in NTC_TABLE slots);
+//   * an inclusive block max-scan of sigma*g*w bit patterns gives every
+//     candidate the exact running maximum;
+//   * draws, screening, acceptance and scattering are those of ntc_cell, so
+//     the result equals the sequential loop (and ntc_cell) bit for bit.
+#pragma once
+
+#include <climits>
+
+#include "cell_ops.cuh"
+
+namespace mz {
+
+constexpr int NTC_BLOCK = 256;
+constexpr int NTC_TABLE = 2048;  // power of two, > 2 NTC_BLOCK / 0.5
+
+struct NtcBlockShared {
+    int32_t key[NTC_TABLE];
+    int32_t first[NTC_TABLE];
+    long long wmax[NTC_BLOCK / 32];
+    int32_t end;
+    int32_t accepted;
+    long long last_max;
+};
+
+__device__ __forceinline__ uint32_t ntc_hash(int32_t t) { return ((uint32_t)t * 0x9E3779B1u) >> (32 - 11); }
+
+__device__ __forceinline__ void ntc_table_insert(NtcBlockShared& sh, int32_t t, int32_t cand)
+{
+    uint32_t h = ntc_hash(t);
+    for (int probe = 0; probe < NTC_TABLE; ++probe) {
+        const int32_t prev = atomicCAS(&sh.key[h], -1, t);
+        if (prev == -1 || prev == t) {
+            atomicMin(&sh.first[h], cand);
+            return;
+        }
+        h = (h + 1) & (NTC_TABLE - 1);
+    }
+}
+
+__device__ __forceinline__ int32_t ntc_table_first(const NtcBlockShared& sh, int32_t t)
+{
+    uint32_t h = ntc_hash(t);
+    for (int probe = 0; probe < NTC_TABLE; ++probe) {
+        if (sh.key[h] == t) return sh.first[h];
+        h = (h + 1) & (NTC_TABLE - 1);
+    }
+    return INT_MAX;
+}
+
+// Equal-weight candidate loop of one cell by the whole block (all threads call
+// it with identical arguments).  Returns the new running maximum and the
+// number of accepted collisions (valid in every thread).
+__device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const Interaction& I, bool single,
+                                                    int32_t ncoll, double smax, const Cols& P1, const Cols& P2,
+                                                    const Indexer& p1, const Indexer& p2, const double2* trig,
+                                                    uint64_t seed, uint32_t pc, uint32_t stp, uint32_t rid)
+{
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, wid = tid >> 5;
+    const double vexp = fma(-2.0, I.vhs_o, 1.0);
+    const float lC = I.vhs_factor > 0.0 ? log2_pos(I.vhs_factor) : 1e30f;
+    const bool screen = fabsf(lC) < LOG_RANGE;
+    const float ex = 1.0f - (float)I.vhs_o;
+    const int32_t nl1 = p1.n1 + p1.n2;
+    const int32_t nl2 = single ? nl1 : p2.n1 + p2.n2;
+    const int32_t tagk = single ? 0 : (int32_t)0x40000000;  // species 2 particles get their own keys
+    NtcResult R;
+    R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
+    for (int32_t j0 = 0; j0 < ncoll;) {
+        const int32_t j = j0 + tid;
+        const bool valid = j < ncoll;
+        Stream st;
+        st.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)j);
+        int32_t i = -1, k = -1;
+        if (valid) {
+            i = floor_u52_times(st.u52(), nl1);
+            k = floor_u52_times(st.u52(), nl2);
+            if (single) {
+                int guard = 0;
+                while (i == k && guard++ < (1 << 20)) k = floor_u52_times(st.u52(), nl1);
+            }
+        }
+        for (int q = tid; q < NTC_TABLE; q += NTC_BLOCK) {
+            sh.key[q] = -1;
+            sh.first[q] = INT_MAX;
+        }
+        if (tid == 0) {
+            sh.end = min(NTC_BLOCK, ncoll - j0);
+            sh.accepted = 0;
+        }
+        __syncthreads();
+        if (valid) {
+            ntc_table_insert(sh, i, tid);
+            ntc_table_insert(sh, k | tagk, tid);
+        }
+        __syncthreads();
+        const bool conflict = valid && (ntc_table_first(sh, i) < tid || ntc_table_first(sh, k | tagk) < tid);
+        const int cmin = __reduce_min_sync(0xFFFFFFFFu, conflict ? tid : INT_MAX);
+        if (lane == 0 && cmin != INT_MAX) atomicMin(&sh.end, cmin);
+        __syncthreads();
+        const int B = sh.end;
+        const bool act = tid < B;
+
+        const float l_smax = log2_pos(smax);
+        const bool screen_b = screen && fabsf(l_smax) < 2.0f * LOG_RANGE;
+        int32_t si = 0, sk = 0;
+        PV a, b;
+        a.w = b.w = 0.0;
+        double g2 = 0.0, g = 0.0, sgw = -1.0, wmax = 0.0;
+        bool has = false, exact = false, have_g = false;
+        float ls = 0.0f;
+        if (act) {
+            si = map_slot(p1, i);
+            sk = map_slot(p2, k);
+            a = P1.wv[si];
+            b = P2.wv[sk];
+            const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
+            g2 = (gx * gx + gy * gy) + gz * gz;
+            wmax = dmax_pos(a.w, b.w);
+            if ((uint64_t)__double_as_longlong(g2) > G2_TINY_BITS) {
+                has = true;
+            } else {
+                g = sqrt(g2);
+                have_g = true;
+                has = g > EPS;
+            }
+            if (has) {
+                const float lw = log2_pos(wmax), lg = log2_pos(g2);
+                ls = lC + lw + ex * lg;
+                exact = !screen_b || fabsf(lw) >= LOG_RANGE || fabsf(lg) >= LOG_RANGE ||
+                        ls > l_smax - SCREEN_MARGIN;
+                if (exact) {
+                    if (!have_g) g = sqrt(g2);
+                    have_g = true;
+                    sgw = I.vhs_factor * pow(g, vexp) * g * wmax;
+                }
+            }
+        }
+        // block inclusive max-scan of the sigma*g*w bit patterns
+        long long mk = max_key(sgw, act && exact);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xFFFFFFFFu, mk, o);
+            if (lane >= o) mk = max(mk, t);
+        }
+        if (lane == 31) sh.wmax[wid] = mk;
+        __syncthreads();
+        long long before = __double_as_longlong(smax);
+        for (int w = 0; w < wid; ++w) before = max(before, sh.wmax[w]);
+        mk = max(mk, before);
+        if (tid == B - 1) sh.last_max = mk;
+        const double m = __longlong_as_double(mk);
+        bool acc = false;
+        if (act && has) {
+            const uint64_t um = st.u52();
+            if (exact) {
+                acc = u52_to_double(um) < sgw / m;
+            } else {
+                const float lm = log2_pos(m);
+                const float dl = ls - lm - log2_u52(um);
+                if (dl > SCREEN_MARGIN && fabsf(lm) < 2.0f * LOG_RANGE) {
+                    acc = true;
+                } else if (dl >= -SCREEN_MARGIN || fabsf(lm) >= 2.0f * LOG_RANGE) {
+                    if (!have_g) g = sqrt(g2);
+                    have_g = true;
+                    const double se = I.vhs_factor * pow(g, vexp) * g * wmax;
+                    acc = u52_to_double(um) < se / m;
+                }
+            }
+        }
+        if (acc) {
+            if (!have_g) g = sqrt(g2);
+            const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
+            const double cy = I.mu1 * a.vy + I.mu2 * b.vy;
+            const double cz = I.mu1 * a.vz + I.mu2 * b.vz;
+            double sphi, cphi;
+            sincos_2pi_u52(trig, st.u52(), sphi, cphi);
+            const double ct = fma(2.0, st.uniform(), -1.0);
+            const double sth = sqrt(1.0 - ct * ct);
+            const double nx = g * (sth * cphi), ny = g * (sth * sphi), nz = g * ct;
+            P1.wv[si] = PV{a.w, cx + I.mu2 * nx, cy + I.mu2 * ny, cz + I.mu2 * nz};
+            P2.wv[sk] = PV{b.w, cx - I.mu1 * nx, cy - I.mu1 * ny, cz - I.mu1 * nz};
+        }
+        const int na = __popc(__ballot_sync(0xFFFFFFFFu, acc));
+        if (lane == 0 && na) atomicAdd(&sh.accepted, na);
+        __syncthreads();
+        R.perf += sh.accepted;
+        smax = __longlong_as_double(sh.last_max);
+        j0 += B;
+        __syncthreads();
+    }
+    R.eqw = R.perf;
+    R.smax = smax;
+    return R;
+}
+
+}  // namespace mz

@@ -19,6 +19,7 @@
 // once in a CUDA graph and replayed.
 #include "cell_ops.cuh"
 #include "mz_host.h"
+#include "ntc_block.cuh"
 #include "sortnet.cuh"
 
 #include <algorithm>
@@ -51,6 +52,7 @@ struct StepArgs {
     unsigned int* hit_n;  // entries in hitq
     unsigned int* hit_done;  // last-block counter of k_wall_hits
     unsigned int hitq_cap;
+    int32_t big_cell;     // cells with at least this many particles collide in k_ntc_big
 };
 
 // cells of the per-warp destination histogram of k_cell (48 KB per block)
@@ -135,7 +137,13 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         // ntc_equal_weight! for every pair in the reference's order, one
         // group per cell
         const int c = c0 + gi;
-        if (a.physics && gi < nq) {
+        bool big = false;
+        if (gi < nq) {
+            int32_t tot = 0;
+            for (int s = 0; s < ns; ++s) tot += d.sp[s].ind[c].n1;
+            big = tot >= a.big_cell;
+        }
+        if (a.physics && gi < nq && !big) {
             const uint64_t seed = cell_seed(d, c);
             const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
             const double V = d.cell_V[c];
@@ -279,6 +287,55 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
     }
 }
 
+// ntc_equal_weight! of the cells with at least a.big_cell particles, one block
+// per cell (ntc_cell_block); k_cell skips their collisions.
+__global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
+{
+    __shared__ NtcBlockShared sh;
+    const uint32_t step = *a.step_ptr;
+    const int ns = d.n_species;
+    unsigned long long cand = 0, accd = 0;
+    for (int c = blockIdx.x; c < d.n_cells; c += gridDim.x) {
+        int32_t tot = 0;
+        for (int s = 0; s < ns; ++s) tot += d.sp[s].ind[c].n1;
+        if (tot < a.big_cell) continue;
+        const uint64_t seed = cell_seed(d, c);
+        const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
+        const double V = d.cell_V[c];
+        for (int s2 = 0; s2 < ns; ++s2) {
+            for (int s1 = s2; s1 < ns; ++s1) {
+                const bool single = s1 == s2;
+                const int cfi = s1 + ns * s2;
+                const SpeciesView& S1 = d.sp[s1];
+                const SpeciesView& S2 = d.sp[s2];
+                const Indexer q1 = S1.ind[c], q2 = S2.ind[c];
+                CollisionFactors cf = d.cf[(size_t)cfi * d.n_cells + c];
+                const uint32_t pc = (uint32_t)(s1 * ns + s2);
+                const int32_t ncoll = ntc_ncoll(d, cf, single, q1.n1, q2.n1, a.dt, V, seed, pc, stp, rid);
+                NtcResult R;
+                R.smax = cf.smax;
+                R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
+                if (ncoll > 0)
+                    R = ntc_cell_block(sh, d.inter[cfi], single, ncoll, cf.smax, a.gather ? S1.B : S1.A,
+                                       a.gather ? S2.B : S2.A, q1, q2, d.trig, seed, pc, stp, rid);
+                if (threadIdx.x == 0) {
+                    cand += ncoll;
+                    accd += R.perf;
+                    cf.smax = R.smax;
+                    cf.n_coll_performed = R.perf;
+                    cf.n_eq_w_coll_performed = R.eqw;
+                    d.cf[(size_t)cfi * d.n_cells + c] = cf;
+                }
+                __syncthreads();
+            }
+        }
+    }
+    if (threadIdx.x == 0 && (cand | accd)) {
+        atomicAdd(&d.counters->candidates, cand);
+        atomicAdd(&d.counters->accepted, accd);
+    }
+}
+
 // The wall-hit loop of convect_particles! (convection_1D.jl:22-46) for the
 // particles k_cell queued, one thread each, with the particle's own stream:
 // the same arithmetic and draws as in k_cell, but the FP64 work of diffuse
@@ -407,6 +464,9 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     }
     a.dt = plan->dt;
     a.dims = plan->dims;
+    // block-per-cell collisions for large 0-D cells (the 1-D step keeps every
+    // cell's phases in one warp)
+    a.big_cell = plan->dims == 0 && plan->big_cell >= 0 ? (plan->big_cell > 0 ? plan->big_cell : 2048) : INT_MAX;
     a.has_inst = inst != nullptr;
     a.has_avg = avg != nullptr && plan->avg_start > 0;
     if (inst) a.inst = PropsPtrs{inst->np, inst->n, inst->v, inst->T};
@@ -452,6 +512,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
+        if (physics && b.big_cell < INT_MAX)
+            MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
         MZ_LAUNCH(c, name, kern, blocks, 256, CELL_SMEM, v, b);
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
     };

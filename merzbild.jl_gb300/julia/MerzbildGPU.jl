@@ -88,7 +88,7 @@ end
 struct MzStepPlan
     dims::Int32; collide::Int32; equal_weight::Int32; props::Int32
     avg_start::Int64; n_avg::Int64; dt::Float64; dw_tol::Float64; step0::UInt64
-    use_graph::Int32; reserved::Int32
+    use_graph::Int32; big_cell::Int32
     grid::DeviceGrid1D; walls::DeviceWalls1D
 end
 

@@ -172,3 +172,44 @@ def test_fused_equals_standalone_ops_bitwise(ctx, orc):
     b, cb = device_logical(dom2, 0)
     assert np.array_equal(ca, cb)
     assert np.array_equal(a, b)
+
+
+def test_fused_0d_block_per_cell_equals_warp_groups_and_oracle(ctx, orc):
+    """Large 0-D cells collide one block per cell (ntc_cell_block) and small
+    ones in 8-lane groups; the mapping changes no result: block-per-cell for
+    cells of >= 2,048 particles, >= 64 particles, and never give identical
+    states, equal to the oracle's ntc_equal_weight! loop."""
+    sp = species(["Ar"])
+    inter = interactions(sp)
+    counts = np.array([100, 800, 2500, 5000, 3000, 50, 2048, 2047, 7000, 300])
+    n_cells, steps, dt, Fnum, T0 = len(counts), 6, 0.05, 1e13, 300.0
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], T0, T0, Fnum)
+    states = []
+    for big in (0, 64, -1):
+        dom = mz.Domain(ctx, n_cells, sp, int(counts.sum()) + 64, interactions=inter, seed=41)
+        dom.sample_cells(0, counts, T0, Fnum, step=0)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        plan = mz._lib.StepPlan()
+        plan.dims, plan.collide, plan.equal_weight, plan.props, plan.dt = 0, 1, 1, 1, dt
+        plan.use_graph, plan.big_cell = 1, big
+        inst = mz.PhysProps(dom)
+        dom.step(plan, steps, inst)
+        cnt = dom.counters()
+        states.append((device_logical(dom, 0), inst.fetch(), cnt))
+        dom.close()
+    (a, ca), pa, na = states[0]
+    assert na["accepted"] > 1000
+    for (b, cb), pb, nb in states[1:]:
+        assert np.array_equal(ca, cb) and np.array_equal(a, b)
+        assert np.array_equal(pa["T"], pb["T"]) and na["accepted"] == nb["accepted"]
+    o = orc.Oracle(n_cells, 1, [sp[0].mass])
+    o.load_interactions(*mz.VHS["Ar,Ar"])
+    o.pv_create(0, int(counts.sum()) + 64)
+    for c in range(n_cells):
+        o.sample_equal_weight(0, c + 1, int(counts[c]), T0, Fnum, seed=41, step=0)
+    o.cf_set_smax(0, 0, smax)
+    for tt in range(1, steps + 1):
+        o.ntc_cells(0, 0, dt, None, 41, tt, equal_weight=True, nthreads=8)
+    orows, oc = oracle_logical(o, 0)
+    assert np.array_equal(oc, ca)
+    assert_close_rows(orows, a, 1e-11, "0-D cells after 6 steps")
