@@ -308,6 +308,16 @@ int mz_server_retired(mz_server* server, int64_t max_ids, int64_t* ids, int64_t*
 /* server steps run and particle-steps done so far */
 int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_steps);
 
+/* Choose the fused step's mapping by timing it: every combination of lanes
+ * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the
+ * block-per-cell threshold (512, 2,048, 8,192 particles, never) runs
+ * trial_steps real steps of `plan` (starting at plan->step0; the state
+ * advances by 12 * trial_steps steps for 0-D plans, 3 * trial_steps for 1-D,
+ * and every mapping gives the same results); the fastest is kept for later
+ * mz_step calls whose plan leaves big_cell at 0.  No counterpart in the
+ * reference. */
+int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
+
 /* ---------------------------------------------------------------- counters */
 int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
 

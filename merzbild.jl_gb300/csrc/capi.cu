@@ -899,6 +899,18 @@ int mz_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* i
     API_CATCH(d->ctx)
 }
 
+int mz_step_autotune(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell)
+{
+    API_TRY
+    MZ_REQUIRE(d && plan, "mz_step_autotune: NULL argument");
+    MZ_REQUIRE(trial_steps >= 1, "mz_step_autotune: trial_steps must be >= 1");
+    MZ_REQUIRE(plan->dims == 0 || plan->dims == 1, "mz_step_autotune: dims must be 0 or 1");
+    MZ_CK(cudaSetDevice(d->ctx->device));
+    autotune_step(d, plan, trial_steps, lanes, big_cell);
+    check_status(d);
+    API_CATCH(d->ctx)
+}
+
 int mz_get_counters(mz_domain* d, mz_counters* out, int32_t reset)
 {
     API_TRY

@@ -104,6 +104,9 @@ struct mz_domain_s {
     unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block}
     void* d_hitq = nullptr;          // fused step: wall-hit queue (int4 entries)
     int64_t hitq_cap = 0;
+    // fused-step mapping chosen by mz_step_autotune (0: the default rules)
+    int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
+    int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
 };
 
 struct mz_props_s {
@@ -167,6 +170,7 @@ void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, d
 void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
                   const mz_octree_params* prm, const mz_grid1d* grid, uint64_t step, int64_t* n_merged);
 void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
+void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes_out, int32_t* big_out);
 void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v);
 void reserve_species(mz_domain* d, int s, int64_t cap);
 void launch_key_from_cell(mz_domain* d, int s);

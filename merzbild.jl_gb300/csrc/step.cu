@@ -466,7 +466,10 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.dims = plan->dims;
     // block-per-cell collisions for large 0-D cells (the 1-D step keeps every
     // cell's phases in one warp)
-    a.big_cell = plan->dims == 0 && plan->big_cell >= 0 ? (plan->big_cell > 0 ? plan->big_cell : 2048) : INT_MAX;
+    {
+        int32_t big = plan->big_cell != 0 ? plan->big_cell : (d->tuned_big != 0 ? d->tuned_big : 2048);
+        a.big_cell = plan->dims == 0 && big > 0 ? big : INT_MAX;
+    }
     a.has_inst = inst != nullptr;
     a.has_avg = avg != nullptr && plan->avg_start > 0;
     if (inst) a.inst = PropsPtrs{inst->np, inst->n, inst->v, inst->T};
@@ -496,7 +499,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         a.hitq_cap = (unsigned)std::min<int64_t>(d->hitq_cap, 0x7FFFFFFF);
     }
     const bool want_props = plan->props && (inst || a.has_avg);
-    const int G = ntc_group_width(d->n_cells);
+    const int G = d->tuned_lanes ? d->tuned_lanes : ntc_group_width(d->n_cells);
     void (*kern)(DomainView, StepArgs) = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
     int per_sm = 0;
     MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, CELL_SMEM));
@@ -570,4 +573,49 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             d->sp[s].hw = d->sp[s].n_total;
             d->sp[s].compact = true;
         }
+}
+
+// Time every mapping of the fused step on real steps of the simulation (the
+// mapping changes no result, so the trial steps are ordinary steps) and keep
+// the fastest for later mz_step calls: lanes per cell in the warp-group NTC
+// and, for 0-D cells, the particle count from which a cell collides one block
+// per cell.
+void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes_out, int32_t* big_out)
+{
+    mz_ctx* c = d->ctx;
+    const int32_t lanes_c[3] = {8, 16, 32};
+    const int32_t big_c[4] = {512, 2048, 8192, -1};
+    const int nb = plan->dims == 0 ? 4 : 1;
+    mz_step_plan p = *plan;
+    p.big_cell = 0;
+    float best = 3.0e38f;
+    int32_t bl = 0, bb = 0;
+    uint64_t step = plan->step0;
+    cudaEvent_t e0, e1;
+    MZ_CK(cudaEventCreate(&e0));
+    MZ_CK(cudaEventCreate(&e1));
+    for (int li = 0; li < 3; ++li)
+        for (int bi = 0; bi < nb; ++bi) {
+            d->tuned_lanes = lanes_c[li];
+            d->tuned_big = plan->dims == 0 ? big_c[bi] : -1;
+            p.step0 = step;
+            MZ_CK(cudaEventRecord(e0, c->stream));
+            launch_step(d, &p, trial_steps, nullptr, nullptr);
+            MZ_CK(cudaEventRecord(e1, c->stream));
+            MZ_CK(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            MZ_CK(cudaEventElapsedTime(&ms, e0, e1));
+            step += (uint64_t)trial_steps;
+            if (ms < best) {
+                best = ms;
+                bl = d->tuned_lanes;
+                bb = d->tuned_big;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    d->tuned_lanes = bl;
+    d->tuned_big = bb;
+    if (lanes_out) *lanes_out = bl;
+    if (big_out) *big_out = bb;
 }

@@ -116,6 +116,7 @@ _SIGS = {
     "mz_sample_grid_ndens": (i32, [vp, i32, P(Grid1D), d, d, d, u64]),
     "mz_step": (i32, [vp, P(StepPlan), i64, vp, vp]),
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
+    "mz_step_autotune": (i32, [vp, P(StepPlan), i64, P(i32), P(i32)]),
     "mz_sort_keys_noalloc": (i32, [vp, vp, i64, i32, vp, vp]),
     "mz_sincos_2pi": (i32, [vp, i64, P(u64), P(d), P(d)]),
     "mz_server_create": (i32, [vp, i32, P(d), P(Interaction), d, i64, P(i64), P(vp)]),

@@ -457,6 +457,13 @@ class Domain:
         self._ck(lib().mz_step(self.h, C.byref(plan), int(n_steps), inst.h if inst else None,
                                avg.h if avg else None))
 
+    def autotune(self, plan, trial_steps=2):
+        """mz_step_autotune: time each fused-step mapping on real steps (the
+        state advances) and keep the fastest; returns (lanes, big_cell)."""
+        lanes, big = C.c_int32(), C.c_int32()
+        self._ck(lib().mz_step_autotune(self.h, C.byref(plan), int(trial_steps), C.byref(lanes), C.byref(big)))
+        return lanes.value, big.value
+
     def counters(self, reset=False):
         c = L.Counters()
         self._ck(lib().mz_get_counters(self.h, C.byref(c), 1 if reset else 0))

@@ -213,3 +213,43 @@ def test_fused_0d_block_per_cell_equals_warp_groups_and_oracle(ctx, orc):
     orows, oc = oracle_logical(o, 0)
     assert np.array_equal(oc, ca)
     assert_close_rows(orows, a, 1e-11, "0-D cells after 6 steps")
+
+
+def test_autotuned_mapping_changes_no_result(ctx, orc):
+    """mz_step_autotune runs real steps under every mapping; the state after
+    tuning plus further steps equals the same number of steps run with the
+    default mapping, bit for bit (0-D and 1-D)."""
+    sp = species(["Ar"])
+    inter = interactions(sp)
+    counts = np.array([60, 900, 2600, 40, 5000, 1200, 300, 8200])
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], 300.0, 300.0, 1e13)
+    runs = []
+    for tune in (True, False):
+        dom = mz.Domain(ctx, len(counts), sp, int(counts.sum()) + 64, interactions=inter, seed=77)
+        dom.sample_cells(0, counts, 300.0, 1e13, step=0)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        plan = mz._lib.StepPlan()
+        plan.dims, plan.collide, plan.equal_weight, plan.props, plan.dt, plan.use_graph = 0, 1, 1, 1, 0.05, 1
+        done = 0
+        if tune:
+            lanes, big = dom.autotune(plan, trial_steps=1)
+            assert lanes in (8, 16, 32) and big in (512, 2048, 8192, -1)
+            done = 12
+        plan.step0 = done
+        dom.step(plan, 15 - done)
+        runs.append(device_logical(dom, 0))
+        dom.close()
+    assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][0], runs[1][0])
+
+    states = []
+    for tune in (True, False):
+        _, grid, walls, dt, _, dom, _ = couette_setup(ctx, orc, nx=40, ppc=100, seed=9)
+        plan = couette_plan(grid, walls, dt, props=False)
+        done = 0
+        if tune:
+            dom.autotune(plan, trial_steps=1)
+            done = 3
+        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 5 - done)
+        states.append(device_logical(dom, 0))
+        dom.close()
+    assert np.array_equal(states[0][1], states[1][1]) and np.array_equal(states[0][0], states[1][0])
