@@ -229,7 +229,9 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
         p.dims, p.collide, p.equal_weight, p.props, p.dt, p.step0, p.use_graph = 0, 1, 1, 1, dt, step0, 1
         return p
 
-    dom.step(plan(0), warmup, inst)
+    lanes, big = dom.autotune(plan(0), trial_steps=1)
+    dom.step(plan(12), warmup, inst)
+    warmup += 12
     dom.counters(reset=True)
     ctx.synchronize()
     ctx.timer_start()
@@ -246,7 +248,7 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
     plain_s = time.perf_counter() - t0
     value = n * steps / (ms / 1e3)
     out = {"workload": "0-D Ar relaxation, 65,536 cells, N log-uniform [50, 4000], bi-Maxwellian 2000/300/300 K",
-           "particles": n, "steps": steps, "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+           "particles": n, "steps": steps, "mapping": {"lanes_per_cell": lanes, "block_per_cell_from": big}, "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
            "collisions_per_s": cnt["accepted"] / (ms / 1e3), "plain_value": n / plain_s,
            "batched_over_plain": value / (n / plain_s)}
     dom.close()
@@ -383,13 +385,17 @@ def run_gpu(args):
     inst = mz.PhysProps(dom)
     avg = mz.PhysProps(dom)
     K, W = args.steps, args.warmup
-    # warm-up
-    dom.step(make_plan(mz, grid, walls, dt, 0, K), W, inst, avg)
+    # the autotuner times each mapping on real steps (3 steps before the
+    # warm-up), then W untimed warm-up steps
+    tune_steps = 3 * 4
+    mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=4)
+    dom.step(make_plan(mz, grid, walls, dt, tune_steps, K), W, inst, avg)
     ctx.synchronize()
-    log("warm-up done")
+    log(f"warm-up done (mapping: {mapping[0]} lanes per cell)")
     mz.clear_props(avg)
     dom.counters(reset=True)
-    plan = make_plan(mz, grid, walls, dt, W, K)
+    step0 = tune_steps + W
+    plan = make_plan(mz, grid, walls, dt, step0, K)
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = ctx.launch_count()
@@ -414,7 +420,7 @@ def run_gpu(args):
     log("kernel timing pass")
     ctx.set_kernel_timing(True)
     kt_steps = max(3, min(K, 6))
-    dom.step(make_plan(mz, grid, walls, dt, W + K, kt_steps, graph=False), kt_steps, inst, avg)
+    dom.step(make_plan(mz, grid, walls, dt, step0 + K, kt_steps, graph=False), kt_steps, inst, avg)
     timings = ctx.kernel_timings()
     ctx.set_kernel_timing(False)
     tot = sum(v[0] for v in timings.values())
@@ -442,7 +448,7 @@ def run_gpu(args):
     plain = None
     log("roofline: " + json.dumps({k: (v if not isinstance(v, dict) else None) for k, v in roofline.items()}))
     if not args.no_plain and rank == 0:
-        rng = mz.PhiloxRNG(seed, W + K + kt_steps)
+        rng = mz.PhiloxRNG(seed, step0 + K + kt_steps)
         pp = mz.PhysProps(dom)
         ctx.synchronize()
         t0 = time.perf_counter()
@@ -503,7 +509,8 @@ def run_gpu(args):
         out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
                "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, sampled on the device)",
-               "config": workload(args) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+               "config": workload(args) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                                           "mapping": {"lanes_per_cell": mapping[0], "autotune_steps": tune_steps}},
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,

@@ -369,7 +369,8 @@ __device__ __forceinline__ void props_pass1_into_lane(double n, double sx, doubl
 }
 
 __device__ __forceinline__ CellMoments props_cells_finish(const Cols& P, const Indexer* ind, int c0, int nq,
-                                                          double mass, double mn, double msx, double msy, double msz)
+                                                          double mass, double mn, double msx, double msy, double msz,
+                                                          unsigned skip = 0u)
 {
     const int lane = threadIdx.x & 31;
     CellMoments r;
@@ -382,6 +383,7 @@ __device__ __forceinline__ CellMoments props_cells_finish(const Cols& P, const I
     }
     double mE = 0.0;
     for (int q = 0; q < nq; ++q) {
+        if ((skip >> q) & 1u) continue;
         const Indexer p = ind[c0 + q];
         const double ux = __shfl_sync(0xFFFFFFFFu, r.ux, q), uy = __shfl_sync(0xFFFFFFFFu, r.uy, q);
         const double uz = __shfl_sync(0xFFFFFFFFu, r.uz, q);
@@ -398,11 +400,15 @@ __device__ __forceinline__ CellMoments props_cells_finish(const Cols& P, const I
     return r;
 }
 
-__device__ __forceinline__ CellMoments props_cells(const Cols& P, const Indexer* ind, int c0, int nq, double mass)
+// cells with bit q of `skip` set are left out (their props come from a
+// block-per-cell pass)
+__device__ __forceinline__ CellMoments props_cells(const Cols& P, const Indexer* ind, int c0, int nq, double mass,
+                                                   unsigned skip = 0u)
 {
     const int lane = threadIdx.x & 31;
     double mn = 0.0, msx = 0.0, msy = 0.0, msz = 0.0;
     for (int q = 0; q < nq; ++q) {
+        if ((skip >> q) & 1u) continue;
         const Indexer p = ind[c0 + q];
         double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
         for (int j = lane; j < p.n1; j += 32) {
@@ -414,7 +420,57 @@ __device__ __forceinline__ CellMoments props_cells(const Cols& P, const Indexer*
         }
         props_pass1_into_lane(n, sx, sy, sz, q, mn, msx, msy, msz);
     }
-    return props_cells_finish(P, ind, c0, nq, mass, mn, msx, msy, msz);
+    return props_cells_finish(P, ind, c0, nq, mass, mn, msx, msy, msz, skip);
+}
+
+// n, u, T of one large cell's group-1 list by a whole block (two passes as
+// props_cell; the sums are combined per warp, then by thread 0 over the
+// warps).  `red` is shared memory of 4 doubles per warp.  Valid in every
+// thread.
+__device__ __forceinline__ CellMoments props_cell_block(const Cols& P, const Indexer& p, double mass, double* red)
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int j = tid; j < p.n1; j += blockDim.x) {
+        const PV r = P.wv[p.start1 + j];
+        n += r.w;
+        sx += r.vx * r.w;
+        sy += r.vy * r.w;
+        sz += r.vz * r.w;
+    }
+    const double t = warp_sum4(n, sx, sy, sz);
+    if ((lane & 7) == 0) red[4 * wid + (lane >> 3)] = t;
+    __syncthreads();
+    double tn = 0.0, tx = 0.0, ty = 0.0, tz = 0.0;
+    for (int w = 0; w < nw; ++w) {
+        tn += red[4 * w];
+        tx += red[4 * w + 1];
+        ty += red[4 * w + 2];
+        tz += red[4 * w + 3];
+    }
+    __syncthreads();
+    CellMoments r;
+    r.n = tn;
+    r.ux = r.uy = r.uz = r.T = 0.0;
+    if (tn > 0.0) {
+        r.ux = tx / tn;
+        r.uy = ty / tn;
+        r.uz = tz / tn;
+    }
+    double E = 0.0;
+    for (int j = tid; j < p.n1; j += blockDim.x) {
+        const PV u = P.wv[p.start1 + j];
+        const double dx = u.vx - r.ux, dy = u.vy - r.uy, dz = u.vz - r.uz;
+        E = fma(u.w, (dx * dx + dy * dy) + dz * dz, E);
+    }
+    E = warp_sum(E);
+    if (lane == 0) red[wid] = E;
+    __syncthreads();
+    double tE = 0.0;
+    for (int w = 0; w < nw; ++w) tE += red[w];
+    __syncthreads();
+    if (tn > 0.0) r.T = (2.0 / 3.0) * (tE * (0.5 * mass / (tn * K_B)));
+    return r;
 }
 
 // ------------------------------------------------------------------ convection

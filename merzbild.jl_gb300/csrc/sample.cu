@@ -5,7 +5,8 @@
 // configurations (not in the reference): per-axis temperatures (a
 // bi-Maxwellian) and log-uniform weights.
 //
-// Every particle draws from its own stream keyed on (cell, particle #):
+// Every particle draws from its own stream keyed on (cell, particle #), one
+// thread per particle:
 // 3 position draws, then the velocity draws, then one weight draw if the
 // weights are log-uniform.  log(1 - U) replaces log(U) so U == 0 cannot give
 // an infinite speed.
@@ -31,88 +32,95 @@ struct SampleArgs {
     uint32_t step;
 };
 
-__global__ void __launch_bounds__(256) k_sample(DomainView d, int s, SampleArgs a)
+// indexers of the sampled cells (lists appended at base[c])
+__global__ void k_sample_cells(DomainView d, int s, SampleArgs a)
 {
     const SpeciesView& S = d.sp[s];
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < d.n_cells; c += nwarps) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d.n_cells; c += gridDim.x * blockDim.x) {
         const int32_t n = a.counts[c];
         if (n <= 0) continue;
-        const int32_t b = a.base[c];
-        if (lane == 0) {
-            const Indexer old = S.ind[c];
-            if (old.n1 + old.n2 != 0) set_status(d, ST_CAPACITY);
-            Indexer p;
-            p.start1 = b;
-            p.n1 = n;
-            p.start2 = 0;
-            p.n2 = 0;
-            S.ind[c] = p;
+        const Indexer old = S.ind[c];
+        if (old.n1 + old.n2 != 0) set_status(d, ST_CAPACITY);
+        S.ind[c] = Indexer{a.base[c], n, 0, 0};
+    }
+}
+
+// One thread per new particle (a cell of 10^5 particles spreads over the
+// whole GPU); the particle's cell is found by bisection of the cell bases, and
+// its stream is keyed on (cell, particle # in the cell) as before.
+__global__ void __launch_bounds__(256) k_sample(DomainView d, int s, SampleArgs a, int64_t hw, int64_t total)
+{
+    const SpeciesView& S = d.sp[s];
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t x = hw + g;
+        // last cell c with base[c] <= x (cells without particles share their successor's base)
+        int lo = 0, hi = d.n_cells - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((int64_t)a.base[mid] <= x) lo = mid;
+            else hi = mid - 1;
         }
-        double lo[3], hi[3];
+        const int c = lo;
+        const int32_t j = (int32_t)(x - a.base[c]);
+        double lo3[3], hi3[3];
         if (a.grid_box) {
-            lo[0] = (double)c * a.dx;
-            hi[0] = (double)(c + 1) * a.dx;
-            lo[1] = 0.0;
-            hi[1] = 1.0;
-            lo[2] = 0.0;
-            hi[2] = 1.0;
+            lo3[0] = (double)c * a.dx;
+            hi3[0] = (double)(c + 1) * a.dx;
+            lo3[1] = 0.0;
+            hi3[1] = 1.0;
+            lo3[2] = 0.0;
+            hi3[2] = 1.0;
         } else if (a.box6) {
             for (int k = 0; k < 3; ++k) {
-                lo[k] = a.box6[6 * (int64_t)c + 2 * k];
-                hi[k] = a.box6[6 * (int64_t)c + 2 * k + 1];
+                lo3[k] = a.box6[6 * (int64_t)c + 2 * k];
+                hi3[k] = a.box6[6 * (int64_t)c + 2 * k + 1];
             }
         } else {
             for (int k = 0; k < 3; ++k) {
-                lo[k] = 0.0;
-                hi[k] = 1.0;
+                lo3[k] = 0.0;
+                hi3[k] = 1.0;
             }
         }
         double T[3];
         for (int k = 0; k < 3; ++k) T[k] = a.T3 ? a.T3[3 * (int64_t)c + k] : a.T3_all[k];
         const double Fn = a.Fnum[c];
-        const uint64_t seed = cell_seed(d, c);
-        const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, a.step);
-        for (int j = lane; j < n; j += 32) {
-            Stream st;
-            st.init(seed, TAG_SAMPLE, (uint32_t)s, stp, rid, (uint32_t)j);
-            const int64_t q = (int64_t)b + j;
-            double x[3];
-            for (int k = 0; k < 3; ++k) x[k] = lo[k] + st.uniform() * (hi[k] - lo[k]);
-            double vx, vy, vz;
-            if (a.dist == 1) {
-                const double vs = sqrt(2.0 * K_B * T[0] / S.mass) * sqrt(0.3);
-                double z[6];
-                for (int k = 0; k < 3; ++k) {
-                    const double r = sqrt(-2.0 * log(1.0 - st.uniform()));
-                    const double ang = TWOPI * st.uniform();
-                    z[2 * k] = r * cos(ang);
-                    z[2 * k + 1] = r * sin(ang);
-                }
-                const double vabs = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2] + z[3] * z[3] + z[4] * z[4]);
-                const double th = st.uniform() * 3.141592653589793;
-                const double ph = st.uniform() * TWOPI;
-                const double sth = sin(th);
-                vx = vs * (vabs * sth * cos(ph));
-                vy = vs * (vabs * sth * sin(ph));
-                vz = vs * (vabs * cos(th));
-            } else {
-                const double vn = sqrt(-log(1.0 - st.uniform()));
-                const double vr = sqrt(-log(1.0 - st.uniform()));
-                const double t1 = TWOPI * st.uniform();
-                const double t2 = TWOPI * st.uniform();
-                vx = sqrt(2.0 * K_B * T[0] / S.mass) * (vn * cos(t1));
-                vy = sqrt(2.0 * K_B * T[1] / S.mass) * (vr * cos(t2));
-                vz = sqrt(2.0 * K_B * T[2] / S.mass) * (vr * sin(t2));
+        Stream st;
+        st.init(cell_seed(d, c), TAG_SAMPLE, (uint32_t)s, cell_step(d, c, a.step), cell_rid(d, c), (uint32_t)j);
+        const int64_t q = x;
+        double xx[3];
+        for (int k = 0; k < 3; ++k) xx[k] = lo3[k] + st.uniform() * (hi3[k] - lo3[k]);
+        double vx, vy, vz;
+        if (a.dist == 1) {
+            const double vs = sqrt(2.0 * K_B * T[0] / S.mass) * sqrt(0.3);
+            double z[6];
+            for (int k = 0; k < 3; ++k) {
+                const double r = sqrt(-2.0 * log(1.0 - st.uniform()));
+                const double ang = TWOPI * st.uniform();
+                z[2 * k] = r * cos(ang);
+                z[2 * k + 1] = r * sin(ang);
             }
-            double w = Fn;
-            if (a.span > 0.0) w = Fn * pow(10.0, a.span * (2.0 * st.uniform() - 1.0));
-            S.A.wv[q] = PV{w, vx, vy, vz};
-            S.A.pos[q] = PX{x[0], x[1], x[2], 0.0};
-            S.cell[q] = c;
-            S.key[q] = c;
+            const double vabs = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2] + z[3] * z[3] + z[4] * z[4]);
+            const double th = st.uniform() * 3.141592653589793;
+            const double ph = st.uniform() * TWOPI;
+            const double sth = sin(th);
+            vx = vs * (vabs * sth * cos(ph));
+            vy = vs * (vabs * sth * sin(ph));
+            vz = vs * (vabs * cos(th));
+        } else {
+            const double vn = sqrt(-log(1.0 - st.uniform()));
+            const double vr = sqrt(-log(1.0 - st.uniform()));
+            const double t1 = TWOPI * st.uniform();
+            const double t2 = TWOPI * st.uniform();
+            vx = sqrt(2.0 * K_B * T[0] / S.mass) * (vn * cos(t1));
+            vy = sqrt(2.0 * K_B * T[1] / S.mass) * (vr * cos(t2));
+            vz = sqrt(2.0 * K_B * T[2] / S.mass) * (vr * sin(t2));
         }
+        double w = Fn;
+        if (a.span > 0.0) w = Fn * pow(10.0, a.span * (2.0 * st.uniform() - 1.0));
+        S.A.wv[q] = PV{w, vx, vy, vz};
+        S.A.pos[q] = PX{xx[0], xx[1], xx[2], 0.0};
+        S.cell[q] = c;
+        S.key[q] = c;
     }
 }
 
@@ -147,8 +155,12 @@ static void run_sample(mz_domain* d, int s, SampleArgs a, int32_t* counts_dev)
     a.counts = counts_dev;
     a.base = S.work;
     DomainView v = make_view(d);
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells * 32, 256), (int64_t)c->num_sms * 16));
-    MZ_LAUNCH(c, "sample", k_sample, blocks, 256, 0, v, s, a);
+    const int cb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells, 256), (int64_t)c->num_sms * 8));
+    MZ_LAUNCH(c, "sample_cells", k_sample_cells, cb, 256, 0, v, s, a);
+    if (total > 0) {
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(total, 256), (int64_t)c->num_sms * 16));
+        MZ_LAUNCH(c, "sample", k_sample, blocks, 256, 0, v, s, a, S.hw, total);
+    }
     S.hw += total;
     S.n_total += total;
 }

@@ -178,10 +178,16 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         __syncwarp();
         // 0-D: compute_props! after the collisions of this step
         if (a.props && a.props_lag == 0) {
+            // large cells get their props in k_ntc_big
+            const unsigned skip = __ballot_sync(0xFFFFFFFFu, grp.rank == 0 && big) >> 0;
+            unsigned skipq = 0u;
+            for (int q = 0; q < nq; ++q)
+                if ((skip >> (q * G)) & 1u) skipq |= 1u << q;
             for (int s = 0; s < ns; ++s) {
                 const SpeciesView& S = d.sp[s];
-                const CellMoments r = props_cells(a.gather ? S.B : S.A, S.ind, c0, nq, S.mass);
-                if (lane < nq) write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
+                const CellMoments r = props_cells(a.gather ? S.B : S.A, S.ind, c0, nq, S.mass, skipq);
+                if (lane < nq && !((skipq >> lane) & 1u))
+                    write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
             }
         }
         if (a.dims != 1 || !a.physics) continue;
@@ -287,11 +293,13 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
     }
 }
 
-// ntc_equal_weight! of the cells with at least a.big_cell particles, one block
-// per cell (ntc_cell_block); k_cell skips their collisions.
+// ntc_equal_weight! and the 0-D compute_props! of the cells with at least
+// a.big_cell particles, one block per cell (ntc_cell_block, props_cell_block);
+// k_cell skips these cells' collisions and props.
 __global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
 {
     __shared__ NtcBlockShared sh;
+    __shared__ double red[4 * (NTC_BLOCK / 32)];
     const uint32_t step = *a.step_ptr;
     const int ns = d.n_species;
     unsigned long long cand = 0, accd = 0;
@@ -302,7 +310,7 @@ __global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
         const uint64_t seed = cell_seed(d, c);
         const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
         const double V = d.cell_V[c];
-        for (int s2 = 0; s2 < ns; ++s2) {
+        for (int s2 = 0; s2 < ns && a.physics; ++s2) {
             for (int s1 = s2; s1 < ns; ++s1) {
                 const bool single = s1 == s2;
                 const int cfi = s1 + ns * s2;
@@ -327,6 +335,15 @@ __global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
                     d.cf[(size_t)cfi * d.n_cells + c] = cf;
                 }
                 __syncthreads();
+            }
+        }
+        // 0-D: compute_props! of the cell after its collisions
+        if (a.props && a.props_lag == 0) {
+            for (int s = 0; s < ns; ++s) {
+                const SpeciesView& S = d.sp[s];
+                const Indexer p = S.ind[c];
+                const CellMoments r = props_cell_block(a.gather ? S.B : S.A, p, S.mass, red);
+                if (threadIdx.x == 0) write_props(a, (int64_t)c + (int64_t)d.n_cells * s, r, p.n1, step);
             }
         }
     }
@@ -483,7 +500,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.next = d->d_done + 1;
     a.hit_n = d->d_done + 2;
     a.hit_done = d->d_done + 3;
-    {
+    if (plan->dims == 1) {
         // wall-hit queue: a fraction of the particles; overflow is handled inline
         int64_t n_all = 0;
         for (int s = 0; s < d->ns; ++s) n_all += d->sp[s].n_total;
@@ -515,7 +532,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
-        if (physics && b.big_cell < INT_MAX)
+        if ((physics || props) && b.big_cell < INT_MAX)
             MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
         MZ_LAUNCH(c, name, kern, blocks, 256, CELL_SMEM, v, b);
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);

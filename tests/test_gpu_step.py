@@ -201,7 +201,10 @@ def test_fused_0d_block_per_cell_equals_warp_groups_and_oracle(ctx, orc):
     assert na["accepted"] > 1000
     for (b, cb), pb, nb in states[1:]:
         assert np.array_equal(ca, cb) and np.array_equal(a, b)
-        assert np.array_equal(pa["T"], pb["T"]) and na["accepted"] == nb["accepted"]
+        assert na["accepted"] == nb["accepted"]
+        # the block-per-cell props sum in another order: equal to round-off
+        assert np.array_equal(pa["np"], pb["np"])
+        assert np.allclose(pa["T"], pb["T"], rtol=1e-13, atol=0) and np.allclose(pa["n"], pb["n"], rtol=1e-14)
     o = orc.Oracle(n_cells, 1, [sp[0].mass])
     o.load_interactions(*mz.VHS["Ar,Ar"])
     o.pv_create(0, int(counts.sum()) + 64)
