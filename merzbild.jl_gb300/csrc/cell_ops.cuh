@@ -430,8 +430,23 @@ __device__ __forceinline__ CellMoments props_cells(const Cols& P, const Indexer*
 __device__ __forceinline__ CellMoments props_cell_block(const Cols& P, const Indexer& p, double mass, double* red)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    const int nt = blockDim.x;
     double n = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int j = tid; j < p.n1; j += blockDim.x) {
+    // four records in flight per thread: a long list is latency-bound
+    int j = tid;
+    for (; j + 3 * nt < p.n1; j += 4 * nt) {
+        PV r[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) r[u] = P.wv[p.start1 + j + u * nt];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            n += r[u].w;
+            sx += r[u].vx * r[u].w;
+            sy += r[u].vy * r[u].w;
+            sz += r[u].vz * r[u].w;
+        }
+    }
+    for (; j < p.n1; j += nt) {
         const PV r = P.wv[p.start1 + j];
         n += r.w;
         sx += r.vx * r.w;
@@ -458,7 +473,18 @@ __device__ __forceinline__ CellMoments props_cell_block(const Cols& P, const Ind
         r.uz = tz / tn;
     }
     double E = 0.0;
-    for (int j = tid; j < p.n1; j += blockDim.x) {
+    j = tid;
+    for (; j + 3 * nt < p.n1; j += 4 * nt) {
+        PV q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = P.wv[p.start1 + j + u * nt];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double dx = q[u].vx - r.ux, dy = q[u].vy - r.uy, dz = q[u].vz - r.uz;
+            E = fma(q[u].w, (dx * dx + dy * dy) + dz * dz, E);
+        }
+    }
+    for (; j < p.n1; j += nt) {
         const PV u = P.wv[p.start1 + j];
         const double dx = u.vx - r.ux, dy = u.vy - r.uy, dz = u.vz - r.uz;
         E = fma(u.w, (dx * dx + dy * dy) + dz * dz, E);
