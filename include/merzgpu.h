@@ -55,6 +55,7 @@ enum {
 typedef struct mz_ctx_s mz_ctx;
 typedef struct mz_domain_s mz_domain;
 typedef struct mz_props_s mz_props;
+typedef struct mz_surf_props_s mz_surf_props;
 
 /* Interaction (collision_utils.jl:73-82) */
 typedef struct {
@@ -210,6 +211,34 @@ int mz_props_download(mz_props* p, double* lpa, double* np, double* n, double* v
  * MZ_CONVECT_COMPUTE_CELL, convect_particles_and_compute_cell! (:225-255) */
 int mz_convect_1d(mz_domain* dom, int32_t species, const mz_grid1d* grid, const mz_walls1d* walls, double dt,
                   uint64_t step, int32_t flags);
+
+/* Surface properties of the two walls of a 1-D grid: SurfProps(pia, grid)
+ * (surface_props.jl:22-67; element 1 = left wall, normal +x, element 2 =
+ * right wall, normal -x, unit areas).  Downloads use the reference's layouts:
+ * np, flux_incident, flux_reflected, normal_pressure, kinetic_energy_flux are
+ * (2, n_species), force and shear_pressure (3, 2, n_species), column-major.
+ * Sums are accumulated with atomic additions: equal to the sequential sums up
+ * to round-off, not bit for bit. */
+int mz_surf_props_create(mz_domain* dom, mz_surf_props** out);
+int mz_surf_props_destroy(mz_surf_props* surf);
+/* clear_props!(surf_props) (surface_props.jl:176-196) */
+int mz_surf_props_clear(mz_surf_props* surf);
+/* avg_props!(surf_props_avg, surf_props, n_avg_timesteps) (surface_props.jl:205-226) */
+int mz_surf_avg_props(mz_surf_props* avg, const mz_surf_props* inst, double n_avg_timesteps);
+int mz_surf_props_download(mz_surf_props* surf, double* np, double* flux_incident, double* flux_reflected,
+                           double* force, double* normal_pressure, double* shear_pressure, double* kinetic_energy_flux);
+/* convect_particles!(rng, grid, boundaries, particles, pia, species,
+ * species_data, surf_props, dt) (convection_1D.jl:176-206): this species'
+ * entries are cleared, every wall hit adds its incident and reflected
+ * contributions, and the sums are scaled by mass / dt / area
+ * (surface_props_scale!).  (The reference clears every species' entries.) */
+int mz_convect_1d_surf(mz_domain* dom, int32_t species, const mz_grid1d* grid, const mz_walls1d* walls, double dt,
+                       uint64_t step, int32_t flags, mz_surf_props* surf);
+/* Attach surface sets to the fused 1-D step: every step clears inst,
+ * samples the walls during convection, scales, and (avg != NULL) adds inst /
+ * plan->n_avg to avg from plan->avg_start on, like avg_props!.  NULL detaches.
+ * No counterpart in the reference (its time loops call the functions above). */
+int mz_step_set_surface(mz_domain* dom, mz_surf_props* inst, mz_surf_props* avg);
 
 /* ---------------------------------------------------------------- sorting */
 /* sort_particles!(gridsort, grid, ...) when grid != NULL (cells from x,

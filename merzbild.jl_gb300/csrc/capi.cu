@@ -385,6 +385,11 @@ int mz_domain_destroy(mz_domain* d)
     cudaStreamSynchronize(d->ctx->stream);
     for (mz_props* p : d->props) free_props(p);
     d->props.clear();
+    for (mz_surf_props* p : d->surf) {
+        cudaFree(p->acc);
+        delete p;
+    }
+    d->surf.clear();
     for (int s = 0; s < d->ns; ++s) {
         free_species(d->sp[s]);
         cudaFree(d->sp[s].counts);

@@ -524,9 +524,73 @@ __device__ __forceinline__ void diffuse_reflect(Stream& st, const double2* trig,
     vz = cR * vt + wv[2];
 }
 
+// Surface sampling of the two walls of a 1-D grid (SurfProps,
+// surface_props.jl:22-67): element 0 = left wall (normal +x), 1 = right wall
+// (normal -x); per element 11 sums: np, flux_incident, flux_reflected,
+// force xyz, normal_pressure, shear_pressure xyz, kinetic_energy_flux.
+// A thread keeps its sums in registers (constant indices) and a block flushes
+// them with one atomic addition per quantity.
+constexpr int SURF_Q = 11;
+
+struct SurfAcc {
+    double q[2][SURF_Q];
+};
+
+// update_surface_incident! (surface_props.jl:78-101, sign +1) and
+// update_surface_reflected! (:113-134, sign -1) of element e
+__device__ __forceinline__ void surf_update(SurfAcc& a, int e, double w, double vx, double vy, double vz,
+                                            bool reflected)
+{
+    const double nx = e == 0 ? 1.0 : -1.0;
+    const double px = w * vx, py = w * vy, pz = w * vz;
+    const double pn = px * nx;
+    const double sg = reflected ? -1.0 : 1.0;
+    double u[SURF_Q];
+    u[0] = reflected ? 0.0 : 1.0;
+    u[1] = reflected ? 0.0 : w;
+    u[2] = reflected ? -w : 0.0;
+    u[3] = sg * px;
+    u[4] = sg * py;
+    u[5] = sg * pz;
+    u[6] = -sg * pn;
+    u[7] = sg * (px - pn * nx);
+    u[8] = sg * py;
+    u[9] = sg * pz;
+    u[10] = sg * (0.5 * (px * vx + py * vy + pz * vz));
+#pragma unroll
+    for (int k = 0; k < SURF_Q; ++k) {
+        a.q[0][k] += e == 0 ? u[k] : 0.0;
+        a.q[1][k] += e == 1 ? u[k] : 0.0;
+    }
+}
+
+// block sum of every thread's SurfAcc into dst[2][SURF_Q] (one atomic per
+// quantity per block); all threads of the block call it
+__device__ __forceinline__ void surf_flush(const SurfAcc& a, double* dst, bool any)
+{
+    __shared__ double part[2 * SURF_Q];
+    __shared__ int active;
+    if (threadIdx.x == 0) active = 0;
+    if (threadIdx.x < 2 * SURF_Q) part[threadIdx.x] = 0.0;
+    __syncthreads();
+    if (__any_sync(0xFFFFFFFFu, any) && (threadIdx.x & 31) == 0) atomicOr(&active, 1);
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+            for (int k = 0; k < SURF_Q; ++k) {
+                const double v = warp_sum(a.q[e][k]);
+                if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&part[e * SURF_Q + k], v);
+            }
+        __syncthreads();
+        if (threadIdx.x < 2 * SURF_Q && part[threadIdx.x] != 0.0) atomicAdd(&dst[threadIdx.x], part[threadIdx.x]);
+    }
+}
+
 // wall-hit loop of convect_single_particle! (convection_1D.jl:22-42); returns hits
 __device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int s, double& x, double& vx, double& vy,
-                                             double& vz, double dt, bool& cap)
+                                             double& vz, double dt, bool& cap, SurfAcc* surf = nullptr, double w = 0.0)
 {
     double t_rest = dt;
     double x_old = x;
@@ -551,6 +615,7 @@ __device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int 
             normal = 1.0;
             x_old = 0.0;
         }
+        if (surf) surf_update(*surf, bc, w, vx, vy, vz, false);
         // reflect_particle_x! (boundary_conditions.jl:108-121)
         const double acc = W.acc[bc];
         if (acc == 0.0) {
@@ -563,6 +628,7 @@ __device__ __forceinline__ int convect_walls(Stream& st, const WallView& W, int 
             else
                 vx = -vx;
         }
+        if (surf) surf_update(*surf, bc, w, vx, vy, vz, true);
         x_new = fma(vx, t_rest, x_old);
     }
     x = fmin(fmax(x_new, W.min_x), W.max_x);

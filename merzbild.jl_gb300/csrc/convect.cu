@@ -17,11 +17,12 @@ using namespace mz;
 namespace {
 
 __global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw, WallView W, double dt, uint32_t step,
-                                                 int compute_cell)
+                                                 int compute_cell, double* surf)
 {
     const SpeciesView& S = d.sp[s];
     unsigned long long my_hits = 0;
     bool cap = false;
+    SurfAcc acc = {};
     for (int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < hw;
          slot += (int64_t)gridDim.x * blockDim.x) {
         const int32_t c = S.cell[slot];
@@ -37,7 +38,7 @@ __global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw
         if (!move_free(W, xn, x)) {
             const PV r = S.A.wv[slot];
             double vy = r.vy, vz = r.vz;
-            my_hits += convect_walls(st, W, s, x, vx, vy, vz, dt, cap);
+            my_hits += convect_walls(st, W, s, x, vx, vy, vz, dt, cap, surf ? &acc : nullptr, r.w);
             S.A.wv[slot] = PV{r.w, vx, vy, vz};
         }
         S.A.pos[slot].x = x;
@@ -45,12 +46,13 @@ __global__ void __launch_bounds__(256) k_convect(DomainView d, int s, int64_t hw
     }
     if (cap) set_status(d, ST_WALL_HITS);
     if (my_hits) atomicAdd(&d.counters->wall_hits, my_hits);
+    if (surf) surf_flush(acc, surf, my_hits != 0);
 }
 
 }  // namespace
 
 void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w, double dt, uint64_t step,
-                    int32_t flags)
+                    int32_t flags, double* surf)
 {
     mz_ctx* c = d->ctx;
     SpeciesHost& S = d->sp[s];
@@ -70,5 +72,5 @@ void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w
     DomainView v = make_view(d);
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.hw, 256), (int64_t)c->num_sms * 8));
     MZ_LAUNCH(c, "convect", k_convect, blocks, 256, 0, v, s, S.hw, W, dt, (uint32_t)step,
-              (flags & MZ_CONVECT_COMPUTE_CELL) ? 1 : 0);
+              (flags & MZ_CONVECT_COMPUTE_CELL) ? 1 : 0, surf);
 }

@@ -99,6 +99,10 @@ struct mz_domain_s {
     size_t merge_scratch_bytes = 0;
     // property sets created on this domain (freed with it)
     std::vector<mz_props*> props;
+    std::vector<mz_surf_props*> surf;
+    // surface sampling of the fused 1-D step (mz_step_set_surface)
+    mz_surf_props* step_surf = nullptr;
+    mz_surf_props* step_surf_avg = nullptr;
     // fused step: RNG step index and last-block counter
     uint32_t* d_step = nullptr;
     unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block}
@@ -107,6 +111,14 @@ struct mz_domain_s {
     // fused-step mapping chosen by mz_step_autotune (0: the default rules)
     int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
     int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
+};
+
+// SurfProps of a domain's 1-D walls (surface_props.jl:22-67): device sums
+// [species][element][11] in the order np, flux_incident, flux_reflected,
+// force xyz, normal_pressure, shear_pressure xyz, kinetic_energy_flux
+struct mz_surf_props_s {
+    mz_domain* dom = nullptr;
+    double* acc = nullptr;  // n_species * 2 * 11
 };
 
 struct mz_props_s {
@@ -161,8 +173,9 @@ void launch_scan_cells(mz_domain* d, int32_t* counts, mz::Indexer* ind, int32_t*
 void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce, uint64_t step, int32_t flags,
                 double dw_tol);
 void launch_props(mz_domain* d, mz_props* p, int32_t mode);
+// surf: this species' 2 x 11 surface sums, or nullptr
 void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w, double dt, uint64_t step,
-                    int32_t flags);
+                    int32_t flags, double* surf = nullptr);
 void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const int32_t* counts_dev,
                          const double* T3, const double* T3_all, const double* Fnum, double span, const double* box6,
                          int32_t distribution, uint64_t step);

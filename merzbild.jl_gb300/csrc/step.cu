@@ -53,6 +53,9 @@ struct StepArgs {
     unsigned int* hit_done;  // last-block counter of k_wall_hits
     unsigned int hitq_cap;
     int32_t big_cell;     // cells with at least this many particles collide in k_ntc_big
+    double* surf;         // wall sums of this step [species][2][11], or nullptr
+    double* surf_avg;     // their average, or nullptr
+    double surf_factor[MZ_MAX_SPECIES];  // mass / dt per species (surface_props_scale!)
 };
 
 // cells of the per-warp destination histogram of k_cell (48 KB per block)
@@ -239,7 +242,13 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                             rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
                             const PV r = Q.wv[qq];
                             double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
-                            hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
+                            SurfAcc one = {};
+                            hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap, a.surf ? &one : nullptr, r.w);
+                            if (a.surf)
+                                for (int e = 0; e < 2; ++e)
+                                    for (int k = 0; k < SURF_Q; ++k)
+                                        if (one.q[e][k] != 0.0)
+                                            atomicAdd(&a.surf[((size_t)s * 2 + e) * SURF_Q + k], one.q[e][k]);
                             Q.wv[qq] = PV{r.w, vx, vy, vz};
                             Q.pos[qq].x = x;
                             key = cell_of(d, x, a.W.inv_dx);
@@ -363,6 +372,8 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
     const unsigned n = min(*a.hit_n, a.hitq_cap);
     unsigned long long hits = 0;
     bool cap = false;
+    SurfAcc acc[MZ_MAX_SPECIES > 1 ? 1 : 1] = {};
+    int acc_s = -1;  // species of this thread's sums (flushed when it changes)
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int4 h = a.hitq[i];
         const int64_t qq = h.x;
@@ -373,7 +384,19 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
         rs.init(cell_seed(d, c), TAG_CONVECT, (uint32_t)s, cell_step(d, c, step), cell_rid(d, c), (uint32_t)j);
         const PV r = Q.wv[qq];
         double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
-        hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap);
+        SurfAcc* sa = nullptr;
+        if (a.surf) {
+            if (acc_s >= 0 && acc_s != s) {
+                // another species: add this thread's sums directly
+                for (int e = 0; e < 2; ++e)
+                    for (int k = 0; k < SURF_Q; ++k)
+                        if (acc[0].q[e][k] != 0.0) atomicAdd(&a.surf[((size_t)acc_s * 2 + e) * SURF_Q + k], acc[0].q[e][k]);
+                acc[0] = SurfAcc{};
+            }
+            acc_s = s;
+            sa = &acc[0];
+        }
+        hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap, sa, r.w);
         Q.wv[qq] = PV{r.w, vx, vy, vz};
         Q.pos[qq].x = x;
         const int32_t key = cell_of(d, x, a.W.inv_dx);
@@ -381,6 +404,11 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
         atomicAdd(&S.counts[key], 1);
     }
     if (cap) set_status(d, ST_WALL_HITS);
+    if (a.surf) {
+        // block sums per species of the last sums each thread holds
+        for (int s = 0; s < d.n_species; ++s)
+            surf_flush(acc_s == s ? acc[0] : SurfAcc{}, a.surf + (size_t)s * 2 * SURF_Q, acc_s == s);
+    }
     hits = __reduce_add_sync(0xFFFFFFFFu, (unsigned)hits);
     if ((threadIdx.x & 31) == 0 && hits) atomicAdd(&d.counters->wall_hits, hits);
     // the last block empties the queue for the next step
@@ -403,6 +431,21 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
 // with one global atomic (consecutive addresses).  Other slots take a ticket
 // directly.  The order inside a segment is arbitrary; k_cell sorts it.
 constexpr int SCATTER_TILE = 2048, SCATTER_WINDOW = 2048;
+
+// surface_props_scale! of the step's wall sums, then avg_props! into the
+// average from avg_start on (the convection of RNG step `step`)
+__global__ void k_surf_finish(StepArgs a, int ns)
+{
+    const uint32_t step = *a.step_ptr - 1;  // k_cell advanced it
+    const bool averaging = a.surf_avg && (int64_t)step - (int64_t)a.step0 >= a.avg_start;
+    for (int i = threadIdx.x; i < ns * 2 * SURF_Q; i += blockDim.x) {
+        const int s = i / (2 * SURF_Q);
+        double v = a.surf[i];
+        if (i % SURF_Q != 0) v *= a.surf_factor[s];
+        a.surf[i] = v;
+        if (averaging) a.surf_avg[i] = fma(v, a.inv_navg, a.surf_avg[i]);
+    }
+}
 
 __global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, int64_t n)
 {
@@ -481,6 +524,11 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     }
     a.dt = plan->dt;
     a.dims = plan->dims;
+    if (plan->dims == 1 && d->step_surf) {
+        a.surf = d->step_surf->acc;
+        a.surf_avg = d->step_surf_avg ? d->step_surf_avg->acc : nullptr;
+        for (int s = 0; s < d->ns; ++s) a.surf_factor[s] = d->mass[s] / plan->dt;
+    }
     // block-per-cell collisions for large 0-D cells (the 1-D step keeps every
     // cell's phases in one warp)
     {
@@ -534,8 +582,11 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
         if ((physics || props) && b.big_cell < INT_MAX)
             MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
+        if (physics && b.surf)
+            MZ_CK(cudaMemsetAsync(b.surf, 0, (size_t)d->ns * 2 * SURF_Q * sizeof(double), c->stream));
         MZ_LAUNCH(c, name, kern, blocks, 256, CELL_SMEM, v, b);
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
+        if (physics && b.surf) MZ_LAUNCH(c, "step_surf", k_surf_finish, 1, 128, 0, b, d->ns);
     };
     // one sort of every species from the keys k_cell wrote, gather in k_cell
     auto sort_launch = [&](int props, int physics) {

@@ -117,6 +117,13 @@ _SIGS = {
     "mz_step": (i32, [vp, P(StepPlan), i64, vp, vp]),
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
     "mz_step_autotune": (i32, [vp, P(StepPlan), i64, P(i32), P(i32)]),
+    "mz_surf_props_create": (i32, [vp, P(vp)]),
+    "mz_surf_props_destroy": (i32, [vp]),
+    "mz_surf_props_clear": (i32, [vp]),
+    "mz_surf_avg_props": (i32, [vp, vp, d]),
+    "mz_surf_props_download": (i32, [vp, P(d), P(d), P(d), P(d), P(d), P(d), P(d)]),
+    "mz_convect_1d_surf": (i32, [vp, i32, P(Grid1D), P(Walls1D), d, u64, i32, vp]),
+    "mz_step_set_surface": (i32, [vp, vp, vp]),
     "mz_sort_keys_noalloc": (i32, [vp, vp, i64, i32, vp, vp]),
     "mz_sincos_2pi": (i32, [vp, i64, P(u64), P(d), P(d)]),
     "mz_server_create": (i32, [vp, i32, P(d), P(Interaction), d, i64, P(i64), P(vp)]),

@@ -457,6 +457,11 @@ class Domain:
         self._ck(lib().mz_step(self.h, C.byref(plan), int(n_steps), inst.h if inst else None,
                                avg.h if avg else None))
 
+    def set_step_surface(self, inst=None, avg=None):
+        """mz_step_set_surface: fused 1-D steps sample the walls into inst (and
+        average into avg from plan.avg_start on)."""
+        self._ck(lib().mz_step_set_surface(self.h, inst.h if inst else None, avg.h if avg else None))
+
     def autotune(self, plan, trial_steps=2):
         """mz_step_autotune: time each fused-step mapping on real steps (the
         state advances) and keep the fastest; returns (lanes, big_cell)."""
@@ -510,6 +515,48 @@ class PhysProps:
         # column-major (Julia) -> numpy [..., cell, species] views
         return dict(lpa=lpa, np=np_.reshape(ns, nc).T, n=n.reshape(ns, nc).T, v=v.reshape(ns, nc, 3).transpose(2, 1, 0),
                     T=T.reshape(ns, nc).T, moments=mom[: nm * nc * ns].reshape(ns, nc, nm).transpose(2, 1, 0))
+
+
+class SurfProps:
+    """SurfProps(pia, grid) of a 1-D domain (surface_props.jl:22-67): element
+    0 = left wall (normal +x), element 1 = right wall (normal -x), unit areas.
+    fetch() returns the reference's arrays (elements x species; force and
+    shear_pressure 3 x elements x species)."""
+
+    def __init__(self, domain: Domain):
+        self.domain = domain
+        self.h = C.c_void_p()
+        domain._ck(lib().mz_surf_props_create(domain.h, C.byref(self.h)))
+        domain._children.add(self)
+
+    def close(self):
+        if self.h:
+            if self.domain.h:
+                lib().mz_surf_props_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fetch(self):
+        ns = self.domain.n_species
+        a = {k: np.zeros(m * 2 * ns) for k, m in (("np", 1), ("flux_incident", 1), ("flux_reflected", 1), ("force", 3),
+                                                   ("normal_pressure", 1), ("shear_pressure", 3),
+                                                   ("kinetic_energy_flux", 1))}
+        self.domain._ck(lib().mz_surf_props_download(self.h, ptr(a["np"]), ptr(a["flux_incident"]),
+                                                     ptr(a["flux_reflected"]), ptr(a["force"]),
+                                                     ptr(a["normal_pressure"]), ptr(a["shear_pressure"]),
+                                                     ptr(a["kinetic_energy_flux"])))
+        out = {}
+        for k, v in a.items():
+            if k in ("force", "shear_pressure"):
+                out[k] = v.reshape(ns, 2, 3).transpose(2, 1, 0)
+            else:
+                out[k] = v.reshape(ns, 2).T
+        return out
 
 
 # --------------------------------------------------------------------- serving
@@ -633,8 +680,14 @@ def ntc_equal_weight(rng, domain, cell, species, dt, species2=None):
     domain.ntc(species, s2, dt, rng.step, cells=cells, equal_weight=True)
 
 
-def convect_particles(rng, grid, boundaries, domain, species, dt):
-    """convect_particles! (convection_1D.jl:130-157)."""
+def convect_particles(rng, grid, boundaries, domain, species, dt, surf_props=None):
+    """convect_particles! (convection_1D.jl:130-157); with surf_props, the
+    surface-sampling form (convection_1D.jl:176-206)."""
+    if surf_props is not None:
+        g, w = grid.c_struct(), boundaries.c_struct()
+        domain._ck(lib().mz_convect_1d_surf(domain.h, species, C.byref(g), C.byref(w), float(dt), int(rng.step), 0,
+                                            surf_props.h))
+        return
     domain.convect(species, grid, boundaries, dt, rng.step, compute_cell=False)
 
 
@@ -672,6 +725,16 @@ def compute_props_sorted(domain, phys_props):
 def avg_props(phys_props_avg, phys_props, n_avg_timesteps):
     """avg_props! (physical_props.jl:281-299)."""
     phys_props.domain._ck(lib().mz_avg_props(phys_props_avg.h, phys_props.h, float(n_avg_timesteps)))
+
+
+def clear_surf_props(surf_props):
+    """clear_props!(surf_props::SurfProps) (surface_props.jl:176-196)."""
+    surf_props.domain._ck(lib().mz_surf_props_clear(surf_props.h))
+
+
+def avg_surf_props(surf_props_avg, surf_props, n_avg_timesteps):
+    """avg_props!(surf_props_avg::SurfProps, surf_props, n) (surface_props.jl:205-226)."""
+    surf_props.domain._ck(lib().mz_surf_avg_props(surf_props_avg.h, surf_props.h, float(n_avg_timesteps)))
 
 
 def clear_props(phys_props):

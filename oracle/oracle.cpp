@@ -657,8 +657,51 @@ Grid1D make_grid(double L, int64_t nx, double wall_offset)
 inline int64_t get_cell(const Grid1D& g, double x) { return (int64_t)std::floor(x * g.inv_dx) + 1; }  // :97-99
 
 // ------------------------------------------------------------- convection_1D.jl
-void convect_single_particle(orc_stream* rng, const Grid1D& g, const Walls& W, Particle& p, int s, double dt)
-{   // convection_1D.jl:17-54
+// SurfProps of a 1-D grid for one species (surface_props.jl:22-67):
+// element 0 = left wall (normal +x), element 1 = right wall (normal -x), unit
+// areas; per element np, flux_incident, flux_reflected, force[3],
+// normal_pressure, shear_pressure[3], kinetic_energy_flux.
+enum { SQ_NP, SQ_FIN, SQ_FREF, SQ_FX, SQ_FY, SQ_FZ, SQ_PN, SQ_SX, SQ_SY, SQ_SZ, SQ_KE, SQ_N };
+struct Surf {
+    double q[2][SQ_N] = {{0}};
+};
+
+inline double surf_normal_x(int e) { return e == 0 ? 1.0 : -1.0; }
+
+// update_surface_incident! (surface_props.jl:78-101), sign +1, and
+// update_surface_reflected! (:113-134), sign -1
+void surf_update(double* q, int e, double w, const double* v, bool reflected)
+{
+    const double n[3] = {surf_normal_x(e), 0.0, 0.0};
+    const double px = w * v[0], py = w * v[1], pz = w * v[2];
+    const double pn = px * n[0] + py * n[1] + pz * n[2];
+    const double sg = reflected ? -1.0 : 1.0;
+    if (!reflected) {
+        q[SQ_NP] += 1.0;
+        q[SQ_FIN] += w;
+    } else {
+        q[SQ_FREF] -= w;
+    }
+    q[SQ_FX] += sg * px;
+    q[SQ_FY] += sg * py;
+    q[SQ_FZ] += sg * pz;
+    q[SQ_PN] -= sg * pn;
+    q[SQ_SX] += sg * (px - pn * n[0]);
+    q[SQ_SY] += sg * (py - pn * n[1]);
+    q[SQ_SZ] += sg * (pz - pn * n[2]);
+    q[SQ_KE] += sg * (0.5 * (px * v[0] + py * v[1] + pz * v[2]));
+}
+
+// surface_props_scale! (surface_props.jl:149-166): all but np times mass / dt / area
+void surf_scale(double* q, double mass, double dt, double inv_area)
+{
+    const double f = mass / dt * inv_area;
+    for (int k = SQ_FIN; k < SQ_N; ++k) q[k] *= f;
+}
+
+void convect_single_particle(orc_stream* rng, const Grid1D& g, const Walls& W, Particle& p, int s, double dt,
+                             Surf* surf = nullptr)
+{   // convection_1D.jl:17-54 (with surf: :72-112)
     double t_rest = dt;
     double x_old = p.x[0];
     double x_new = std::fma(p.v[0], dt, p.x[0]);
@@ -678,7 +721,9 @@ void convect_single_particle(orc_stream* rng, const Grid1D& g, const Walls& W, P
             normal = 1.0;
             x_old = 0.0;
         }
+        if (surf) surf_update(surf->q[bc], bc, p.w, p.v, false);
         reflect_particle_x(rng, p, W.vsq[bc + 2 * s], normal, W.v[bc], W.acc[bc]);
+        if (surf) surf_update(surf->q[bc], bc, p.w, p.v, true);
         x_new = std::fma(p.v[0], t_rest, x_old);
     }
     x_new = std::min(std::max(x_new, g.min_x), g.max_x);  // clamp
@@ -686,13 +731,16 @@ void convect_single_particle(orc_stream* rng, const Grid1D& g, const Walls& W, P
 }
 
 // convect_particles! (convection_1D.jl:130-157) and
-// convect_particles_and_compute_cell! (convection_1D.jl:225-255).  Each
-// particle's stream is keyed on (cell, position j in the cell's logical list).
+// convect_particles_and_compute_cell! (convection_1D.jl:225-255); with surf,
+// convect_particles!(..., surf_props, dt) (:176-206), sequential so the
+// surface sums keep the reference's order.  Each particle's stream is keyed
+// on (cell, position j in the cell's logical list).
 void convect_particles(Orc& o, int s, const Grid1D& g, const Walls& W, double dt, uint64_t seed, uint64_t step,
-                       bool compute_cell, int nthreads)
+                       bool compute_cell, int nthreads, Surf* surf = nullptr)
 {
     ParticleVector& pv = o.pv[s];
     const int64_t nc = o.n_cells;
+    if (surf) nthreads = 1;
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64) if (nthreads > 1)
     for (int64_t cell = 1; cell <= nc; ++cell) {
         ParticleIndexer p = o.pi(cell, s);
@@ -700,13 +748,15 @@ void convect_particles(Orc& o, int s, const Grid1D& g, const Walls& W, double dt
         auto one = [&](int64_t i) {
             orc_stream rng = orc_stream_make(seed, ORC_TAG_CONVECT, (uint32_t)s, step, (uint32_t)(cell - 1), (uint32_t)j);
             ++j;
-            convect_single_particle(&rng, g, W, pv.at(i), s, dt);
+            convect_single_particle(&rng, g, W, pv.at(i), s, dt, surf);
             if (compute_cell) pv.cell[i - 1] = get_cell(g, pv.at(i).x[0]);
         };
         for (int64_t i = p.start1; i <= p.end1; ++i) one(i);
         if (p.n_group2 > 0)
             for (int64_t i = p.start2; i <= p.end2; ++i) one(i);
     }
+    if (surf)
+        for (int e = 0; e < 2; ++e) surf_scale(surf->q[e], o.mass[s], dt, 1.0);
 }
 
 // --------------------------------------------------------------- grid_sorting.jl
@@ -1413,11 +1463,10 @@ void orc_avg_props(int64_t count, double* avg, const double* inst, double n_avg_
 }
 
 // walls: [T_l, T_r, vl0, vl1, vl2, vr0, vr1, vr2, acc_l, acc_r]
-void orc_convect(void* h, int32_t s, double L, int64_t nx, double wall_offset, const double* walls, double dt,
-                 uint64_t seed, uint64_t step, int32_t compute_cell, int32_t nthreads)
+// MaxwellWalls1D (boundary_conditions.jl:29-53) from the flat array
+// {T_l, T_r, v_l[3], v_r[3], acc_l, acc_r}
+static Walls make_walls(const Orc& o, const double* walls)
 {
-    Orc* o = (Orc*)h;
-    Grid1D g = make_grid(L, nx, wall_offset);
     Walls W;
     W.T[0] = walls[0];
     W.T[1] = walls[1];
@@ -1427,12 +1476,46 @@ void orc_convect(void* h, int32_t s, double L, int64_t nx, double wall_offset, c
     }
     W.acc[0] = walls[8];
     W.acc[1] = walls[9];
-    W.vsq.resize(2 * o->n_species);
-    for (int sp = 0; sp < o->n_species; ++sp) {
-        W.vsq[0 + 2 * sp] = 2.0 * k_B * W.T[0] / o->mass[sp];
-        W.vsq[1 + 2 * sp] = 2.0 * k_B * W.T[1] / o->mass[sp];
+    W.vsq.resize(2 * o.n_species);
+    for (int sp = 0; sp < o.n_species; ++sp) {
+        W.vsq[0 + 2 * sp] = 2.0 * k_B * W.T[0] / o.mass[sp];
+        W.vsq[1 + 2 * sp] = 2.0 * k_B * W.T[1] / o.mass[sp];
     }
+    return W;
+}
+
+void orc_convect(void* h, int32_t s, double L, int64_t nx, double wall_offset, const double* walls, double dt,
+                 uint64_t seed, uint64_t step, int32_t compute_cell, int32_t nthreads)
+{
+    Orc* o = (Orc*)h;
+    Grid1D g = make_grid(L, nx, wall_offset);
+    Walls W = make_walls(*o, walls);
     convect_particles(*o, s, g, W, dt, seed, step, compute_cell != 0, nthreads);
+}
+
+// convect_particles! with SurfProps: out[2][11] = the scaled surface sums of
+// this call (surface_props.jl layout per element, see SQ_*)
+void orc_convect_surf(void* h, int32_t s, double L, int64_t nx, double wall_offset, const double* walls, double dt,
+                      uint64_t seed, uint64_t step, double* out)
+{
+    Orc* o = (Orc*)h;
+    Grid1D g = make_grid(L, nx, wall_offset);
+    Walls W = make_walls(*o, walls);
+    Surf surf;
+    convect_particles(*o, s, g, W, dt, seed, step, false, 1, &surf);
+    for (int e = 0; e < 2; ++e)
+        for (int k = 0; k < SQ_N; ++k) out[e * SQ_N + k] = surf.q[e][k];
+}
+
+// one incident (reflected = 0) or reflected update of element e of q[2][11]
+void orc_surf_update(double* q, int32_t e, double w, const double* v, int32_t reflected)
+{
+    surf_update(q + e * SQ_N, e, w, v, reflected != 0);
+}
+
+void orc_surf_scale(double* q, double mass, double dt, const double* inv_areas)
+{
+    for (int e = 0; e < 2; ++e) surf_scale(q + e * SQ_N, mass, dt, inv_areas[e]);
 }
 
 void orc_grid(double L, int64_t nx, double wall_offset, double* out5)

@@ -70,6 +70,9 @@ def lib():
             "orc_compute_props": (None, [vp, i32, P(i32), i32, d, P(d), P(d), P(d), P(d), P(d), P(d), P(d), i32]),
             "orc_avg_props": (None, [i64, P(d), P(d), d]),
             "orc_convect": (None, [vp, i32, d, i64, d, P(d), d, u64, u64, i32, i32]),
+            "orc_convect_surf": (None, [vp, i32, d, i64, d, P(d), d, u64, u64, P(d)]),
+            "orc_surf_update": (None, [P(d), i32, d, P(d), i32]),
+            "orc_surf_scale": (None, [P(d), d, d, P(d)]),
             "orc_grid": (None, [d, i64, d, P(d)]),
             "orc_sort": (None, [vp, i32, d, i64, d]),
             "orc_squash": (None, [vp, i32]),
@@ -108,6 +111,19 @@ def lib():
 
 def _p(a, ctype=C.c_double):
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def surf_update(q, element, w, v, reflected):
+    """update_surface_incident! / update_surface_reflected! (surface_props.jl:78-134)
+    on q (2 x 11, see Oracle.convect_surf)."""
+    v = np.ascontiguousarray(v, float)
+    lib().orc_surf_update(_p(q), element, w, _p(v), 1 if reflected else 0)
+
+
+def surf_scale(q, mass, dt, inv_areas):
+    """surface_props_scale! (surface_props.jl:149-166) on q (2 x 11)."""
+    ia = np.ascontiguousarray(inv_areas, float)
+    lib().orc_surf_scale(_p(q), mass, dt, _p(ia))
 
 
 def stream_draws(seed, tag, sub, step, a, b, n):
@@ -311,6 +327,16 @@ class Oracle:
 
     def delete_particle_end(self, s, cell):
         self.L.orc_delete_particle_end(self.h, s, cell)
+
+    def convect_surf(self, s, L, nx, walls, dt, seed, step, wall_offset=1e-12):
+        """convect_particles! with SurfProps (convection_1D.jl:176-206): returns
+        the scaled surface sums of this call as (2 elements, 11 quantities):
+        np, flux_incident, flux_reflected, force xyz, normal_pressure, shear
+        xyz, kinetic_energy_flux."""
+        w = np.ascontiguousarray(walls, float)
+        out = np.zeros(22)
+        self.L.orc_convect_surf(self.h, s, L, nx, wall_offset, _p(w), dt, seed, step, _p(out))
+        return out.reshape(2, 11)
 
     def merge_octree(self, octree, s, cell, target, L=None, nx=0, seed=0, step=0, wall_offset=1e-12):
         self.L.orc_merge_octree(self.h, octree.h, s, cell, target, -1.0 if L is None else float(L), nx, wall_offset,

@@ -471,3 +471,41 @@ def test_collisions_1d_conservation(orc, golden):
     # the bounds here are FP64 round-off bounds with 2-3x headroom.
     assert abs(pr["T"][0, 1] - pr0["T"][0, 1]) < 4e-15 * T
     assert np.max(np.abs(pr["v"][0, 1] - pr0["v"][0, 1])) < 1e-13
+
+
+def test_surface_props_known_answers(orc):
+    """test/test_surface_props_1D_uniform.jl:74-178: incident and reflected
+    updates of the two wall elements, then surface_props_scale! with areas 2
+    and 4 and dt 1e-20 (values transcribed from the test's expressions)."""
+    EPS2 = 2 * np.finfo(float).eps
+    q = np.zeros((2, 11))
+    orc.surf_update(q, 0, 3.5, [-9.0, 9.0, 0.0], False)
+    orc.surf_update(q, 1, 10.5, [10.0, 0.0, 3.0], False)
+    NP, FIN, FREF, FX, FY, FZ, PN, SX, SY, SZ, KE = range(11)
+    assert q[:, NP].tolist() == [1.0, 1.0] and q[:, FIN].tolist() == [3.5, 10.5] and q[:, FREF].tolist() == [0, 0]
+    assert abs(q[0, FX] - 3.5 * -9) < EPS2 and abs(q[1, FX] - 10.5 * 10) < EPS2
+    assert abs(q[0, FY] - 3.5 * 9) < EPS2 and q[1, FY] == 0.0 and q[0, FZ] == 0.0
+    assert abs(q[1, FZ] - 10.5 * 3) < EPS2
+    assert abs(q[0, PN] - 9 * 3.5) < EPS2 and abs(q[1, PN] - 10 * 10.5) < EPS2
+    assert abs(q[0, SY] - 9 * 3.5) < EPS2 and abs(q[1, SZ] - 3 * 10.5) < EPS2 and q[0, SX] == 0.0
+    assert abs(q[0, KE] - 0.5 * 3.5 * (81 + 81)) < EPS2 and abs(q[1, KE] - 0.5 * 10.5 * (100 + 9)) < EPS2
+    # reflections: left specular (-9, 9, 0) -> (9, 9, 0); right re-emitted at
+    # (-1, -2, -4) with weight 10
+    orc.surf_update(q, 0, 3.5, [9.0, 9.0, 0.0], True)
+    orc.surf_update(q, 1, 10.0, [-1.0, -2.0, -4.0], True)
+    assert q[:, FREF].tolist() == [-3.5, -10.0]
+    assert abs(q[0, FX] - (3.5 * -9 - 3.5 * 9)) < EPS2 and abs(q[1, FX] - (10.5 * 10 - 10.0 * -1)) < EPS2
+    assert abs(q[0, FY]) < EPS2 and abs(q[1, FY] - (-10.0 * -2)) < EPS2
+    assert abs(q[1, FZ] - (10.5 * 3 - 10.0 * -4)) < EPS2
+    assert abs(q[0, PN] - (9 * 3.5 + 9 * 3.5)) < EPS2 and abs(q[1, PN] - (10 * 10.5 + 1 * 10.0)) < EPS2
+    assert abs(q[0, SY] - (9 * 3.5 - 9 * 3.5)) < EPS2 and abs(q[1, SY] - (0 * 10.5 - -2 * 10.0)) < EPS2
+    assert abs(q[1, SZ] - (3 * 10.5 - -4 * 10.0)) < EPS2
+    assert abs(q[0, KE]) < EPS2
+    assert abs(q[1, KE] - (0.5 * 10.5 * 109 - 0.5 * 10.0 * 21)) < EPS2
+    kept = q.copy()
+    mass, dt = 6.633e-26, 1e-20
+    orc.surf_scale(q, mass, dt, [0.5, 0.25])
+    f = mass * np.array([0.5, 0.25]) / dt
+    assert q[:, NP].tolist() == [1.0, 1.0]
+    for k in range(1, 11):
+        assert np.all(np.abs(q[:, k] - f * kept[:, k]) <= EPS2 * np.maximum(1.0, np.abs(f * kept[:, k])))
