@@ -230,8 +230,8 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
         return p
 
     lanes, big = dom.autotune(plan(0), trial_steps=1)
-    dom.step(plan(12), warmup, inst)
-    warmup += 12
+    dom.step(plan(24), warmup, inst)
+    warmup += 24
     dom.counters(reset=True)
     ctx.synchronize()
     ctx.timer_start()
@@ -387,7 +387,7 @@ def run_gpu(args):
     K, W = args.steps, args.warmup
     # the autotuner times each mapping on real steps (3 steps before the
     # warm-up), then W untimed warm-up steps
-    tune_steps = 3 * 4
+    tune_steps = 6 * 4
     mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=4)
     dom.step(make_plan(mz, grid, walls, dt, tune_steps, K), W, inst, avg)
     ctx.synchronize()

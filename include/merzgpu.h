@@ -340,11 +340,11 @@ int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_step
 /* Choose the fused step's mapping by timing it: every combination of lanes
  * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the
  * block-per-cell threshold (512, 2,048, 8,192 particles, never) runs
- * trial_steps real steps of `plan` (starting at plan->step0; the state
- * advances by 12 * trial_steps steps for 0-D plans, 3 * trial_steps for 1-D,
- * and every mapping gives the same results); the fastest is kept for later
- * mz_step calls whose plan leaves big_cell at 0.  No counterpart in the
- * reference. */
+ * trial_steps real steps of `plan` twice, in interleaved rounds (starting at
+ * plan->step0; the state advances by 24 * trial_steps steps for 0-D plans,
+ * 6 * trial_steps for 1-D, and every mapping gives the same results); the
+ * fastest is kept for later mz_step calls whose plan leaves big_cell at 0.
+ * No counterpart in the reference. */
 int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
 
 /* ---------------------------------------------------------------- counters */

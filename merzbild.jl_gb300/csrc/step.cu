@@ -654,18 +654,19 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     const int32_t lanes_c[3] = {8, 16, 32};
     const int32_t big_c[4] = {512, 2048, 8192, -1};
     const int nb = plan->dims == 0 ? 4 : 1;
+    const int nconf = 3 * nb;
     mz_step_plan p = *plan;
     p.big_cell = 0;
-    float best = 3.0e38f;
-    int32_t bl = 0, bb = 0;
+    std::vector<float> best(nconf, 3.0e38f);
     uint64_t step = plan->step0;
     cudaEvent_t e0, e1;
     MZ_CK(cudaEventCreate(&e0));
     MZ_CK(cudaEventCreate(&e1));
-    for (int li = 0; li < 3; ++li)
-        for (int bi = 0; bi < nb; ++bi) {
-            d->tuned_lanes = lanes_c[li];
-            d->tuned_big = plan->dims == 0 ? big_c[bi] : -1;
+    // two interleaved rounds; a configuration's time is its faster round
+    for (int round = 0; round < 2; ++round)
+        for (int k = 0; k < nconf; ++k) {
+            d->tuned_lanes = lanes_c[k / nb];
+            d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
             p.step0 = step;
             MZ_CK(cudaEventRecord(e0, c->stream));
             launch_step(d, &p, trial_steps, nullptr, nullptr);
@@ -674,16 +675,13 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
             float ms = 0.0f;
             MZ_CK(cudaEventElapsedTime(&ms, e0, e1));
             step += (uint64_t)trial_steps;
-            if (ms < best) {
-                best = ms;
-                bl = d->tuned_lanes;
-                bb = d->tuned_big;
-            }
+            best[k] = std::min(best[k], ms);
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    d->tuned_lanes = bl;
-    d->tuned_big = bb;
-    if (lanes_out) *lanes_out = bl;
-    if (big_out) *big_out = bb;
+    const int kb = (int)(std::min_element(best.begin(), best.end()) - best.begin());
+    d->tuned_lanes = lanes_c[kb / nb];
+    d->tuned_big = plan->dims == 0 ? big_c[kb % nb] : -1;
+    if (lanes_out) *lanes_out = d->tuned_lanes;
+    if (big_out) *big_out = d->tuned_big;
 }

@@ -237,9 +237,9 @@ def test_autotuned_mapping_changes_no_result(ctx, orc):
         if tune:
             lanes, big = dom.autotune(plan, trial_steps=1)
             assert lanes in (8, 16, 32) and big in (512, 2048, 8192, -1)
-            done = 12
+            done = 24
         plan.step0 = done
-        dom.step(plan, 15 - done)
+        dom.step(plan, 27 - done)
         runs.append(device_logical(dom, 0))
         dom.close()
     assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][0], runs[1][0])
@@ -251,8 +251,8 @@ def test_autotuned_mapping_changes_no_result(ctx, orc):
         done = 0
         if tune:
             dom.autotune(plan, trial_steps=1)
-            done = 3
-        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 5 - done)
+            done = 6
+        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 8 - done)
         states.append(device_logical(dom, 0))
         dom.close()
     assert np.array_equal(states[0][1], states[1][1]) and np.array_equal(states[0][0], states[1][0])
