@@ -240,6 +240,69 @@ int mz_convect_1d_surf(mz_domain* dom, int32_t species, const mz_grid1d* grid, c
  * No counterpart in the reference (its time loops call the functions above). */
 int mz_step_set_surface(mz_domain* dom, mz_surf_props* inst, mz_surf_props* avg);
 
+/* ---------------------------------------------------------------- netCDF output */
+/* Output files of cell properties (NCDataHolder, io.jl:116-243) and surface
+ * properties (NCDataHolderSurf, io.jl:430-547): the reference's dimensions,
+ * variables (names, Float64 / Int32 types, dimension order) and skip lists, in
+ * the netCDF classic 64-bit-offset container (the reference writes netCDF-4,
+ * which needs HDF5).  species_names is a char variable (n_species,
+ * species_name_length); a cell-property file without moments has no
+ * n_moments dimension and no moment variables (classic netCDF has no
+ * fixed dimension of length 0).
+ * Writes from device sets (mz_nc_props_write, mz_nc_surf_write) are enqueued
+ * on the context's stream after the work already there: the record is packed
+ * on the device, copied to pinned memory on a side stream and written to the
+ * file by the file's writer thread, so the caller does not wait for the disk.
+ * The *_host forms take the reference's host arrays (column-major layouts of
+ * mz_props_download / mz_surf_props_download).  ctx may be NULL for a file
+ * written only from host arrays.  Handles are not thread-safe. */
+typedef struct mz_nc_file_s mz_nc_file;
+enum { MZ_NC_ATTR_TEXT = 0, MZ_NC_ATTR_INT = 1, MZ_NC_ATTR_DOUBLE = 2 };
+/* one global attribute (NCDataHolder's global_attributes): count chars,
+ * int32 values or doubles at `values` */
+typedef struct {
+    const char* name;
+    int32_t type;
+    int32_t count;
+    const void* values;
+} mz_nc_attribute;
+/* NCDataHolder(nc_filename, names_skip_list, species_data, phys_props;
+ * global_attributes) (io.jl:143-224); skip names as IOSkipList (io.jl:19-80):
+ * length_particle_array, moments, np / nparticles, ndens, v, T.  Adds the
+ * "COMMENT ndens" attribute.  The first n_names of the n_species entries of
+ * species_names are set (the reference's putvar of species_data's names). */
+int mz_nc_props_create(const char* path, const char* const* skip, int32_t n_skip, const char* const* species_names,
+                       int32_t n_names, int32_t n_species, int32_t n_cells, int32_t n_moments, const int32_t* moment_powers,
+                       int32_t ndens_not_Np, const mz_nc_attribute* gatts, int32_t n_gatts, mz_ctx* ctx,
+                       mz_nc_file** out);
+/* NCDataHolderSurf(nc_filename, names_skip_list, species_data, surf_props;
+ * global_attributes) (io.jl:457-527); skip names as IOSkipListSurf
+ * (io.jl:334-418): np / nparticles, fluxes, force, normal_pressure,
+ * shear_pressure, kinetic_energy_flux. */
+int mz_nc_surf_create(const char* path, const char* const* skip, int32_t n_skip, const char* const* species_names,
+                      int32_t n_names, int32_t n_species, int32_t n_elements, const mz_nc_attribute* gatts, int32_t n_gatts,
+                      mz_ctx* ctx, mz_nc_file** out);
+/* write_netcdf(ds, phys_props, timestep; sync_freq) (io.jl:274-317): one
+ * record; MZ_E_ARG if the set's ndens_not_Np differs from the file's (the
+ * reference's ErrorException); sync_freq > 0 syncs the file to disk after
+ * every sync_freq-th record. */
+int mz_nc_props_write(mz_nc_file* f, const mz_props* p, double timestep, int32_t sync_freq);
+int mz_nc_props_write_host(mz_nc_file* f, const double* lpa, const double* np, const double* ndens, const double* v,
+                           const double* T, const double* moments, int32_t ndens_not_Np, double timestep,
+                           int32_t sync_freq);
+/* write_netcdf(ds, surf_props, timestep; sync_freq) (io.jl:566-603) */
+int mz_nc_surf_write(mz_nc_file* f, const mz_surf_props* surf, double timestep, int32_t sync_freq);
+int mz_nc_surf_write_host(mz_nc_file* f, const double* np, const double* flux_incident, const double* flux_reflected,
+                          const double* force, const double* normal_pressure, const double* shear_pressure,
+                          const double* kinetic_energy_flux, double timestep, int32_t sync_freq);
+/* wait until every enqueued record is in the file; reports a failed write */
+int mz_nc_flush(mz_nc_file* f);
+/* records enqueued so far */
+int mz_nc_records(const mz_nc_file* f, int64_t* n);
+/* close_netcdf(ds) (io.jl:251-253): writes what is enqueued and closes */
+int mz_nc_close(mz_nc_file* f);
+int mz_nc_last_error(const mz_nc_file* f, char* buf, size_t len);
+
 /* ---------------------------------------------------------------- sorting */
 /* sort_particles!(gridsort, grid, ...) when grid != NULL (cells from x,
  * grid_sorting.jl:58-113), sort_particles!(gridsort, ...) with the cells

@@ -54,6 +54,10 @@ class Counters(C.Structure):
     _fields_ = [(n, C.c_ulonglong) for n in ("candidates", "accepted", "splits", "merges", "wall_hits")]
 
 
+class NcAttribute(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("type", i32), ("count", i32), ("values", vp)]
+
+
 class Request(C.Structure):
     _fields_ = [("count", i64 * MZ_MAX_SPECIES), ("T", d * MZ_MAX_SPECIES), ("Fnum", d), ("V", d), ("n_steps", i64),
                 ("seed", u64)]
@@ -133,6 +137,18 @@ _SIGS = {
     "mz_server_result": (i32, [vp, i64, P(RequestResult)]),
     "mz_server_retired": (i32, [vp, i64, P(i64), P(i64)]),
     "mz_server_info": (i32, [vp, P(i64), P(i64)]),
+    "mz_nc_props_create": (i32, [C.c_char_p, P(C.c_char_p), i32, P(C.c_char_p), i32, i32, i32, i32, P(i32), i32,
+                                 P(NcAttribute), i32, vp, P(vp)]),
+    "mz_nc_surf_create": (i32, [C.c_char_p, P(C.c_char_p), i32, P(C.c_char_p), i32, i32, i32, P(NcAttribute), i32, vp,
+                                P(vp)]),
+    "mz_nc_props_write": (i32, [vp, vp, d, i32]),
+    "mz_nc_props_write_host": (i32, [vp, P(d), P(d), P(d), P(d), P(d), P(d), i32, d, i32]),
+    "mz_nc_surf_write": (i32, [vp, vp, d, i32]),
+    "mz_nc_surf_write_host": (i32, [vp, P(d), P(d), P(d), P(d), P(d), P(d), P(d), d, i32]),
+    "mz_nc_flush": (i32, [vp]),
+    "mz_nc_records": (i32, [vp, P(i64)]),
+    "mz_nc_close": (i32, [vp]),
+    "mz_nc_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
 }
 NOALLOC_MAX_CELLS = 262144
 
