@@ -29,7 +29,8 @@ module MerzbildGPU
 export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, DeviceWalls1D, DeviceOctree,
        upload!, download, ntc!, ntc_equal_weight!, convect_particles!, convect_particles_and_compute_cell!,
        sort_particles!, squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
-       avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters
+       avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
+       DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -138,6 +139,8 @@ mutable struct DeviceProps
     dp::DeviceParticles
     ptr::Ptr{Cvoid}
     n_moments::Int
+    moment_powers::Vector{Int32}
+    ndens_not_Np::Bool
 end
 
 """
@@ -151,7 +154,7 @@ function DeviceProps(dp::DeviceParticles; moments_list=Int32[], Tref=300.0, nden
     m = Int32.(moments_list)
     check(ccall((:mz_props_create, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{Int32}, Float64, Int32, Ref{Ptr{Cvoid}}),
                 dp.ptr, length(m), m, Tref, ndens_not_Np ? 1 : 0, r), dp.ctx)
-    p = DeviceProps(dp, r[], length(m))
+    p = DeviceProps(dp, r[], length(m), m, ndens_not_Np)
     finalizer(q -> ccall((:mz_props_destroy, libmz), Cint, (Ptr{Cvoid},), q.ptr), p)
     p
 end
@@ -324,6 +327,162 @@ function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D, walls::DeviceWa
     check(ccall((:mz_step, libmz), Cint, (Ptr{Cvoid}, Ref{MzStepPlan}, Int64, Ptr{Cvoid}, Ptr{Cvoid}),
                 dp.ptr, plan, n_steps, inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr),
           dp.ctx)
+end
+
+# ------------------------------------------------------------------ surface properties
+mutable struct DeviceSurfProps
+    dp::DeviceParticles
+    ptr::Ptr{Cvoid}
+end
+
+"""
+    DeviceSurfProps(dp)
+
+Device counterpart of `SurfProps(pia, grid)` for a 1-D grid
+(surface_props.jl:22-67): element 1 = left wall, element 2 = right wall.
+"""
+function DeviceSurfProps(dp::DeviceParticles)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mz_surf_props_create, libmz), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), dp.ptr, r), dp.ctx)
+    sp = DeviceSurfProps(dp, r[])
+    finalizer(q -> ccall((:mz_surf_props_destroy, libmz), Cint, (Ptr{Cvoid},), q.ptr), sp)
+    sp
+end
+
+"""convect_particles! with surface sampling (convection_1D.jl:176-206)."""
+convect_particles!(rng::DeviceRNG, grid::DeviceGrid1D, walls::DeviceWalls1D, dp::DeviceParticles, species,
+                   surf::DeviceSurfProps, Δt) =
+    check(ccall((:mz_convect_1d_surf, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ref{DeviceWalls1D}, Float64, UInt64, Int32, Ptr{Cvoid}),
+                dp.ptr, species - 1, grid, walls, Δt, rng.step, 0, surf.ptr), dp.ctx)
+clear_props!(sp::DeviceSurfProps) =
+    check(ccall((:mz_surf_props_clear, libmz), Cint, (Ptr{Cvoid},), sp.ptr), sp.dp.ctx)
+avg_props!(avg::DeviceSurfProps, inst::DeviceSurfProps, n_avg_timesteps) =
+    check(ccall((:mz_surf_avg_props, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64), avg.ptr, inst.ptr,
+                n_avg_timesteps), avg.dp.ctx)
+
+"""Copy device surface properties into a Merzbild `SurfProps` (same layouts)."""
+function fetch!(surf_props, sp::DeviceSurfProps)
+    check(ccall((:mz_surf_props_download, libmz), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                 Ptr{Float64}), sp.ptr, surf_props.np, surf_props.flux_incident, surf_props.flux_reflected,
+                surf_props.force, surf_props.normal_pressure, surf_props.shear_pressure,
+                surf_props.kinetic_energy_flux), sp.dp.ctx)
+    surf_props
+end
+
+"""Sample the walls in every fused step (clear, sample, scale; `avg` averaged like avg_props!)."""
+set_step_surface!(dp::DeviceParticles, inst::Union{Nothing,DeviceSurfProps},
+                  avg::Union{Nothing,DeviceSurfProps}=nothing) =
+    check(ccall((:mz_step_set_surface, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}), dp.ptr,
+                inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr), dp.ctx)
+
+# ------------------------------------------------------------------ netCDF output
+struct MzNcAttribute
+    name::Cstring
+    type::Int32
+    count::Int32
+    values::Ptr{Cvoid}
+end
+
+mutable struct DeviceNCDataHolder
+    ptr::Ptr{Cvoid}
+    ctx::DeviceContext
+end
+
+function nc_check(rc, f::Ptr{Cvoid}, ctx)
+    rc == 0 && return nothing
+    if f != C_NULL
+        buf = Vector{UInt8}(undef, 1024)
+        ccall((:mz_nc_last_error, libmz), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), f, buf, length(buf))
+        throw(ErrorException(unsafe_string(pointer(buf))))
+    end
+    check(rc, ctx)
+end
+
+# global attributes as text, Int32 or Float64 arrays (the values stay referenced in `keep`)
+function nc_attributes(global_attributes, keep)
+    atts = MzNcAttribute[]
+    for (k, v) in global_attributes
+        name = Base.cconvert(Cstring, string(k)); push!(keep, name)
+        if v isa AbstractString
+            data = Vector{UInt8}(codeunits(v)); t = Int32(0)
+        elseif eltype(v) <: Integer
+            data = Int32.(collect(v)); t = Int32(1)
+        else
+            data = Float64.(collect(v)); t = Int32(2)
+        end
+        push!(keep, data)
+        push!(atts, MzNcAttribute(Base.unsafe_convert(Cstring, name), t, length(data), pointer(data)))
+    end
+    atts
+end
+
+"""
+    DeviceNCDataHolder(nc_filename, names_skip_list, species_data, p::DeviceProps; global_attributes=Dict())
+
+`NCDataHolder` (io.jl:143-224) whose records are written from device
+properties; the layout is the reference's (netCDF classic container).
+"""
+function DeviceNCDataHolder(nc_filename, names_skip_list, species_data, p::DeviceProps;
+                            global_attributes=Dict{Any,Any}())
+    keep = Any[]
+    atts = nc_attributes(global_attributes, keep)
+    powers = Int32.(p.moment_powers)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve keep begin
+        check(ccall((:mz_nc_props_create, libmz), Cint,
+                    (Cstring, Ptr{Cstring}, Int32, Ptr{Cstring}, Int32, Int32, Int32, Int32, Ptr{Int32}, Int32,
+                     Ptr{MzNcAttribute}, Int32, Ptr{Cvoid}, Ref{Ptr{Cvoid}}),
+                    nc_filename, String.(names_skip_list), length(names_skip_list), [s.name for s in species_data],
+                    length(species_data), p.dp.n_species, p.dp.n_cells, length(powers), powers,
+                    p.ndens_not_Np ? 1 : 0, atts, length(atts), p.dp.ctx.ptr, r), p.dp.ctx)
+    end
+    ds = DeviceNCDataHolder(r[], p.dp.ctx)
+    finalizer(close_netcdf, ds)
+    ds
+end
+DeviceNCDataHolder(nc_filename, species_data, p::DeviceProps; global_attributes=Dict{Any,Any}()) =
+    DeviceNCDataHolder(nc_filename, String[], species_data, p; global_attributes=global_attributes)
+
+"""`NCDataHolderSurf` (io.jl:457-527) for device surface properties."""
+function DeviceNCDataHolderSurf(nc_filename, names_skip_list, species_data, sp::DeviceSurfProps;
+                                global_attributes=Dict{Any,Any}())
+    keep = Any[]
+    atts = nc_attributes(global_attributes, keep)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve keep begin
+        check(ccall((:mz_nc_surf_create, libmz), Cint,
+                    (Cstring, Ptr{Cstring}, Int32, Ptr{Cstring}, Int32, Int32, Int32, Ptr{MzNcAttribute}, Int32,
+                     Ptr{Cvoid}, Ref{Ptr{Cvoid}}),
+                    nc_filename, String.(names_skip_list), length(names_skip_list), [s.name for s in species_data],
+                    length(species_data), sp.dp.n_species, 2, atts, length(atts), sp.dp.ctx.ptr, r), sp.dp.ctx)
+    end
+    ds = DeviceNCDataHolder(r[], sp.dp.ctx)
+    finalizer(close_netcdf, ds)
+    ds
+end
+DeviceNCDataHolderSurf(nc_filename, species_data, sp::DeviceSurfProps; global_attributes=Dict{Any,Any}()) =
+    DeviceNCDataHolderSurf(nc_filename, String[], species_data, sp; global_attributes=global_attributes)
+
+"""write_netcdf(ds, phys_props, timestep; sync_freq) (io.jl:274-317), enqueued
+behind the device work; the library's writer thread writes the record."""
+write_netcdf(ds::DeviceNCDataHolder, p::DeviceProps, timestep; sync_freq=0) =
+    nc_check(ccall((:mz_nc_props_write, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32),
+                   ds.ptr, p.ptr, timestep, sync_freq), ds.ptr, ds.ctx)
+
+"""write_netcdf(ds, surf_props, timestep; sync_freq) (io.jl:566-603)."""
+write_netcdf(ds::DeviceNCDataHolder, sp::DeviceSurfProps, timestep; sync_freq=0) =
+    nc_check(ccall((:mz_nc_surf_write, libmz), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32),
+                   ds.ptr, sp.ptr, timestep, sync_freq), ds.ptr, ds.ctx)
+
+"""close_netcdf(ds) (io.jl:251-253): writes what is enqueued, then closes."""
+function close_netcdf(ds::DeviceNCDataHolder)
+    ds.ptr == C_NULL && return nothing
+    p, ds.ptr = ds.ptr, C_NULL
+    rc = ccall((:mz_nc_close, libmz), Cint, (Ptr{Cvoid},), p)
+    rc == 0 || throw(ErrorException("netCDF file could not be completed"))
+    nothing
 end
 
 function counters(dp::DeviceParticles; reset=false)
