@@ -192,6 +192,19 @@ int mz_get_collision_factors(mz_domain* dom, int32_t s1, int32_t s2, mz_collisio
 int mz_ntc(mz_domain* dom, int32_t s1, int32_t s2, double dt, int64_t cell_begin, int64_t cell_end, uint64_t step,
            int32_t flags, double dw_tol);
 
+/* swpm!(rng, collision_factors_swpm, collision_data, interaction, particles,
+ * pia, cell, species, G, dt, V) (collision_swpm.jl:201-288) for cells
+ * [cell_begin, cell_end) of one species, G >= 0.  The pair (species,
+ * species)'s collision factors hold CollisionFactorsSWPM
+ * (collision_swpm.jl:18-24): set (sigma g)_max with mz_set_collision_factors
+ * (create_collision_factors_swpm_array: estimate_sigma_g_w_max with Fnum = 1),
+ * read sigma_g_max, n_coll and n_coll_performed back with
+ * mz_get_collision_factors (field sigma_g_w_max).  Every accepted collision
+ * appends two particles to the cell's group 2.  Draws come from the NTC
+ * streams of the pair. */
+int mz_swpm(mz_domain* dom, int32_t species, double G, double dt, int64_t cell_begin, int64_t cell_end,
+            uint64_t step);
+
 /* ---------------------------------------------------------------- properties */
 /* PhysProps(n_cells, n_species, moments_list; ndens_not_Np, Tref) (physical_props.jl:24-58) */
 int mz_props_create(mz_domain* dom, int32_t n_moments, const int32_t* moment_powers, double Tref, int32_t ndens_not_Np,

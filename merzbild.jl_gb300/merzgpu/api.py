@@ -402,6 +402,10 @@ class Domain:
         flags = L.NTC_EQUAL_WEIGHT if equal_weight else 0
         self._ck(lib().mz_ntc(self.h, s1, s2, float(dt), int(cb), int(ce), int(step), flags, float(dw_tol)))
 
+    def swpm(self, species, G, dt, step, cells=None):
+        cb, ce = (0, self.n_cells) if cells is None else cells
+        self._ck(lib().mz_swpm(self.h, species, float(G), float(dt), int(cb), int(ce), int(step)))
+
     # convection / sorting / merging ----------------------------------------
     def convect(self, species, grid, walls, dt, step, compute_cell=False):
         g = grid.c_struct()
@@ -680,6 +684,14 @@ def ntc_equal_weight(rng, domain, cell, species, dt, species2=None):
     domain.ntc(species, s2, dt, rng.step, cells=cells, equal_weight=True)
 
 
+def swpm(rng, domain, cell, species, G, dt):
+    """swpm! (collision_swpm.jl:201-288) for one cell or a (begin, end) range;
+    (sigma g)_max comes from the pair's collision factors
+    (create_collision_factors_swpm_array)."""
+    cells = cell if isinstance(cell, tuple) else (cell, cell + 1)
+    domain.swpm(species, G, dt, rng.step, cells=cells)
+
+
 def convect_particles(rng, grid, boundaries, domain, species, dt, surf_props=None):
     """convect_particles! (convection_1D.jl:130-157); with surf_props, the
     surface-sampling form (convection_1D.jl:176-206)."""
@@ -760,3 +772,11 @@ def create_collision_factors_array(domain, interactions, species_data, T_list, F
             v = estimate_sigma_g_w_max(interactions[s1][s2], species_data[s1], species_data[s2], T_list[s1],
                                        T_list[s2], F, mult_factor)
             domain.set_sigma_g_w_max(s1, s2, v)
+
+
+def create_collision_factors_swpm_array(domain, interactions, species_data, T_list, mult_factor=1.0):
+    """create_collision_factors_swpm_array(pia, interactions, species_data, T;
+    mult_factor) (collision_swpm.jl:118-149): (sigma g)_max of every pair and
+    cell from estimate_sigma_g_max! (collision_utils.jl:523-534), the NTC
+    estimate with Fnum = 1; stored in the domain's collision factors."""
+    create_collision_factors_array(domain, interactions, species_data, T_list, 1.0, mult_factor)

@@ -479,6 +479,78 @@ void ntc_two(Orc& o, int s1, int s2, int64_t cell, double dt, double V, uint64_t
     }
 }
 
+// ------------------------------------------------------------ collision_swpm.jl
+// swpm! (collision_swpm.jl:201-288) with compute_n_coll_single_species
+// (:170-173).  The (sigma g)_max estimate lives in the pair's
+// CollisionFactors (sigma_g_w_max field).  Draws come from the NTC streams:
+// U for n_coll, then per candidate U_i, U_k, retries of U_k, U_acc (g > eps),
+// U_phi, U_theta (accepted).  The reference checks the storage size once per
+// accepted collision and then appends two particles; here each append checks.
+void swpm_cell(Orc& o, int s, int64_t cell, double G, double dt, double V, uint64_t seed, uint64_t step)
+{
+    CollisionFactors& cf = o.cfa(s, s, cell);
+    const uint32_t pc = pair_code(o, s, s);
+    const uint32_t rc = (uint32_t)(cell - 1);
+    ParticleVector& P = o.pv[s];
+    double w_max = 0.0;
+    {
+        const ParticleIndexer& p = o.pi(cell, s);
+        for (int64_t i = p.start1; i <= p.end1; ++i) w_max = std::max(w_max, P.at(i).w);
+        if (p.n_group2 > 0)
+            for (int64_t i = p.start2; i <= p.end2; ++i) w_max = std::max(w_max, P.at(i).w);
+    }
+    const double wtf = 1.0 / (1.0 + G);
+    const double inv_w_max = 1.0 / w_max;
+    const int64_t np = o.pi(cell, s).n_local;
+    cf.n1 = np;
+    cf.n2 = np;
+    orc_stream r0 = orc_stream_make(seed, ORC_TAG_NCOLL, pc, step, rc, 0);
+    const double n_coll_float =
+        0.5 * dt * (double)np * (double)(np - 1) * cf.sigma_g_w_max * w_max * (G + 1.0) / V + orc_stream_uniform(&r0);
+    const int64_t n_coll_int = (int64_t)std::floor(n_coll_float);
+    cf.n_coll = n_coll_int;
+    cf.n_coll_performed = 0;
+    const Interaction& I = o.inter[s + o.n_species * s];
+    CollisionData cd;
+    for (int64_t j = 0; j < n_coll_int; ++j) {
+        orc_stream rng = orc_stream_make(seed, ORC_TAG_CAND, pc, step, rc, (uint32_t)j);
+        const int64_t nl = o.pi(cell, s).n_local;
+        int64_t i = (int64_t)std::floor(orc_stream_uniform(&rng) * (double)nl);
+        int64_t k = (int64_t)std::floor(orc_stream_uniform(&rng) * (double)nl);
+        while (i == k) k = (int64_t)std::floor(orc_stream_uniform(&rng) * (double)nl);
+        i = map_cont_index(o.pi(cell, s), i);
+        k = map_cont_index(o.pi(cell, s), k);
+        const int64_t phys_i = P.index[i - 1] - 1;
+        const int64_t phys_k = P.index[k - 1] - 1;
+        compute_g(cd, P.particles[phys_i], P.particles[phys_k]);
+        if (cd.g > EPS) {
+            const double sigma = sigma_vhs(I, cd.g);
+            const double sigma_g = sigma * cd.g;
+            cf.sigma_g_w_max = std::max(sigma_g, cf.sigma_g_w_max);
+            const double wm = std::max(P.particles[phys_i].w, P.particles[phys_k].w);
+            if (orc_stream_uniform(&rng) < sigma_g * wm * inv_w_max / cf.sigma_g_w_max) {
+                cf.n_coll_performed += 1;
+                compute_com(cd, I, P.particles[phys_i], P.particles[phys_k]);
+                const double dw = std::min(P.particles[phys_i].w, P.particles[phys_k].w) * wtf;
+                P.particles[phys_i].w -= dw;
+                P.particles[phys_k].w -= dw;
+                for (int q = 0; q < 2; ++q) {
+                    if (P.length() <= o.n_total[s]) pv_resize(P, P.length() + DELTA_PARTICLES);
+                    update_buffer_index_new_particle(o, cell, s);
+                    Particle& src = P.particles[q == 0 ? phys_i : phys_k];
+                    Particle& dst = P.at(o.n_total[s]);
+                    dst.w = dw;
+                    for (int c = 0; c < 3; ++c) {
+                        dst.v[c] = src.v[c];
+                        dst.x[c] = src.x[c];
+                    }
+                }
+                scatter_vhs(&rng, cd, I, P.at(o.n_total[s] - 1), P.at(o.n_total[s]));
+            }
+        }
+    }
+}
+
 // ----------------------------------------------------------- physical_props.jl
 struct PropsOut {
     double* lpa;
@@ -1436,6 +1508,20 @@ void orc_ntc_cells(void* h, int32_t s1, int32_t s2, double dt, const double* V, 
     } else {
         for (int64_t c = 1; c <= nc; ++c) orc_ntc(h, s1, s2, c, dt, V ? V[c - 1] : 1.0, seed, step, dw_tol, equal_weight);
     }
+}
+
+// swpm! over every cell in order (the per-cell loop of
+// test/test_1D_couette_varweight_swpm.jl:76-83 without the merging); V per
+// cell, NULL for 1.0.  Cell is 1-based in orc_swpm.
+void orc_swpm(void* h, int32_t s, int64_t cell, double G, double dt, double V, uint64_t seed, uint64_t step)
+{
+    swpm_cell(*(Orc*)h, s, cell, G, dt, V, seed, step);
+}
+
+void orc_swpm_cells(void* h, int32_t s, double G, double dt, const double* V, uint64_t seed, uint64_t step)
+{
+    Orc* o = (Orc*)h;
+    for (int64_t c = 1; c <= o->n_cells; ++c) swpm_cell(*o, s, c, G, dt, V ? V[c - 1] : 1.0, seed, step);
 }
 
 // mode 0: compute_props!, 1: compute_props_with_total_moments!,

@@ -67,6 +67,8 @@ def lib():
             "orc_estimate_sigma_g_w_max_single": (d, [vp, i32, i32, d, d, d, d]),
             "orc_ntc": (None, [vp, i32, i32, i64, d, d, u64, u64, d, i32]),
             "orc_ntc_cells": (None, [vp, i32, i32, d, P(d), u64, u64, d, i32, i32]),
+            "orc_swpm": (None, [vp, i32, i64, d, d, d, u64, u64]),
+            "orc_swpm_cells": (None, [vp, i32, d, d, P(d), u64, u64]),
             "orc_compute_props": (None, [vp, i32, P(i32), i32, d, P(d), P(d), P(d), P(d), P(d), P(d), P(d), i32]),
             "orc_avg_props": (None, [i64, P(d), P(d), d]),
             "orc_convect": (None, [vp, i32, d, i64, d, P(d), d, u64, u64, i32, i32]),
@@ -292,6 +294,16 @@ class Oracle:
             Va = np.ascontiguousarray(np.broadcast_to(np.asarray(V, float), (self.n_cells,)))
         self.L.orc_ntc_cells(self.h, s1, s2, dt, _p(Va) if Va is not None else None, seed, step, dw_tol,
                              1 if equal_weight else 0, nthreads)
+
+    def swpm(self, s, cell, G, dt, V, seed, step):
+        """swpm! of one cell (1-based), collision_swpm.jl:201-288."""
+        self.L.orc_swpm(self.h, s, cell, G, dt, V, seed, step)
+
+    def swpm_cells(self, s, G, dt, V, seed, step):
+        Va = None
+        if V is not None:
+            Va = np.ascontiguousarray(np.broadcast_to(np.asarray(V, float), (self.n_cells,)))
+        self.L.orc_swpm_cells(self.h, s, G, dt, _p(Va) if Va is not None else None, seed, step)
 
     def compute_props(self, mode=0, powers=(), Tref=300.0, inv_V=None, nthreads=1):
         ns, nc = self.n_species, self.n_cells
