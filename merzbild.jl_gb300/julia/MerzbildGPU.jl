@@ -26,11 +26,14 @@ carries a seed and the time-step index instead of a generator state.
 """
 module MerzbildGPU
 
+import Merzbild  # setup estimates (estimate_sigma_g_w_max) stay the reference's own
+
 export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, DeviceWalls1D, DeviceOctree,
        upload!, download, ntc!, ntc_equal_weight!, convect_particles!, convect_particles_and_compute_cell!,
        sort_particles!, squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
        avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
-       DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf
+       DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf,
+       swpm!, create_collision_factors_swpm_array!
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -222,6 +225,30 @@ function ntc_equal_weight!(rng::DeviceRNG, dp::DeviceParticles, cell, species1, 
 end
 ntc_equal_weight!(rng::DeviceRNG, dp::DeviceParticles, cell, species, Δt) =
     ntc_equal_weight!(rng, dp, cell, species, species, Δt)
+
+"""
+    swpm!(rng, dp, cell, species, G, Δt)
+
+swpm! (collision_swpm.jl:201-288) for one cell or a range (first, last);
+(σ g)_max per cell is the pair's collision factor
+(`create_collision_factors_swpm_array!`).
+"""
+function swpm!(rng::DeviceRNG, dp::DeviceParticles, cell, species, G, Δt)
+    cb, ce = cellrange(cell)
+    check(ccall((:mz_swpm, libmz), Cint, (Ptr{Cvoid}, Int32, Float64, Float64, Int64, Int64, UInt64),
+                dp.ptr, species - 1, G, Δt, cb, ce, rng.step), dp.ctx)
+end
+
+"""(σ g)_max of every species pair in every cell: estimate_sigma_g_w_max with
+Fnum = 1 (create_collision_factors_swpm_array, collision_swpm.jl:118-149)."""
+function create_collision_factors_swpm_array!(dp::DeviceParticles, interactions, species_data, T_list;
+                                              mult_factor=1.0)
+    for s2 in 1:dp.n_species, s1 in 1:dp.n_species
+        v = Merzbild.estimate_sigma_g_w_max(interactions[s1, s2], species_data[s1], species_data[s2], T_list[s1],
+                                            T_list[s2], 1.0; mult_factor=mult_factor)
+        set_sigma_g_w_max!(dp, s1, s2, fill(v, dp.n_cells))
+    end
+end
 
 """Set (σ g w)_max of a species pair for every cell (create_collision_factors_array)."""
 function set_sigma_g_w_max!(dp::DeviceParticles, species1, species2, values::Vector{Float64})
