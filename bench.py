@@ -45,7 +45,10 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--no-extra", action="store_true", help="skip the batched 0-D and serving measurements")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the batched 0-D, variable-weight Couette and serving measurements")
+    p.add_argument("--only-extra", default=None, choices=["batched_0d", "varweight", "serving"],
+                   help="run one of the extra measurements alone and print its result")
     p.add_argument("--seed", type=int, default=1234)
     return p.parse_args()
 
@@ -255,6 +258,79 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
     return out
 
 
+def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
+    """Variable-weight Couette (test/test_1D_couette_varweight.jl's loop at the
+    configuration's size): 1,000 cells over L = 5e-4 m, Ar at n = 1e23 and
+    273 K, 1,000 particles per cell with seeded log-uniform weights over two
+    decades, diffuse walls at -/+500 m/s, dt = 0.2 / nu.  One step = ntc! with
+    splitting for every cell, octree N:2 merging of the cells above 1,200
+    particles down to 300 (one launch), convection, sort,
+    compute_props_sorted!.  The plain form calls ntc! and the merge cell by
+    cell (the reference's loop) for one step."""
+    import numpy as np
+
+    nx, ppc, threshold, target = 1000, 1000, 1200, 300
+    sp = [mz.Species("Ar", mz.AR_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    grid = mz.Grid1DUniform(L_DOMAIN, nx)
+    Fnum = grid.dx * NDENS / ppc
+    walls = mz.MaxwellWalls1D(sp, T_WALL, T_WALL, -V_WALL, V_WALL, 1.0, 1.0)
+    dt = 0.2 / mz.mean_collision_frequency(inter, sp, 0, NDENS, T_WALL)
+    rng = np.random.default_rng(seed)
+    n0 = nx * ppc
+    cell = np.repeat(np.arange(nx, dtype=np.int32), ppc)
+    x = rng.random((n0, 3))
+    x[:, 0] = (cell + rng.uniform(0.01, 0.99, n0)) * grid.dx
+    v = rng.normal(0.0, (mz.K_B * T_WALL / mz.AR_MASS) ** 0.5, (n0, 3))
+    w = Fnum * 10.0 ** (2.0 * (rng.random(n0) - 0.5))
+    w *= n0 * Fnum / w.sum()
+    dom = mz.Domain(ctx, nx, sp, 5_000_000, interactions=inter, seed=seed)
+    dom.upload(0, w, v, x, cell)
+    dom.set_cell_volumes(grid.V)
+    dom.set_sigma_g_w_max(0, 0, mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], T_WALL, T_WALL, Fnum))
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    props = mz.PhysProps(dom)
+
+    def one_step(step, plain=False):
+        if plain:
+            for c in range(nx):
+                dom.ntc(0, 0, dt, step, cells=(c, c + 1), equal_weight=False)
+                dom.merge_octree(0, octree, target, threshold=threshold, cells=(c, c + 1), grid=grid, step=step)
+        else:
+            dom.ntc(0, 0, dt, step, equal_weight=False)
+            dom.merge_octree(0, octree, target, threshold=threshold, grid=grid, step=step)
+        dom.convect(0, grid, walls, dt, step)
+        dom.sort(0, grid)
+        mz.compute_props_sorted(dom, props)
+
+    for t in range(1, warmup + 1):
+        one_step(t)
+    dom.counters(reset=True)
+    ctx.synchronize()
+    ctx.timer_start()
+    live = 0
+    for t in range(warmup + 1, warmup + steps + 1):
+        live += dom.info(0)["n_total"]
+        one_step(t)
+    ms = ctx.timer_stop()
+    cnt = dom.counters(reset=True)
+    ctx.synchronize()
+    n_plain = dom.info(0)["n_total"]
+    t0 = time.perf_counter()
+    one_step(warmup + steps + 1, plain=True)
+    ctx.synchronize()
+    plain_s = time.perf_counter() - t0
+    value = live / (ms / 1e3)
+    out = {"workload": "1-D Couette, variable weight (2 decades), 1,000 cells x 1,000 initial particles, "
+                       "ntc! with splitting + octree merge 1,200 -> 300 + convect + sort + props",
+           "mean_live_particles": live / steps, "steps": steps, "value": value, "unit": "particle-steps/s",
+           "ms_per_step": ms / steps, "collisions_per_s": cnt["accepted"] / (ms / 1e3),
+           "splits_per_step": cnt["splits"] / steps, "merged_cells_per_step": cnt["merges"] / steps,
+           "plain_value": n_plain / plain_s, "batched_over_plain": value / (n_plain / plain_s)}
+    dom.close()
+    return out
+
+
 def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
     """Serving loop: seeded Poisson arrivals (mean `rate` per s over `window_s`)
     of 0-D relaxation requests, 70 % Ar and 30 % Ar + He, particles
@@ -377,6 +453,11 @@ def run_gpu(args):
     barrier = Barrier(world)
     ctx = mz.Context(local)
     seed = args.seed + 7919 * rank  # independent replicas
+    if args.only_extra:
+        fn = {"batched_0d": batched_0d, "varweight": varweight_couette, "serving": serving}[args.only_extra]
+        print(json.dumps({args.only_extra: fn(mz, ctx, seed)}), flush=True)
+        ctx.close()
+        return
     sp, inter, grid, Fnum, walls, dt, dom, smax = setup_device(mz, ctx, args, seed)
     log("domain created")
     dom.sample_grid_ndens(0, grid, NDENS, T_WALL, Fnum, step=0)
@@ -385,8 +466,8 @@ def run_gpu(args):
     inst = mz.PhysProps(dom)
     avg = mz.PhysProps(dom)
     K, W = args.steps, args.warmup
-    # the autotuner times each mapping on real steps (3 steps before the
-    # warm-up), then W untimed warm-up steps
+    # the autotuner times each mapping on real steps (two rounds of 4 steps
+    # per mapping before the warm-up), then W untimed warm-up steps
     tune_steps = 6 * 4
     mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=4)
     dom.step(make_plan(mz, grid, walls, dt, tune_steps, K), W, inst, avg)
@@ -492,11 +573,13 @@ def run_gpu(args):
                "note": f"initial state uploaded once ({h2d} B) inside the timed region, amortised over {K} steps; "
                        "cell properties (np, n, v, T) read back after every step"}
 
-    extra_0d = extra_srv = None
+    extra_0d = extra_srv = extra_vw = None
     log(f"e2e: {e2e}")
     if not args.no_extra and rank == 0:
         extra_0d = batched_0d(mz, ctx, seed)
         log(f"batched 0-D: {extra_0d}")
+        extra_vw = varweight_couette(mz, ctx, seed)
+        log(f"variable-weight Couette: {extra_vw}")
         extra_srv = serving(mz, ctx, seed)
         log(f"serving: {extra_srv}")
 
@@ -514,7 +597,7 @@ def run_gpu(args):
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-               "plain": plain, "batched_0d": extra_0d, "serving": extra_srv}
+               "plain": plain, "batched_0d": extra_0d, "varweight_couette": extra_vw, "serving": extra_srv}
         print(json.dumps(out), flush=True)
     ctx.close()
 

@@ -360,7 +360,7 @@ int mz_domain_create(mz_ctx* c, int64_t n_cells, int32_t n_species, const int64_
     MZ_CK(cudaMemset(d->d_counters, 0, sizeof(Counters)));
     MZ_CK(cudaMalloc(&d->d_status, sizeof(int)));
     MZ_CK(cudaMemset(d->d_status, 0, sizeof(int)));
-    MZ_CK(cudaMalloc(&d->d_scalar, 8 * sizeof(int64_t)));
+    MZ_CK(cudaMalloc(&d->d_scalar, 16 * sizeof(int64_t)));
     MZ_CK(cudaMalloc(&d->d_tile_sums, (scan_tiles(n_cells) + 1) * sizeof(int64_t)));
     MZ_CK(cudaMallocHost(&d->h_scalar, 8 * sizeof(int64_t)));
     *out = d;

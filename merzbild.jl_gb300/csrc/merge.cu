@@ -8,12 +8,14 @@
 //     ties (compute_octree!, :998-1039), found by a warp arg-max;
 //   * split_bin! (:503-633): octants and counts per particle in parallel; the
 //     per-octant weight sums are accumulated sequentially in particle order
-//     (one lane per octant), so bin weights -- which decide later splits --
-//     carry the reference's rounding; children are numbered as the reference
+//     (one lane per octant, over the octant's range after the counting sort),
+//     so bin weights -- which decide later splits -- carry the reference's
+//     rounding; children are numbered as the reference
 //     numbers them and the particle list is re-ordered with the reference's
 //     counting sort (which reverses the order inside each octant);
 //   * bin moments (compute_bin_props!, :646-700) are sequential sums, one
-//     lane per bin;
+//     lane per bin; bins of more than WIDE_BIN particles are summed by the
+//     whole warp (equal to the sequential sums to round-off);
 //   * the k-th bin that holds more than two particles draws its six direction
 //     signs from draws 6k .. 6k+5 of the cell's stream: the reference's
 //     sequential draws in bin order.
@@ -22,7 +24,8 @@
 // particles.jl:478-566): group 2 first, then group 1; deleted slots become dead.
 //
 // Each warp works in its own slice of a scratch buffer: the bins, the
-// particle list, the octant of every particle and the new particles.
+// particle list, the octant of every particle, a copy of the particles in
+// list order (bin moments read contiguous ranges) and the new particles.
 #include "mz_host.h"
 
 #include <algorithm>
@@ -54,9 +57,10 @@ struct MergeArgs {
     uint32_t step;
     // per-warp scratch: stride in bytes and offsets of each array
     char* scratch;
-    size_t stride, off_pis, off_tmp, off_w, off_oct, off_ov, off_ox;
+    size_t stride, off_pis, off_tmp, off_w, off_tw, off_lv, off_lx, off_oct, off_ov, off_ox;
     int64_t* deleted;  // total particles deleted
     int64_t* merged;   // cells merged
+    unsigned int* next;  // cell counter of the warps
 };
 
 __device__ __forceinline__ double warp_min(double v)
@@ -100,6 +104,121 @@ __device__ __forceinline__ void bounds_of(const Cols& A, const int32_t* pis, int
     }
 }
 
+// compute_bin_props! (:646-700) of the bin list[bs, be]: mean velocity and
+// position, and the standard deviations sqrt(sum w (v - vm)^2 / w) per
+// component; sums in particle order by one lane
+__device__ __forceinline__ void bin_moments_lane(const PV* lv, const PX* lx, int bs, int be, double inv_w, double* vm,
+                                                 double* xm, double* sv, double* sx)
+{
+    double vs[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k) vm[k] = xm[k] = 0.0;
+    for (int i = bs; i <= be; ++i) {
+        const PV v = lv[i];
+        const PX x = lx[i];
+        vm[0] = vm[0] + v.w * v.vx;
+        vm[1] = vm[1] + v.w * v.vy;
+        vm[2] = vm[2] + v.w * v.vz;
+        xm[0] = xm[0] + v.w * x.x;
+        xm[1] = xm[1] + v.w * x.y;
+        xm[2] = xm[2] + v.w * x.z;
+    }
+    for (int k = 0; k < 3; ++k) {
+        vm[k] = vm[k] * inv_w;
+        xm[k] = xm[k] * inv_w;
+    }
+    for (int i = bs; i <= be; ++i) {
+        const PV v = lv[i];
+        const PX x = lx[i];
+        const double dv[3] = {v.vx - vm[0], v.vy - vm[1], v.vz - vm[2]};
+        const double dx[3] = {x.x - xm[0], x.y - xm[1], x.z - xm[2]};
+        for (int k = 0; k < 3; ++k) {
+            vs[k] = vs[k] + v.w * (dv[k] * dv[k]);
+            xs[k] = xs[k] + v.w * (dx[k] * dx[k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        sv[k] = sqrt(vs[k] * inv_w);
+        sx[k] = sqrt(xs[k] * inv_w);
+    }
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// the same moments by the whole warp: lane-strided partial sums added in a
+// tree (equal to the sequential sums to round-off; the bin weight inv_w and
+// with it every split decision come from the sequential octant sums)
+__device__ __forceinline__ void bin_moments_warp(const PV* lv, const PX* lx, int bs, int be, double inv_w, double* vm,
+                                                 double* xm, double* sv, double* sx)
+{
+    const int lane = threadIdx.x & 31;
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = bs + lane; i <= be; i += 32) {
+        const PV v = lv[i];
+        const PX x = lx[i];
+        m[0] += v.w * v.vx;
+        m[1] += v.w * v.vy;
+        m[2] += v.w * v.vz;
+        m[3] += v.w * x.x;
+        m[4] += v.w * x.y;
+        m[5] += v.w * x.z;
+    }
+    for (int k = 0; k < 3; ++k) {
+        vm[k] = warp_sum_d(m[k]) * inv_w;
+        xm[k] = warp_sum_d(m[3 + k]) * inv_w;
+    }
+    double q[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = bs + lane; i <= be; i += 32) {
+        const PV v = lv[i];
+        const PX x = lx[i];
+        const double dv[3] = {v.vx - vm[0], v.vy - vm[1], v.vz - vm[2]};
+        const double dx[3] = {x.x - xm[0], x.y - xm[1], x.z - xm[2]};
+        for (int k = 0; k < 3; ++k) {
+            q[k] += v.w * (dv[k] * dv[k]);
+            q[3 + k] += v.w * (dx[k] * dx[k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        sv[k] = sqrt(warp_sum_d(q[k]) * inv_w);
+        sx[k] = sqrt(warp_sum_d(q[3 + k]) * inv_w);
+    }
+}
+
+// compute_new_particles! (:736-933) for one bin of more than two particles:
+// two particles of half its weight at vm -/+ sv and xm -/+ sx, the six signs
+// from draws 6k .. 6k+5 of the cell's stream (k-th such bin), positions
+// clamped to the grid in 1-D
+__device__ __forceinline__ void emit_pair(const MergeArgs& a, const Stream& st, int kbig, double w,
+                                          const double* vm, const double* xm, const double* sv, const double* sx,
+                                          PV* ov, PX* ox)
+{
+    Stream r = st;
+    r.n = 6u * (uint32_t)kbig;
+    double dvs[3], dxs[3];
+    for (int k = 0; k < 3; ++k) dvs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
+    for (int k = 0; k < 3; ++k) dxs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
+    const double w1 = 0.5 * w;
+    double x1[3], x2[3];
+    for (int k = 0; k < 3; ++k) {
+        x1[k] = xm[k] + dxs[k] * sx[k];
+        x2[k] = xm[k] - dxs[k] * sx[k];
+    }
+    if (a.clamp) {
+        x1[0] = x1[0] < a.min_x ? a.min_x : (x1[0] > a.max_x ? a.max_x : x1[0]);
+        x2[0] = x2[0] < a.min_x ? a.min_x : (x2[0] > a.max_x ? a.max_x : x2[0]);
+    }
+    ov[0] = PV{w1, vm[0] + dvs[0] * sv[0], vm[1] + dvs[1] * sv[1], vm[2] + dvs[2] * sv[2]};
+    ov[1] = PV{w1, vm[0] - dvs[0] * sv[0], vm[1] - dvs[1] * sv[1], vm[2] - dvs[2] * sv[2]};
+    ox[0] = PX{x1[0], x1[1], x1[2], 0.0};
+    ox[1] = PX{x2[0], x2[1], x2[2], 0.0};
+}
+
+constexpr int WIDE_BIN = 48;  // bins of more particles get their moments from the whole warp
+
 __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char* base)
 {
     const int lane = threadIdx.x & 31;
@@ -109,6 +228,9 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
     int32_t* pis = reinterpret_cast<int32_t*>(base + a.off_pis);
     int32_t* tmp = reinterpret_cast<int32_t*>(base + a.off_tmp);
     double* wl = reinterpret_cast<double*>(base + a.off_w);
+    double* tw = reinterpret_cast<double*>(base + a.off_tw);
+    PV* lv = reinterpret_cast<PV*>(base + a.off_lv);
+    PX* lx = reinterpret_cast<PX*>(base + a.off_lx);
     uint8_t* oct = reinterpret_cast<uint8_t*>(base + a.off_oct);
     PV* ov = reinterpret_cast<PV*>(base + a.off_ov);
     PX* ox = reinterpret_cast<PX*>(base + a.off_ox);
@@ -186,6 +308,7 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
         if (a.prm.bin_bounds_compute == BOUNDS_RECOMPUTE) bounds_of(A, pis, bs, be, vmin, vmax);
         double mid[3];
         for (int k = 0; k < 3; ++k) mid[k] = 0.5 * (vmin[k] + vmax[k]);
+        // octant and weight of every particle, in parallel
         int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int i = lane; i < nb; i += 32) {
             const PV v = A.wv[pis[bs + i]];
@@ -198,16 +321,6 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
 #pragma unroll
         for (int k = 0; k < 8; ++k) cnt[k] = __reduce_add_sync(0xFFFFFFFFu, cnt[k]);
         __syncwarp();
-        // weight per octant, summed in particle order as the reference does
-        int mine = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (lane == k) mine = cnt[k];
-        double wo = 0.0;
-        if (lane < 8 && mine > 0)
-            for (int i = 0; i < nb; ++i)
-                if (oct[i] == lane) wo += wl[i];
-        // children: non-empty octants in order; the first keeps the bin id
         int incl[8], run = 0;
         int nne = 0;
 #pragma unroll
@@ -216,6 +329,44 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
             incl[k] = run;
             nne += cnt[k] > 0;
         }
+        // the reference's counting sort: octant k fills [incl[k-1], incl[k])
+        // from its end, in particle order
+        int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i0 = 0; i0 < nb; i0 += 32) {
+            const int i = i0 + lane;
+            const bool in = i < nb;
+            const int o = in ? oct[i] : 8;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, o);
+            int r = __popc(peers & lanemask_lt()), end_o = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (o == k) {
+                    r += seen[k];
+                    end_o = incl[k];
+                }
+            if (in) {
+                tmp[end_o - 1 - r] = pis[bs + i];
+                tw[end_o - 1 - r] = wl[i];
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
+        }
+        // weight per octant, summed in particle order as the reference sums
+        // it: octant k's particles now sit in [incl[k-1], incl[k]) in reversed
+        // particle order, so lane k walks that range backwards
+        __syncwarp();
+        double wo = 0.0;
+        {
+            int lo = 0, hi = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (lane == k) {
+                    lo = incl[k] - cnt[k];
+                    hi = incl[k];
+                }
+            for (int j = hi - 1; j >= lo; --j) wo += tw[j];
+        }
+        // children: non-empty octants in order; the first keeps the bin id
         {
             int kch = 0, startk = bs;
             for (int k = 0; k < 8; ++k) {
@@ -250,40 +401,28 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
             }
             total -= 2;
         }
-        // the reference's counting sort: octant k fills [incl[k-1], incl[k])
-        // from its end, in particle order
-        int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int i0 = 0; i0 < nb; i0 += 32) {
-            const int i = i0 + lane;
-            const bool in = i < nb;
-            const int o = in ? oct[i] : 8;
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, o);
-            int r = __popc(peers & lanemask_lt()), end_o = 0;
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (o == k) {
-                    r += seen[k];
-                    end_o = incl[k];
-                }
-            if (in) tmp[end_o - 1 - r] = pis[bs + i];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
-        }
         __syncwarp();
         for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
         nbins += nne - 1;
         __syncwarp();
         if (nbins + 7 > a.prm.max_Nbins) break;
     }
+    // the particles in list order, so that every bin reads a contiguous range
+    for (int i = lane; i < n; i += 32) {
+        lv[i] = A.wv[pis[i]];
+        lx[i] = A.pos[pis[i]];
+    }
+    __syncwarp();
     if (nbins == 1 && lane == 0) {
         double w = 0.0;
-        for (int i = 0; i < n; ++i) w += A.wv[pis[i]].w;
+        for (int i = 0; i < n; ++i) w += lv[i].w;
         bins[0].w = w;
     }
     __syncwarp();
 
     // compute_bin_props! (:646-700) and compute_new_particles! (:736-933),
-    // one lane per bin; outputs in bin order
+    // one lane per bin (the whole warp for bins of many particles); outputs
+    // in bin order
     int out_base = 0, big_base = 0;
     Stream st;
     st.init(cell_seed(d, c), TAG_MERGE, (uint32_t)a.s, cell_step(d, c, a.step), cell_rid(d, c), 0);
@@ -308,63 +447,30 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
             }
         }
         const int pos = out_base + io - cnt_out, kbig = big_base + ib - big;
-        if (npe > 2) {
-            double vm[3] = {0, 0, 0}, xm[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
-            const double inv_w = 1.0 / B.w;
-            for (int i = B.start; i <= B.end; ++i) {
-                const PV v = A.wv[pis[i]];
-                const PX x = A.pos[pis[i]];
-                vm[0] = vm[0] + v.w * v.vx;
-                vm[1] = vm[1] + v.w * v.vy;
-                vm[2] = vm[2] + v.w * v.vz;
-                xm[0] = xm[0] + v.w * x.x;
-                xm[1] = xm[1] + v.w * x.y;
-                xm[2] = xm[2] + v.w * x.z;
-            }
-            for (int k = 0; k < 3; ++k) {
-                vm[k] = vm[k] * inv_w;
-                xm[k] = xm[k] * inv_w;
-            }
-            for (int i = B.start; i <= B.end; ++i) {
-                const PV v = A.wv[pis[i]];
-                const PX x = A.pos[pis[i]];
-                const double dv[3] = {v.vx - vm[0], v.vy - vm[1], v.vz - vm[2]};
-                const double dx[3] = {x.x - xm[0], x.y - xm[1], x.z - xm[2]};
-                for (int k = 0; k < 3; ++k) {
-                    vs[k] = vs[k] + v.w * (dv[k] * dv[k]);
-                    xs[k] = xs[k] + v.w * (dx[k] * dx[k]);
-                }
-            }
-            double sv[3], sx[3];
-            for (int k = 0; k < 3; ++k) {
-                sv[k] = sqrt(vs[k] * inv_w);
-                sx[k] = sqrt(xs[k] * inv_w);
-            }
-            Stream r = st;
-            r.n = 6u * (uint32_t)kbig;
-            double dvs[3], dxs[3];
-            for (int k = 0; k < 3; ++k) dvs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
-            for (int k = 0; k < 3; ++k) dxs[k] = r.u52() < (1ull << 51) ? -1.0 : 1.0;
-            const double w1 = 0.5 * B.w;
-            double x1[3], x2[3];
-            for (int k = 0; k < 3; ++k) {
-                x1[k] = xm[k] + dxs[k] * sx[k];
-                x2[k] = xm[k] - dxs[k] * sx[k];
-            }
-            if (a.clamp) {
-                x1[0] = x1[0] < a.min_x ? a.min_x : (x1[0] > a.max_x ? a.max_x : x1[0]);
-                x2[0] = x2[0] < a.min_x ? a.min_x : (x2[0] > a.max_x ? a.max_x : x2[0]);
-            }
-            ov[pos] = PV{w1, vm[0] + dvs[0] * sv[0], vm[1] + dvs[1] * sv[1], vm[2] + dvs[2] * sv[2]};
-            ov[pos + 1] = PV{w1, vm[0] - dvs[0] * sv[0], vm[1] - dvs[1] * sv[1], vm[2] - dvs[2] * sv[2]};
-            ox[pos] = PX{x1[0], x1[1], x1[2], 0.0};
-            ox[pos + 1] = PX{x2[0], x2[1], x2[2], 0.0};
-        } else if (npe >= 1) {
+        const bool wide = npe > WIDE_BIN;
+        if (npe > 2 && !wide) {
+            double vm[3], xm[3], sv[3], sx[3];
+            bin_moments_lane(lv, lx, B.start, B.end, 1.0 / B.w, vm, xm, sv, sx);
+            emit_pair(a, st, kbig, B.w, vm, xm, sv, sx, ov + pos, ox + pos);
+        } else if (npe >= 1 && npe <= 2) {
             // np == 1 or 2: the bin's particles are kept as they are
             for (int q = 0; q < npe; ++q) {
-                ov[pos + q] = A.wv[pis[B.start + q]];
-                ox[pos + q] = A.pos[pis[B.start + q]];
+                ov[pos + q] = lv[B.start + q];
+                ox[pos + q] = lx[B.start + q];
             }
+        }
+        // bins of many particles: the whole warp sums their moments, one bin
+        // at a time (a lane alone would walk hundreds of particles)
+        unsigned wmask = __ballot_sync(0xFFFFFFFFu, wide);
+        while (wmask) {
+            const int q = __ffs(wmask) - 1;
+            wmask &= wmask - 1;
+            const int qs = __shfl_sync(0xFFFFFFFFu, B.start, q), qe = __shfl_sync(0xFFFFFFFFu, B.end, q);
+            const double qw = __shfl_sync(0xFFFFFFFFu, B.w, q);
+            const int qpos = __shfl_sync(0xFFFFFFFFu, pos, q), qk = __shfl_sync(0xFFFFFFFFu, kbig, q);
+            double vm[3], xm[3], sv[3], sx[3];
+            bin_moments_warp(lv, lx, qs, qe, 1.0 / qw, vm, xm, sv, sx);
+            if (lane == 0) emit_pair(a, st, qk, qw, vm, xm, sv, sx, ov + qpos, ox + qpos);
         }
         out_base += __shfl_sync(0xFFFFFFFFu, io, 31);
         big_base += __shfl_sync(0xFFFFFFFFu, ib, 31);
@@ -398,15 +504,29 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
     }
 }
 
+// Warps take the next cell from a counter, so the merged cells (a minority of
+// the range, and each merge a long chain) spread evenly over the warps.
 __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
     char* base = a.scratch + (size_t)warp * a.stride;
-    for (int c = a.cb + warp; c < a.ce; c += nwarps) {
-        const Indexer p = d.sp[a.s].ind[c];
-        const int n = p.n1 + p.n2;
-        if (n == 0 || (a.threshold >= 0 && n <= a.threshold)) continue;
+    for (;;) {
+        // lane 0 claims cells until it finds one to merge
+        int c = a.ce;
+        if (lane == 0)
+            for (;;) {
+                const int q = a.cb + (int)atomicAdd(a.next, 1u);
+                if (q >= a.ce) break;
+                const Indexer p = d.sp[a.s].ind[q];
+                const int n = p.n1 + p.n2;
+                if (n > 0 && (a.threshold < 0 || n > a.threshold)) {
+                    c = q;
+                    break;
+                }
+            }
+        c = __shfl_sync(0xFFFFFFFFu, c, 0);
+        if (c >= a.ce) break;
         merge_cell(d, a, c, base);
         __syncwarp();
     }
@@ -480,6 +600,12 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
     off += align256(nmax * sizeof(int32_t));
     a.off_w = off;
     off += align256(nmax * sizeof(double));
+    a.off_tw = off;
+    off += align256(nmax * sizeof(double));
+    a.off_lv = off;
+    off += align256(nmax * sizeof(PV));
+    a.off_lx = off;
+    off += align256(nmax * sizeof(PX));
     a.off_oct = off;
     off += align256(nmax);
     a.off_ov = off;
@@ -487,9 +613,11 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
     a.off_ox = off;
     off += align256(outmax * sizeof(PX));
     a.stride = off;
+    // one warp per block: the merging warps spread over all SMs (a merge is a
+    // long sequential chain; SMs shared by several merging warps slow each)
     const int warps_wanted = (int)std::min<int64_t>(ncells, (int64_t)c->num_sms * 16);
-    const int blocks = (int)std::max<int64_t>(1, div_up(warps_wanted, 8));
-    const size_t need = (size_t)blocks * 8 * a.stride;
+    const int blocks = std::max(1, warps_wanted);
+    const size_t need = (size_t)blocks * a.stride;
     if (need > d->merge_scratch_bytes) {
         cudaFree(d->d_merge_scratch);
         d->d_merge_scratch = nullptr;
@@ -500,7 +628,9 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
     a.scratch = static_cast<char*>(d->d_merge_scratch);
     a.deleted = d->d_scalar + 2;
     a.merged = d->d_scalar + 3;
-    MZ_LAUNCH(c, "merge", k_merge, blocks, 256, 0, v, a);
+    a.next = reinterpret_cast<unsigned int*>(d->d_scalar + 8);
+    MZ_CK(cudaMemsetAsync(a.next, 0, sizeof(unsigned int), c->stream));
+    MZ_LAUNCH(c, "merge", k_merge, blocks, 32, 0, v, a);
     MZ_CK(cudaMemcpyAsync(d->h_scalar + 2, d->d_scalar + 2, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     MZ_CK(cudaStreamSynchronize(c->stream));
     SpeciesHost& S = d->sp[s];

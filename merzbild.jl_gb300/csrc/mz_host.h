@@ -90,7 +90,7 @@ struct mz_domain_s {
     mz::CollisionFactors* d_cf = nullptr;
     mz::Counters* d_counters = nullptr;
     int* d_status = nullptr;
-    int64_t* d_scalar = nullptr;   // small device scratch (totals)
+    int64_t* d_scalar = nullptr;   // small device scratch (totals), 16 entries
     int64_t* d_tile_sums = nullptr;  // per-tile totals of the cell scans
     int64_t* h_scalar = nullptr;   // pinned mirror
     uint64_t seed = 1234;
