@@ -466,13 +466,14 @@ def run_gpu(args):
     inst = mz.PhysProps(dom)
     avg = mz.PhysProps(dom)
     K, W = args.steps, args.warmup
-    # the autotuner times each mapping on real steps (two rounds of 4 steps
-    # per mapping before the warm-up), then W untimed warm-up steps
-    tune_steps = 6 * 4
-    mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=4)
+    # the autotuner times each mapping (lanes per cell x one or two launches
+    # per step) on real steps, two rounds of 8 steps each before the warm-up,
+    # then W untimed warm-up steps
+    tune_steps = 12 * 8
+    mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=8)
     dom.step(make_plan(mz, grid, walls, dt, tune_steps, K), W, inst, avg)
     ctx.synchronize()
-    log(f"warm-up done (mapping: {mapping[0]} lanes per cell)")
+    log(f"warm-up done (mapping: {mapping[0]} lanes per cell, {2 if mapping[1] == 1 else 1} launches per step)")
     mz.clear_props(avg)
     dom.counters(reset=True)
     step0 = tune_steps + W
@@ -505,18 +506,28 @@ def run_gpu(args):
     timings = ctx.kernel_timings()
     ctx.set_kernel_timing(False)
     tot = sum(v[0] for v in timings.values())
-    kname = "step_cell" if "step_cell" in timings else max(timings.items(), key=lambda kv: kv[1][0])[0]
-    kms, klaunch = timings[kname]
-    avg_launch_s = kms / klaunch / 1e3
+    # the step's particle kernel: one fused launch, or (when the autotuner
+    # chose two launches per step) the gather + props launch and the NTC +
+    # convection launch together, each launched once per step
+    two = "step_cell" not in timings and "step_cell_final" in timings and "step_cell_inplace" in timings
+    if two:
+        kname = "step_cell_final+step_cell_inplace"
+        avg_launch_s = sum(timings[k][0] / timings[k][1] for k in ("step_cell_final", "step_cell_inplace")) / 1e3
+    else:
+        kname = "step_cell" if "step_cell" in timings else max(timings.items(), key=lambda kv: kv[1][0])[0]
+        kms, klaunch = timings[kname]
+        avg_launch_s = kms / klaunch / 1e3
     peak, peak_kind = measured_peaks()
     achieved = ALG_BYTES * n / avg_launch_s / 1e9
-    # DRAM bytes per particle of the full-step launch from the committed ncu
-    # summary (captured on a smaller case; traffic scales with particles)
+    # DRAM bytes per particle of the step's particle kernel(s) from the
+    # committed ncu summary (captured on a smaller case; traffic scales with
+    # particles)
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "step_cell_traffic.md")
     if os.path.exists(tfile):
+        key = "dram_bytes_per_particle_two_launch" if two else "dram_bytes_per_particle"
         with open(tfile) as f:
-            m = re.search(r"^dram_bytes_per_particle:\s*([0-9.eE+-]+)", f.read(), re.M)
+            m = re.search(r"^" + key + r":\s*([0-9.eE+-]+)", f.read(), re.M)
         if m:
             traffic = float(m.group(1)) * n
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -593,7 +604,9 @@ def run_gpu(args):
                "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, sampled on the device)",
                "config": workload(args) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                                           "mapping": {"lanes_per_cell": mapping[0], "autotune_steps": tune_steps}},
+                                           "mapping": {"lanes_per_cell": mapping[0],
+                                                       "launches_per_step": 2 if mapping[1] == 1 else 1,
+                                                       "autotune_steps": tune_steps}},
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,

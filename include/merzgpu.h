@@ -121,6 +121,8 @@ typedef struct {
                              (0: 2,048; < 0: never); results do not depend on it */
     mz_grid1d grid;
     mz_walls1d walls;
+    int32_t launches;     /* 1-D: launches per step, 1 (fused) or 2 (sort + gather + props, then NTC +
+                             convection); 0: the autotuner's choice, else 1.  Results do not depend on it */
 } mz_step_plan;
 
 /* ---------------------------------------------------------------- context */
@@ -415,12 +417,16 @@ int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_step
 
 /* Choose the fused step's mapping by timing it: every combination of lanes
  * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the
- * block-per-cell threshold (512, 2,048, 8,192 particles, never) runs
- * trial_steps real steps of `plan` twice, in interleaved rounds (starting at
- * plan->step0; the state advances by 24 * trial_steps steps for 0-D plans,
- * 6 * trial_steps for 1-D, and every mapping gives the same results); the
- * fastest is kept for later mz_step calls whose plan leaves big_cell at 0.
- * No counterpart in the reference. */
+ * block-per-cell threshold (512, 2,048, 8,192 particles, never) or, for 1-D
+ * plans, of one fused launch per step against two (sort + gather + props,
+ * then NTC + convection) runs trial_steps real steps of `plan` twice, in
+ * two rounds of opposite order whose times add up (starting at
+ * plan->step0; the state advances by
+ * 24 * trial_steps steps for 0-D plans and 12 * trial_steps for 1-D, and
+ * every mapping gives the same results); the fastest is kept for later
+ * mz_step calls whose plan leaves big_cell at 0.  *big_cell_out receives the
+ * threshold (0-D) or 1 for the two-launch step (1-D).  No counterpart in the
+ * reference. */
 int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
 
 /* ---------------------------------------------------------------- counters */

@@ -111,6 +111,7 @@ struct mz_domain_s {
     // fused-step mapping chosen by mz_step_autotune (0: the default rules)
     int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
     int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
+    int32_t tuned_split = 0;    // 1-D: 1 = gather + props and NTC + convection in two launches
 };
 
 // SurfProps of a domain's 1-D walls (surface_props.jl:22-67): device sums

@@ -39,6 +39,7 @@ struct StepArgs {
     int gather;        // sort segment + gather A -> B
     int props;         // compute props of the (gathered) state
     int physics;       // NTC + convection of the next step
+    int advance;       // the last block advances the RNG step index
     int has_inst, has_avg;
     PropsPtrs inst, avg;
     double inv_navg;
@@ -89,16 +90,22 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
 // cells at once, one group of G lanes per cell.  The grid is resident (one
 // wave) and hands out cells through an atomic counter, so no partial last wave
 // idles the GPU.
-template <int G>
-__global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
+// MODE 0: the phases the launch's flags select; MODE 1: sort + gather + props
+// only (no NTC or convection code, so fewer registers and more resident
+// warps for this memory-bound part); MODE 2: NTC + convection in place only.
+template <int G, int MODE>
+__device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a, int32_t* cell_hist)
 {
     constexpr int CPW = 32 / G;
-    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
+    const bool gather_on = MODE == 1 ? true : (MODE == 2 ? false : a.gather != 0);
+    const bool physics_on = MODE == 1 ? false : (MODE == 2 ? true : a.physics != 0);
     const uint32_t step = *a.step_ptr;
     const int lane = threadIdx.x & 31;
     int32_t* wh = cell_hist + (threadIdx.x >> 5) * CELL_WINDOW;
-    for (int bin = lane; bin < CELL_WINDOW; bin += 32) wh[bin] = 0;
-    __syncwarp();
+    if (MODE != 1) {
+        for (int bin = lane; bin < CELL_WINDOW; bin += 32) wh[bin] = 0;
+        __syncwarp();
+    }
     const WarpGroup<G> grp;
     const int gi = lane / G;
     const int ns = d.n_species;
@@ -117,7 +124,7 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
             const SpeciesView& S = d.sp[s];
             const bool props1 = a.props && a.props_lag == 1;
             double mn = 0.0, msx = 0.0, msy = 0.0, msz = 0.0;
-            if (a.gather) {
+            if (gather_on) {
                 for (int q = 0; q < nq; ++q) {
                     const Indexer p = S.ind[c0 + q];
                     const Sums4 t = sort_gather_segment(S, c0 + q, p.start1, p.n1);
@@ -136,7 +143,7 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
             }
         }
         __syncwarp();
-        if (!a.physics && !(a.props && a.props_lag == 0)) continue;
+        if (!physics_on && !(a.props && a.props_lag == 0)) continue;
         // ntc_equal_weight! for every pair in the reference's order, one
         // group per cell
         const int c = c0 + gi;
@@ -146,7 +153,7 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
             for (int s = 0; s < ns; ++s) tot += d.sp[s].ind[c].n1;
             big = tot >= a.big_cell;
         }
-        if (a.physics && gi < nq && !big) {
+        if (physics_on && gi < nq && !big) {
             const uint64_t seed = cell_seed(d, c);
             const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
             const double V = d.cell_V[c];
@@ -164,8 +171,8 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                     R.smax = cf.smax;
                     R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
                     if (ncoll > 0)
-                        R = ntc_cell<true, G>(d, d.inter[cfi], single, c, ncoll, cf.smax, a.gather ? S1.B : S1.A,
-                                              a.gather ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
+                        R = ntc_cell<true, G>(d, d.inter[cfi], single, c, ncoll, cf.smax, gather_on ? S1.B : S1.A,
+                                              gather_on ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
                                               0, 0.0, seed, pc, stp, rid);
                     if (grp.rank == 0) {
                         cand += ncoll;
@@ -188,12 +195,12 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
                 if ((skip >> (q * G)) & 1u) skipq |= 1u << q;
             for (int s = 0; s < ns; ++s) {
                 const SpeciesView& S = d.sp[s];
-                const CellMoments r = props_cells(a.gather ? S.B : S.A, S.ind, c0, nq, S.mass, skipq);
+                const CellMoments r = props_cells(gather_on ? S.B : S.A, S.ind, c0, nq, S.mass, skipq);
                 if (lane < nq && !((skipq >> lane) & 1u))
                     write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
             }
         }
-        if (a.dims != 1 || !a.physics) continue;
+        if (a.dims != 1 || !physics_on) continue;
         // convect_particles! + get_cell for the next sort.  Destination counts
         // go to a per-warp histogram over a window of cells around the warp's
         // cells, flushed with one atomic per non-empty cell (consecutive
@@ -201,7 +208,7 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         const int kb = c0 + CPW / 2 - CELL_WINDOW / 2;
         for (int s = 0; s < ns; ++s) {
             const SpeciesView& S = d.sp[s];
-            const Cols& Q = a.gather ? S.B : S.A;
+            const Cols& Q = gather_on ? S.B : S.A;
             for (int q = 0; q < nq; ++q) {
                 const int cq = c0 + q;
                 const uint64_t seed = cell_seed(d, cq);
@@ -296,10 +303,30 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
         if (prev == gridDim.x - 1) {
             *a.done = 0;
             *a.next = 0;
-            *a.step_ptr = step + 1;
+            if (a.advance) *a.step_ptr = step + 1;
             __threadfence();
         }
     }
+}
+
+
+template <int G>
+__global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
+{
+    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
+    cell_body<G, 0>(d, a, cell_hist);
+}
+
+__global__ void __launch_bounds__(256, 2) k_cell_gather(DomainView d, StepArgs a)
+{
+    cell_body<8, 1>(d, a, nullptr);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256, 2) k_cell_physics(DomainView d, StepArgs a)
+{
+    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
+    cell_body<G, 2>(d, a, cell_hist);
 }
 
 // ntc_equal_weight! and the 0-D compute_props! of the cells with at least
@@ -564,18 +591,28 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         a.hitq_cap = (unsigned)std::min<int64_t>(d->hitq_cap, 0x7FFFFFFF);
     }
     const bool want_props = plan->props && (inst || a.has_avg);
+    const bool split = plan->dims == 1 && (plan->launches == 2 || (plan->launches == 0 && d->tuned_split > 0));
     const int G = d->tuned_lanes ? d->tuned_lanes : ntc_group_width(d->n_cells);
-    void (*kern)(DomainView, StepArgs) = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
-    int per_sm = 0;
-    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, CELL_SMEM));
-    const int blocks = (int)std::max<int64_t>(
-        1, std::min<int64_t>(div_up(d->n_cells, 8 * (32 / G)), (int64_t)c->num_sms * std::max(per_sm, 1)));
+    using KCell = void (*)(DomainView, StepArgs);
+    const KCell kern_full = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
+    const KCell kern_phys = G == 8 ? k_cell_physics<8> : (G == 16 ? k_cell_physics<16> : k_cell_physics<32>);
+    // a resident grid: as many blocks as fit at once, no more than the cells need
+    auto resident = [&](KCell k, size_t smem, int cpw) {
+        int per_sm = 0;
+        MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+        return (int)std::max<int64_t>(
+            1, std::min<int64_t>(div_up(d->n_cells, 8 * cpw), (int64_t)c->num_sms * std::max(per_sm, 1)));
+    };
+    const int blocks_full = resident(kern_full, CELL_SMEM, 32 / G);
+    const int blocks_phys = plan->dims == 1 ? resident(kern_phys, CELL_SMEM, 32 / G) : 0;
+    const int blocks_gather = plan->dims == 1 ? resident(k_cell_gather, 0, 4) : 0;
 
-    auto cell_launch = [&](int gather, int props, int physics) {
+    auto cell_launch = [&](int gather, int props, int physics, int advance = 1) {
         StepArgs b = a;
         b.gather = gather;
         b.props = props;
         b.physics = physics;
+        b.advance = advance;
         DomainView v = make_view(d);
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
@@ -584,7 +621,14 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
         if (physics && b.surf)
             MZ_CK(cudaMemsetAsync(b.surf, 0, (size_t)d->ns * 2 * SURF_Q * sizeof(double), c->stream));
-        MZ_LAUNCH(c, name, kern, blocks, 256, CELL_SMEM, v, b);
+        // 1-D launches that only sort + gather + props, or only collide and
+        // convect, take the kernels compiled for that part alone
+        if (a.dims == 1 && gather && !physics)
+            MZ_LAUNCH(c, name, k_cell_gather, blocks_gather, 256, 0, v, b);
+        else if (a.dims == 1 && !gather && !props && physics)
+            MZ_LAUNCH(c, name, kern_phys, blocks_phys, 256, CELL_SMEM, v, b);
+        else
+            MZ_LAUNCH(c, name, kern_full, blocks_full, 256, CELL_SMEM, v, b);
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
         if (physics && b.surf) MZ_LAUNCH(c, "step_surf", k_surf_finish, 1, 128, 0, b, d->ns);
     };
@@ -597,8 +641,16 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, SCATTER_TILE), (int64_t)c->num_sms * 8));
             MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total);
         }
-        cell_launch(1, props, physics);
-        for (int s = 0; s < d->ns; ++s) d->sp[s].cur ^= 1;  // B holds the sorted state
+        if (split && physics) {
+            // gather + props, then NTC + convection in place on the sorted
+            // state: each launch keeps less data in flight between its reads
+            cell_launch(1, props, 0, 0);
+            for (int s = 0; s < d->ns; ++s) d->sp[s].cur ^= 1;  // B holds the sorted state
+            cell_launch(0, 0, physics);
+        } else {
+            cell_launch(1, props, physics);
+            for (int s = 0; s < d->ns; ++s) d->sp[s].cur ^= 1;  // B holds the sorted state
+        }
     };
 
     const bool graph = plan->use_graph != 0;
@@ -653,20 +705,30 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     mz_ctx* c = d->ctx;
     const int32_t lanes_c[3] = {8, 16, 32};
     const int32_t big_c[4] = {512, 2048, 8192, -1};
-    const int nb = plan->dims == 0 ? 4 : 1;
+    // the second choice: the block-per-cell threshold (0-D) or the fused
+    // against the two-launch step (1-D)
+    const int nb = plan->dims == 0 ? 4 : 2;
     const int nconf = 3 * nb;
     mz_step_plan p = *plan;
     p.big_cell = 0;
-    std::vector<float> best(nconf, 3.0e38f);
+    p.launches = 0;
+    std::vector<float> total(nconf, 0.0f);
     uint64_t step = plan->step0;
     cudaEvent_t e0, e1;
     MZ_CK(cudaEventCreate(&e0));
     MZ_CK(cudaEventCreate(&e1));
-    // two interleaved rounds; a configuration's time is its faster round
+    auto apply = [&](int k) {
+        d->tuned_lanes = lanes_c[k / nb];
+        d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
+        d->tuned_split = plan->dims == 0 ? 0 : k % nb;
+    };
+    // two rounds, the second in reverse order, and a configuration's time is
+    // the sum of its two: the step time drifts as the simulation evolves (the
+    // collision-rate estimate adapts), and the reversal cancels a linear drift
     for (int round = 0; round < 2; ++round)
-        for (int k = 0; k < nconf; ++k) {
-            d->tuned_lanes = lanes_c[k / nb];
-            d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
+        for (int i = 0; i < nconf; ++i) {
+            const int k = round == 0 ? i : nconf - 1 - i;
+            apply(k);
             p.step0 = step;
             MZ_CK(cudaEventRecord(e0, c->stream));
             launch_step(d, &p, trial_steps, nullptr, nullptr);
@@ -675,13 +737,11 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
             float ms = 0.0f;
             MZ_CK(cudaEventElapsedTime(&ms, e0, e1));
             step += (uint64_t)trial_steps;
-            best[k] = std::min(best[k], ms);
+            total[k] += ms;
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const int kb = (int)(std::min_element(best.begin(), best.end()) - best.begin());
-    d->tuned_lanes = lanes_c[kb / nb];
-    d->tuned_big = plan->dims == 0 ? big_c[kb % nb] : -1;
+    apply((int)(std::min_element(total.begin(), total.end()) - total.begin()));
     if (lanes_out) *lanes_out = d->tuned_lanes;
-    if (big_out) *big_out = d->tuned_big;
+    if (big_out) *big_out = plan->dims == 0 ? d->tuned_big : d->tuned_split;
 }

@@ -94,6 +94,7 @@ struct MzStepPlan
     avg_start::Int64; n_avg::Int64; dt::Float64; dw_tol::Float64; step0::UInt64
     use_graph::Int32; big_cell::Int32
     grid::DeviceGrid1D; walls::DeviceWalls1D
+    launches::Int32
 end
 
 # ------------------------------------------------------------------ handles
@@ -350,7 +351,7 @@ simulations/1D/couette_benchmarking.jl:58-85 in one call.
 function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D, walls::DeviceWalls1D, Δt, step0=0,
                inst::Union{Nothing,DeviceProps}=nothing, avg::Union{Nothing,DeviceProps}=nothing,
                avg_start=0, n_avg=1, dims=1)
-    plan = MzStepPlan(dims, 1, 1, 1, avg_start, n_avg, Δt, 1e-16, step0, 1, 0, grid, walls)
+    plan = MzStepPlan(dims, 1, 1, 1, avg_start, n_avg, Δt, 1e-16, step0, 1, 0, grid, walls, 0)
     check(ccall((:mz_step, libmz), Cint, (Ptr{Cvoid}, Ref{MzStepPlan}, Int64, Ptr{Cvoid}, Ptr{Cvoid}),
                 dp.ptr, plan, n_steps, inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr),
           dp.ctx)

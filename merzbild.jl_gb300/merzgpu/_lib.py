@@ -74,7 +74,7 @@ MZ_REQ_QUEUED, MZ_REQ_RUNNING, MZ_REQ_DONE = 0, 1, 2
 class StepPlan(C.Structure):
     _fields_ = [("dims", i32), ("collide", i32), ("equal_weight", i32), ("props", i32), ("avg_start", i64),
                 ("n_avg", i64), ("dt", d), ("dw_tol", d), ("step0", u64), ("use_graph", i32), ("big_cell", i32),
-                ("grid", Grid1D), ("walls", Walls1D)]
+                ("grid", Grid1D), ("walls", Walls1D), ("launches", i32)]
 
 
 _SIGS = {

@@ -251,8 +251,30 @@ def test_autotuned_mapping_changes_no_result(ctx, orc):
         done = 0
         if tune:
             dom.autotune(plan, trial_steps=1)
-            done = 6
-        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 8 - done)
+            done = 12
+        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 16 - done)
         states.append(device_logical(dom, 0))
         dom.close()
     assert np.array_equal(states[0][1], states[1][1]) and np.array_equal(states[0][0], states[1][0])
+
+
+def test_two_launch_step_equals_fused(ctx, orc):
+    """The 1-D step as one fused launch and as two (sort + gather + props, then
+    NTC + convection in place) gives the same particles and the same averaged
+    and instantaneous properties, and both equal the oracle loop's averages."""
+    results = []
+    for launches in (1, 2):
+        sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc, nx=60, ppc=100, seed=23)
+        inst, avg = mz.PhysProps(dom), mz.PhysProps(dom)
+        plan = couette_plan(grid, walls, dt, avg_start=3, n_avg=5)
+        plan.launches = launches
+        dom.step(plan, 7, inst, avg)
+        results.append((device_logical(dom, 0), inst.fetch(), avg.fetch()))
+        if launches == 2:
+            ref_avg = oracle_couette(orc, o, grid, walls, dt, seed, 7, 3)
+        dom.close()
+    (r1, i1, a1), (r2, i2, a2) = results
+    assert np.array_equal(r1[1], r2[1]) and np.array_equal(r1[0], r2[0])
+    for k in ("np", "n", "v", "T"):
+        assert np.array_equal(i1[k], i2[k]) and np.array_equal(a1[k], a2[k]), k
+    assert_close_rows(a2["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T, two launches")
