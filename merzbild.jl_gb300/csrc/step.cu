@@ -317,9 +317,14 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
     cell_body<G, 0>(d, a, cell_hist);
 }
 
-__global__ void __launch_bounds__(256, 2) k_cell_gather(DomainView d, StepArgs a)
+// One cell per warp: the gather's random reads fetch whole 128-byte lines,
+// and a line's other records (neighbouring particles of the old order) are
+// gathered into nearby cells soon after; with one cell in flight per warp the
+// lines in flight fit in L2 and are reused there (four cells per warp keep
+// twice the L2 in flight and miss).
+__global__ void __launch_bounds__(256, 3) k_cell_gather(DomainView d, StepArgs a)
 {
-    cell_body<8, 1>(d, a, nullptr);
+    cell_body<32, 1>(d, a, nullptr);
 }
 
 template <int G>
@@ -605,7 +610,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     };
     const int blocks_full = resident(kern_full, CELL_SMEM, 32 / G);
     const int blocks_phys = plan->dims == 1 ? resident(kern_phys, CELL_SMEM, 32 / G) : 0;
-    const int blocks_gather = plan->dims == 1 ? resident(k_cell_gather, 0, 4) : 0;
+    const int blocks_gather = plan->dims == 1 ? resident(k_cell_gather, 0, 1) : 0;
 
     auto cell_launch = [&](int gather, int props, int physics, int advance = 1) {
         StepArgs b = a;
