@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--only-extra", default=None, choices=["batched_0d", "varweight", "serving"],
                    help="run one of the extra measurements alone and print its result")
     p.add_argument("--seed", type=int, default=1234)
+    p.add_argument("--launches", type=int, default=0, choices=[0, 1, 2],
+                   help="1 or 2 kernel launches per step instead of the autotuner's choice (no autotuning; for "
+                        "profiling runs)")
     return p.parse_args()
 
 
@@ -185,7 +188,7 @@ def setup_device(mz, ctx, args, seed):
     return sp, inter, grid, Fnum, walls, dt, dom, smax
 
 
-def make_plan(mz, grid, walls, dt, step0, n_avg, graph=True):
+def make_plan(mz, grid, walls, dt, step0, n_avg, graph=True, launches=0):
     plan = mz._lib.StepPlan()
     plan.dims = 1
     plan.collide = 1
@@ -197,6 +200,7 @@ def make_plan(mz, grid, walls, dt, step0, n_avg, graph=True):
     plan.dw_tol = 1e-16
     plan.step0 = step0
     plan.use_graph = 1 if graph else 0
+    plan.launches = launches
     plan.grid = grid.c_struct()
     plan.walls = walls.c_struct()
     return plan
@@ -469,15 +473,20 @@ def run_gpu(args):
     # the autotuner times each mapping (lanes per cell x one or two launches
     # per step) on real steps, two rounds of 8 steps each before the warm-up,
     # then W untimed warm-up steps
-    tune_steps = 12 * 8
-    mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=8)
-    dom.step(make_plan(mz, grid, walls, dt, tune_steps, K), W, inst, avg)
+    if args.launches:
+        # a fixed mapping: the default lanes per cell and the launches asked for
+        tune_steps = 0
+        mapping = (8 if args.cells >= 4096 else (16 if args.cells >= 1024 else 32), 1 if args.launches == 2 else 0)
+    else:
+        tune_steps = 12 * 8
+        mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=8)
+    dom.step(make_plan(mz, grid, walls, dt, tune_steps, K, launches=args.launches), W, inst, avg)
     ctx.synchronize()
     log(f"warm-up done (mapping: {mapping[0]} lanes per cell, {2 if mapping[1] == 1 else 1} launches per step)")
     mz.clear_props(avg)
     dom.counters(reset=True)
     step0 = tune_steps + W
-    plan = make_plan(mz, grid, walls, dt, step0, K)
+    plan = make_plan(mz, grid, walls, dt, step0, K, launches=args.launches)
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = ctx.launch_count()
@@ -502,7 +511,8 @@ def run_gpu(args):
     log("kernel timing pass")
     ctx.set_kernel_timing(True)
     kt_steps = max(3, min(K, 6))
-    dom.step(make_plan(mz, grid, walls, dt, step0 + K, kt_steps, graph=False), kt_steps, inst, avg)
+    dom.step(make_plan(mz, grid, walls, dt, step0 + K, kt_steps, graph=False, launches=args.launches), kt_steps,
+             inst, avg)
     timings = ctx.kernel_timings()
     ctx.set_kernel_timing(False)
     tot = sum(v[0] for v in timings.values())
@@ -573,7 +583,7 @@ def run_gpu(args):
         dom2.upload(0, w, v, x, cell)
         d2h = 0
         for k in range(K):
-            dom2.step(make_plan(mz, grid, walls, dt, 1000 + k, 1), 1, inst, None)
+            dom2.step(make_plan(mz, grid, walls, dt, 1000 + k, 1, launches=args.launches), 1, inst, None)
             r = inst.fetch()
             d2h += r["np"].nbytes + r["n"].nbytes + r["v"].nbytes + r["T"].nbytes
         ctx.synchronize()

@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(256) k_wall_hits(DomainView d, StepArgs a)
 // each non-empty destination then reserves its run of the cell's segment
 // with one global atomic (consecutive addresses).  Other slots take a ticket
 // directly.  The order inside a segment is arbitrary; k_cell sorts it.
-constexpr int SCATTER_TILE = 2048, SCATTER_WINDOW = 2048;
+constexpr int SCATTER_TILE = 4096, SCATTER_WINDOW = 2048;
 
 // surface_props_scale! of the step's wall sums, then avg_props! into the
 // average from avg_start on (the convection of RNG step `step`)
