@@ -4,8 +4,9 @@
  * A plain C++ restatement of Merzbild.jl's per-step DSMC hot path (reference
  * v0.7.10, Julia; the reference itself cannot run in this environment because
  * no Julia toolchain exists).  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load this library, and only as the checker
- * or the timed CPU baseline.  The product library never links or calls it.
+ * CPU-baseline legs of bench.py may load this library, and only as the
+ * result the device is compared against or as the timed CPU baseline.  The
+ * product library never links or calls it.
  *
  * Every function follows one reference function (file:line in the reference
  * repository is given beside it).  Data layout mirrors the reference: AoS

@@ -3,7 +3,7 @@ seeded inputs, plus the reference's known-answer vectors run on the device.
 
 Tolerances: integer / index / permutation results are compared bit-exactly;
 floating-point particle state and moments within 1e-12 relative to the
-magnitude of the quantity (the spec replay tolerance)."""
+magnitude of the quantity (the replay tolerance of the collision routine)."""
 import numpy as np
 import pytest
 
