@@ -278,3 +278,57 @@ def test_two_launch_step_equals_fused(ctx, orc):
     for k in ("np", "n", "v", "T"):
         assert np.array_equal(i1[k], i2[k]) and np.array_equal(a1[k], a2[k]), k
     assert_close_rows(a2["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T, two launches")
+
+
+def test_two_species_couette_step_matches_reference_loop(ctx, orc):
+    """An Ar + He mixture between the Couette walls: the fused and the
+    two-launch 1-D step give the same particles, and both follow the
+    reference loop (ntc_equal_weight! for (Ar,Ar), (He,Ar), (He,He), then
+    convection and sorting of both species) run by the oracle on the same
+    streams."""
+    sp = species(["Ar", "He"])
+    inter = interactions(sp)
+    nx, L, T, seed, steps = 30, 5e-4, 273.0, 61, 4
+    grid = mz.Grid1DUniform(L, nx)
+    walls = mz.MaxwellWalls1D(sp, T, T, -500.0, 500.0, 1.0, 1.0)
+    ndens = (6e22, 4e22)
+    Fnum = [grid.dx * n / 60 for n in ndens]
+    dt = 0.2 / mz.mean_collision_frequency(inter, sp, 0, 1e23, T)
+    t = mz.VHS
+    o = orc.Oracle(nx, 2, [s.mass for s in sp])
+    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    smax = {}
+    for s in range(2):
+        o.pv_create(s, 4 * 60 * nx)
+        o.sample_grid_ndens(s, L, nx, ndens[s], T, Fnum[s], seed=seed, step=0)
+    for s1 in range(2):
+        for s2 in range(2):
+            smax[s1, s2] = mz.estimate_sigma_g_w_max(inter[s1][s2], sp[s1], sp[s2], T, T, max(Fnum[s1], Fnum[s2]))
+            o.cf_set_smax(s1, s2, smax[s1, s2])
+    for step in range(1, steps + 1):
+        for s2 in range(2):
+            for s1 in range(s2, 2):
+                o.ntc_cells(s1, s2, dt, grid.V, seed, step, equal_weight=True)
+        for s in range(2):
+            o.convect(s, L, nx, walls.as_flat_array(), dt, seed, step)
+            o.sort(s, L=L, nx=nx)
+    states = []
+    for launches in (1, 2):
+        dom = mz.Domain(ctx, nx, sp, 4 * 60 * nx, interactions=inter, seed=seed)
+        dom.set_cell_volumes(grid.V)
+        for s in range(2):
+            dom.sample_grid_ndens(s, grid, ndens[s], T, Fnum[s], step=0)
+        for (s1, s2), v in smax.items():
+            dom.set_sigma_g_w_max(s1, s2, v)
+        plan = couette_plan(grid, walls, dt, props=False)
+        plan.launches = launches
+        dom.step(plan, steps)
+        states.append([device_logical(dom, s) for s in range(2)])
+        dom.close()
+    for s in range(2):
+        (r1, c1), (r2, c2) = states[0][s], states[1][s]
+        assert np.array_equal(c1, c2) and np.array_equal(r1, r2), f"species {s}: fused and two-launch differ"
+        orows, oc = oracle_logical(o, s)
+        assert np.array_equal(oc, c1), f"species {s}: cells"
+        assert_close_rows(orows, r1, 1e-11, f"species {s} after {steps} steps")
