@@ -220,6 +220,20 @@ int mz_avg_props(mz_props* avg, const mz_props* inst, double n_avg_timesteps);
 int mz_clear_props(mz_props* p);
 /* copy to host; any pointer may be NULL */
 int mz_props_download(mz_props* p, double* lpa, double* np, double* n, double* v, double* T, double* moments);
+/* Read a property set back without stopping the device: np, n, v and T (the
+ * layouts of mz_props_download, back to back: 6 n_cells n_species doubles)
+ * are copied into one of two device snapshot buffers (slot 0 or 1) after the
+ * work already enqueued, and from there to host memory `dst` on a side
+ * stream while later work runs.  dst must stay valid until
+ * mz_props_snapshot_wait(p, slot) returns; page-locked memory (mz_host_alloc)
+ * makes the copy asynchronous.  A slot is refilled only after its previous
+ * host copy has finished.  No counterpart in the reference (its loops read
+ * phys_props on the host). */
+int mz_props_snapshot(mz_props* p, int32_t slot, double* dst);
+int mz_props_snapshot_wait(mz_props* p, int32_t slot);
+/* page-locked host memory for asynchronous copies */
+int mz_host_alloc(mz_ctx* ctx, size_t bytes, void** out);
+int mz_host_free(void* ptr);
 
 /* ---------------------------------------------------------------- convection */
 /* convect_particles! (convection_1D.jl:130-157) or, with

@@ -370,6 +370,7 @@ int mz_domain_create(mz_ctx* c, int64_t n_cells, int32_t n_species, const int64_
 
 static void free_props(mz_props* p)
 {
+    free_props_snapshot(p);
     cudaFree(p->np);
     cudaFree(p->n);
     cudaFree(p->v);

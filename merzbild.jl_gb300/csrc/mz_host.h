@@ -135,6 +135,7 @@ struct mz_props_s {
     double* T = nullptr;        // n_cells * ns
     double* moments = nullptr;  // n_moments * n_cells * ns
     double lpa[MZ_MAX_SPECIES] = {0};
+    void* snapshot = nullptr;   // asynchronous read-back state (snapshot.cu)
 };
 
 // ---------------------------------------------------------------- helpers
@@ -142,6 +143,7 @@ mz::DomainView make_view(mz_domain* d);
 void ensure_compact(mz_domain* d, int s);
 void swap_buffers(mz_domain* d, int s);
 void check_status(mz_domain* d);
+void free_props_snapshot(mz_props* p);
 // last-error text of a context, and the try / catch that turns MzError and
 // other exceptions into a status code at every C entry point
 void set_err(const mz_ctx* c, const std::string& m);

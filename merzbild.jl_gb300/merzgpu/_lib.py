@@ -138,6 +138,10 @@ _SIGS = {
     "mz_server_retired": (i32, [vp, i64, P(i64), P(i64)]),
     "mz_server_info": (i32, [vp, P(i64), P(i64)]),
     "mz_swpm": (i32, [vp, i32, d, d, i64, i64, u64]),
+    "mz_props_snapshot": (i32, [vp, i32, P(d)]),
+    "mz_props_snapshot_wait": (i32, [vp, i32]),
+    "mz_host_alloc": (i32, [vp, C.c_size_t, P(vp)]),
+    "mz_host_free": (i32, [vp]),
     "mz_nc_props_create": (i32, [C.c_char_p, P(C.c_char_p), i32, P(C.c_char_p), i32, i32, i32, i32, P(i32), i32,
                                  P(NcAttribute), i32, vp, P(vp)]),
     "mz_nc_surf_create": (i32, [C.c_char_p, P(C.c_char_p), i32, P(C.c_char_p), i32, i32, i32, P(NcAttribute), i32, vp,

@@ -507,6 +507,21 @@ class PhysProps:
         except Exception:
             pass
 
+    def snapshot(self, slot, dst: PinnedArray):
+        """mz_props_snapshot: start copying np, n, v, T into dst (6 x cells x
+        species doubles) without waiting; see snapshot_wait and unpack."""
+        self.domain._ck(lib().mz_props_snapshot(self.h, int(slot), ptr(dst.array)))
+
+    def snapshot_wait(self, slot):
+        self.domain._ck(lib().mz_props_snapshot_wait(self.h, int(slot)))
+
+    def unpack(self, flat):
+        """np, n, v, T of a snapshot in the shapes fetch() returns."""
+        nc, ns = self.domain.n_cells, self.domain.n_species
+        m = nc * ns
+        return dict(np=flat[:m].reshape(ns, nc).T, n=flat[m:2 * m].reshape(ns, nc).T,
+                    v=flat[2 * m:5 * m].reshape(ns, nc, 3).transpose(2, 1, 0), T=flat[5 * m:6 * m].reshape(ns, nc).T)
+
     def fetch(self):
         nc, ns, nm = self.domain.n_cells, self.domain.n_species, len(self.moment_powers)
         lpa = np.zeros(ns)
@@ -519,6 +534,32 @@ class PhysProps:
         # column-major (Julia) -> numpy [..., cell, species] views
         return dict(lpa=lpa, np=np_.reshape(ns, nc).T, n=n.reshape(ns, nc).T, v=v.reshape(ns, nc, 3).transpose(2, 1, 0),
                     T=T.reshape(ns, nc).T, moments=mom[: nm * nc * ns].reshape(ns, nc, nm).transpose(2, 1, 0))
+
+
+class PinnedArray:
+    """A numpy array in page-locked host memory (mz_host_alloc), for
+    asynchronous copies such as PhysProps.snapshot and fast uploads."""
+
+    def __init__(self, ctx: Context, shape, dtype=np.float64):
+        shape = (int(shape),) if np.ndim(shape) == 0 else tuple(int(k) for k in shape)
+        dt = np.dtype(dtype)
+        nbytes = max(1, int(np.prod(shape)) * dt.itemsize)
+        self.ptr = C.c_void_p()
+        check(lib().mz_host_alloc(ctx.h, nbytes, C.byref(self.ptr)), ctx.h)
+        raw = np.ctypeslib.as_array(C.cast(self.ptr, C.POINTER(C.c_uint8)), shape=(nbytes,))
+        self.array = raw[: int(np.prod(shape)) * dt.itemsize].view(dt).reshape(shape)
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            lib().mz_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class SurfProps:

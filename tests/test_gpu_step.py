@@ -332,3 +332,37 @@ def test_two_species_couette_step_matches_reference_loop(ctx, orc):
         orows, oc = oracle_logical(o, s)
         assert np.array_equal(oc, c1), f"species {s}: cells"
         assert_close_rows(orows, r1, 1e-11, f"species {s} after {steps} steps")
+
+
+def test_async_snapshots_equal_fetched_properties(ctx, orc):
+    """mz_props_snapshot: each step's read-back, taken without stopping the
+    device (two slots, each read two steps later), equals the properties a
+    synchronous fetch returns after the same step of an identical run."""
+    runs = []
+    for use_snapshot in (True, False):
+        sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc, nx=50, ppc=80, seed=29)
+        inst = mz.PhysProps(dom)
+        m = grid.n_cells
+        snaps = [mz.PinnedArray(ctx, 6 * m), mz.PinnedArray(ctx, 6 * m)]
+        got = []
+        for k in range(5):
+            dom.step(couette_plan(grid, walls, dt, step0=k), 1, inst)
+            if use_snapshot:
+                if k >= 2:
+                    inst.snapshot_wait(k % 2)
+                    got.append(inst.unpack(snaps[k % 2].array.copy()))
+                inst.snapshot(k % 2, snaps[k % 2])
+            else:
+                got.append(inst.fetch())
+        if use_snapshot:
+            for k in (3, 4):
+                inst.snapshot_wait(k % 2)
+                got.append(inst.unpack(snaps[k % 2].array.copy()))
+        runs.append(got)
+        for a in snaps:
+            a.close()
+        dom.close()
+    assert len(runs[0]) == len(runs[1]) == 5
+    for a, b in zip(*runs):
+        for key in ("np", "n", "v", "T"):
+            assert np.array_equal(a[key], b[key]), key
