@@ -33,7 +33,7 @@ export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, Dev
        sort_particles!, squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
        avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
        DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf,
-       swpm!, create_collision_factors_swpm_array!
+       swpm!, create_collision_factors_swpm_array!, snapshot!, snapshot_wait, unpack_snapshot!
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -310,6 +310,30 @@ function fetch!(phys_props, p::DeviceProps)
                 (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
                 p.ptr, lpa, phys_props.np, phys_props.n, phys_props.v, phys_props.T, mom), p.dp.ctx)
     phys_props.lpa .= lpa
+    phys_props
+end
+
+"""
+    snapshot!(p::DeviceProps, slot, dst::Vector{Float64})
+
+Start copying np, n, v, T (back to back, 6 n_cells n_species values) into
+`dst` without stopping the device (`mz_props_snapshot`); the copy overlaps the
+steps enqueued after it.  `dst` must stay alive until `snapshot_wait(p, slot)`;
+pin it with `Base.Libc`-allocated memory registered by the caller, or accept a
+synchronous copy for pageable memory.
+"""
+snapshot!(p::DeviceProps, slot, dst::Vector{Float64}) =
+    check(ccall((:mz_props_snapshot, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}), p.ptr, slot, dst), p.dp.ctx)
+snapshot_wait(p::DeviceProps, slot) =
+    check(ccall((:mz_props_snapshot_wait, libmz), Cint, (Ptr{Cvoid}, Int32), p.ptr, slot), p.dp.ctx)
+
+"""Copy a snapshot's values into a Merzbild `PhysProps` (np, n, v, T)."""
+function unpack_snapshot!(phys_props, flat::Vector{Float64})
+    m = length(phys_props.np)
+    copyto!(phys_props.np, 1, flat, 1, m)
+    copyto!(phys_props.n, 1, flat, m + 1, m)
+    copyto!(phys_props.v, 1, flat, 2m + 1, 3m)
+    copyto!(phys_props.T, 1, flat, 5m + 1, m)
     phys_props
 end
 
