@@ -33,7 +33,8 @@ export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, Dev
        sort_particles!, squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
        avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
        DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf,
-       swpm!, create_collision_factors_swpm_array!, snapshot!, snapshot_wait, unpack_snapshot!
+       swpm!, create_collision_factors_swpm_array!, snapshot!, snapshot_wait, unpack_snapshot!, pinned_vector,
+       free_pinned!
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -318,14 +319,23 @@ end
 
 Start copying np, n, v, T (back to back, 6 n_cells n_species values) into
 `dst` without stopping the device (`mz_props_snapshot`); the copy overlaps the
-steps enqueued after it.  `dst` must stay alive until `snapshot_wait(p, slot)`;
-pin it with `Base.Libc`-allocated memory registered by the caller, or accept a
-synchronous copy for pageable memory.
+steps enqueued after it.  `dst` must stay alive until `snapshot_wait(p, slot)`.
+With a `pinned_vector` the call returns at once; with ordinary (pageable)
+memory the CUDA runtime completes the copy before returning.
 """
 snapshot!(p::DeviceProps, slot, dst::Vector{Float64}) =
     check(ccall((:mz_props_snapshot, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}), p.ptr, slot, dst), p.dp.ctx)
 snapshot_wait(p::DeviceProps, slot) =
     check(ccall((:mz_props_snapshot_wait, libmz), Cint, (Ptr{Cvoid}, Int32), p.ptr, slot), p.dp.ctx)
+
+"""A page-locked `Vector{Float64}` of length n (`mz_host_alloc`); release it
+with `free_pinned!`."""
+function pinned_vector(ctx::DeviceContext, n::Integer)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mz_host_alloc, libmz), Cint, (Ptr{Cvoid}, Csize_t, Ref{Ptr{Cvoid}}), ctx.ptr, n * 8, r), ctx)
+    unsafe_wrap(Vector{Float64}, Ptr{Float64}(r[]), n; own=false)
+end
+free_pinned!(v::Vector{Float64}) = ccall((:mz_host_free, libmz), Cint, (Ptr{Cvoid},), pointer(v))
 
 """Copy a snapshot's values into a Merzbild `PhysProps` (np, n, v, T)."""
 function unpack_snapshot!(phys_props, flat::Vector{Float64})
