@@ -421,6 +421,12 @@ int mz_server_submit(mz_server* server, const mz_request* request, int64_t* id);
 /* admit what fits, advance every running request by one step, retire the
  * finished ones; counts after the step */
 int mz_server_step(mz_server* server, int64_t* n_running, int64_t* n_queued, int64_t* n_retired);
+/* The same for up to max_steps steps in one call: the call runs k steps, k =
+ * the fewest steps any running request still needs (at most max_steps), so
+ * no request steps past its end; queued requests are admitted at the start
+ * of the call.  *n_steps receives k.  Results are those of k single steps. */
+int mz_server_step_many(mz_server* server, int64_t max_steps, int64_t* n_steps, int64_t* n_running,
+                        int64_t* n_queued, int64_t* n_retired);
 /* state of a request and, once done, its final properties */
 int mz_server_result(mz_server* server, int64_t id, mz_request_result* out);
 /* ids of the requests the last mz_server_step retired (*n of them; up to

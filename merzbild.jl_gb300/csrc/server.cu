@@ -275,10 +275,12 @@ int mz_server_submit(mz_server* sv, const mz_request* r, int64_t* id)
     API_CATCH(sv->ctx)
 }
 
-int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t* n_retired)
+int mz_server_step_many(mz_server* sv, int64_t max_steps, int64_t* n_steps, int64_t* n_running, int64_t* n_queued,
+                        int64_t* n_retired)
 {
     API_TRY
-    MZ_REQUIRE(sv, "mz_server_step: NULL server");
+    MZ_REQUIRE(sv && max_steps >= 1, "mz_server_step_many: bad argument");
+    if (n_steps) *n_steps = 0;
     MZ_CK(cudaSetDevice(sv->ctx->device));
     mz_domain* d = sv->dom;
     admit(sv);
@@ -295,13 +297,22 @@ int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t
         plan.dw_tol = 1e-16;
         plan.step0 = (uint64_t)sv->step;
         plan.use_graph = 0;
+        // as many steps as every running request still needs, at most max_steps:
+        // no request steps past its end, and admissions wait for the next call
+        int64_t ksteps = max_steps;
+        for (int64_t k : sv->running) {
+            const ReqRec& q = sv->reqs.at(k);
+            ksteps = std::min<int64_t>(ksteps, q.r.n_steps - (sv->step - q.start_step));
+        }
+        ksteps = std::max<int64_t>(ksteps, 1);
         std::vector<int64_t> done;
-        launch_step(d, &plan, 1, sv->props, nullptr);
-        ++sv->step;
+        launch_step(d, &plan, ksteps, sv->props, nullptr);
+        sv->step += ksteps;
+        if (n_steps) *n_steps = ksteps;
         for (int64_t k : sv->running) {
             ReqRec& q = sv->reqs.at(k);
             q.res.steps_done = sv->step - q.start_step;
-            for (int s = 0; s < sv->ns; ++s) sv->particle_steps += q.r.count[s];
+            for (int s = 0; s < sv->ns; ++s) sv->particle_steps += q.r.count[s] * ksteps;
             if (q.res.steps_done >= q.r.n_steps) done.push_back(k);
         }
         if (!done.empty()) {
@@ -353,6 +364,11 @@ int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t
     if (n_retired) *n_retired = retired;
     check_status(d);
     API_CATCH(sv->ctx)
+}
+
+int mz_server_step(mz_server* sv, int64_t* n_running, int64_t* n_queued, int64_t* n_retired)
+{
+    return mz_server_step_many(sv, 1, nullptr, n_running, n_queued, n_retired);
 }
 
 int mz_server_result(mz_server* sv, int64_t id, mz_request_result* out)

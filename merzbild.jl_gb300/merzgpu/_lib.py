@@ -134,6 +134,7 @@ _SIGS = {
     "mz_server_destroy": (i32, [vp]),
     "mz_server_submit": (i32, [vp, P(Request), P(i64)]),
     "mz_server_step": (i32, [vp, P(i64), P(i64), P(i64)]),
+    "mz_server_step_many": (i32, [vp, i64, P(i64), P(i64), P(i64), P(i64)]),
     "mz_server_result": (i32, [vp, i64, P(RequestResult)]),
     "mz_server_retired": (i32, [vp, i64, P(i64), P(i64)]),
     "mz_server_info": (i32, [vp, P(i64), P(i64)]),

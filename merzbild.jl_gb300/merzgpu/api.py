@@ -652,9 +652,12 @@ class Server:
         self._ck(lib().mz_server_submit(self.h, C.byref(r), C.byref(rid)))
         return rid.value
 
-    def step(self):
-        run, que, ret = C.c_int64(), C.c_int64(), C.c_int64()
-        self._ck(lib().mz_server_step(self.h, C.byref(run), C.byref(que), C.byref(ret)))
+    def step(self, max_steps=1):
+        """mz_server_step_many: admit, then up to max_steps steps of every running
+        request (no request past its end); returns (running, queued, retired)."""
+        k, run, que, ret = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        self._ck(lib().mz_server_step_many(self.h, int(max_steps), C.byref(k), C.byref(run), C.byref(que),
+                                           C.byref(ret)))
         return run.value, que.value, ret.value
 
     def result(self, rid):
@@ -678,12 +681,13 @@ class Server:
         self._ck(lib().mz_server_info(self.h, C.byref(steps), C.byref(ps)))
         return dict(steps=steps.value, particle_steps=ps.value)
 
-    def serve(self, requests, clock=time.perf_counter):
+    def serve(self, requests, clock=time.perf_counter, max_steps=16):
         """Request loop: `requests` are (arrival_s, kwargs of submit) sorted by
         arrival.  Requests are submitted when their arrival time has passed
-        (relative to the start), the server steps while work remains, and the
-        latency of each request (completion - arrival) is recorded.  Returns
-        (latencies in s, ids, elapsed s)."""
+        (relative to the start), the server steps while work remains (up to
+        max_steps steps per call, fewer when a running request finishes
+        sooner), and the latency of each request (completion - arrival) is
+        recorded.  Returns (latencies in s, ids, elapsed s)."""
         t0 = clock()
         i, n = 0, len(requests)
         ids, arrival = [], {}
@@ -701,7 +705,7 @@ class Server:
                 # idle until the next arrival
                 time.sleep(max(0.0, min(requests[i][0] - now, 0.002)))
                 continue
-            _, _, retired = self.step()
+            _, _, retired = self.step(max_steps)
             if retired:
                 t = clock() - t0
                 for rid in self.retired():

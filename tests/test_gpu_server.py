@@ -45,8 +45,8 @@ def _fnum(counts):
     return 2.2e16 / max(1, sum(counts))
 
 
-def _run(server, reqs, stagger=False):
-    """Submit (all at once, or one every few steps) and step until done."""
+def _run(server, reqs, stagger=False, max_steps=1):
+    """Submit (all at once, or one every few calls) and step until done."""
     ids = {}
     pending = list(reqs)
     k = 0
@@ -54,7 +54,7 @@ def _run(server, reqs, stagger=False):
         if pending and (not stagger or k % 3 == 0):
             c, T, n, seed = pending.pop(0)
             ids[seed] = server.submit(c, T, _fnum(c), n, seed)
-        server.step()
+        server.step(max_steps)
         k += 1
         assert k < 10_000
     return {seed: server.result(i) for seed, i in ids.items()}
@@ -76,6 +76,23 @@ def test_results_alone_equal_results_in_the_mix(ctx):
             assert a[key] == m[key], (seed, key)
         assert a["v"] == m["v"], seed
     sv.close()
+
+
+def test_multi_step_calls_give_the_same_results(ctx):
+    """mz_server_step_many: up to 7 steps per call (never past a running
+    request's end; admissions between calls) gives every request the results
+    of single steps."""
+    sv = _server(ctx, max_requests=4, capacity=16_000)
+    single = _run(sv, REQUESTS, stagger=True)
+    sv.close()
+    sv = _server(ctx, max_requests=4, capacity=16_000)
+    many = _run(sv, REQUESTS, stagger=True, max_steps=7)
+    sv.close()
+    for seed, a in single.items():
+        m = many[seed]
+        assert m["state"] == mz._lib.MZ_REQ_DONE and a["steps_done"] == m["steps_done"]
+        for key in ("np", "n", "T", "v"):
+            assert a[key] == m[key], (seed, key)
 
 
 def test_served_request_matches_the_oracle(ctx, orc):
