@@ -105,7 +105,7 @@ struct mz_domain_s {
     mz_surf_props* step_surf_avg = nullptr;
     // fused step: RNG step index and last-block counter
     uint32_t* d_step = nullptr;
-    unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block}
+    unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block, next big cell, big last block}
     void* d_hitq = nullptr;          // fused step: wall-hit queue (int4 entries)
     int64_t hitq_cap = 0;
     // fused-step mapping chosen by mz_step_autotune (0: the default rules)

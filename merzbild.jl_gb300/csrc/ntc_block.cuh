@@ -16,6 +16,13 @@
 //     candidate the exact running maximum;
 //   * draws, screening, acceptance and scattering are those of ntc_cell, so
 //     the result equals the sequential loop (and ntc_cell) bit for bit.
+// A warp-wide FP64 instruction holds the SM's FP64 pipe for 16 clocks however
+// few of its lanes are active, and one block is the only FP64 user of its cell.
+// The two long FP64 sequences therefore run on compacted threads: the exact
+// sigma*g*w (pow, about 1 % of the candidates) and the scattering of the
+// accepted candidates (about a third) are listed in shared memory and done by
+// the first threads of the block, each resuming the candidate's own stream at
+// the draw it had reached.
 #pragma once
 
 #include <climits>
@@ -33,7 +40,14 @@ struct NtcBlockShared {
     long long wmax[NTC_BLOCK / 32];
     int32_t end;
     int32_t accepted;
+    int32_t n_exact;
     long long last_max;
+    // per candidate of the batch (indexed by its thread), for the compacted work
+    int32_t list[NTC_BLOCK];   // candidates needing the exact sigma*g*w, then the accepted ones
+    int32_t slot1[NTC_BLOCK], slot2[NTC_BLOCK];
+    uint32_t draws[NTC_BLOCK];  // draws taken from the candidate's stream before scattering
+    double g2[NTC_BLOCK];
+    double val[NTC_BLOCK];      // the pair's larger weight, then its exact sigma*g*w
 };
 
 __device__ __forceinline__ uint32_t ntc_hash(int32_t t) { return ((uint32_t)t * 0x9E3779B1u) >> (32 - 11); }
@@ -101,6 +115,7 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
         if (tid == 0) {
             sh.end = min(NTC_BLOCK, ncoll - j0);
             sh.accepted = 0;
+            sh.n_exact = 0;
         }
         __syncthreads();
         if (valid) {
@@ -143,12 +158,25 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
                 ls = lC + lw + ex * lg;
                 exact = !screen_b || fabsf(lw) >= LOG_RANGE || fabsf(lg) >= LOG_RANGE ||
                         ls > l_smax - SCREEN_MARGIN;
-                if (exact) {
-                    if (!have_g) g = sqrt(g2);
-                    have_g = true;
-                    sgw = I.vhs_factor * pow(g, vexp) * g * wmax;
-                }
             }
+            sh.g2[tid] = g2;
+            if (exact) {
+                sh.val[tid] = wmax;
+                sh.list[atomicAdd(&sh.n_exact, 1)] = tid;
+            }
+        }
+        __syncthreads();
+        // exact sigma*g*w on compacted threads (list order does not matter:
+        // each value depends on its own candidate only)
+        const int ne = sh.n_exact;
+        if (ne > 0) {
+            for (int q = tid; q < ne; q += NTC_BLOCK) {
+                const int t = sh.list[q];
+                const double gt = sqrt(sh.g2[t]);
+                sh.val[t] = I.vhs_factor * pow(gt, vexp) * gt * sh.val[t];
+            }
+            __syncthreads();
+            if (act && exact) sgw = sh.val[tid];
         }
         // block inclusive max-scan of the sigma*g*w bit patterns
         long long mk = max_key(sgw, act && exact);
@@ -183,24 +211,38 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
             }
         }
         if (acc) {
-            if (!have_g) g = sqrt(g2);
-            const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
-            const double cy = I.mu1 * a.vy + I.mu2 * b.vy;
-            const double cz = I.mu1 * a.vz + I.mu2 * b.vz;
-            double sphi, cphi;
-            sincos_2pi_u52(trig, st.u52(), sphi, cphi);
-            const double ct = fma(2.0, st.uniform(), -1.0);
-            const double sth = sqrt(1.0 - ct * ct);
-            const double nx = g * (sth * cphi), ny = g * (sth * sphi), nz = g * ct;
-            P1.wv[si] = PV{a.w, cx + I.mu2 * nx, cy + I.mu2 * ny, cz + I.mu2 * nz};
-            P2.wv[sk] = PV{b.w, cx - I.mu1 * nx, cy - I.mu1 * ny, cz - I.mu1 * nz};
+            sh.slot1[tid] = si;
+            sh.slot2[tid] = sk;
+            sh.draws[tid] = st.n;
+            sh.list[atomicAdd(&sh.accepted, 1)] = tid;
         }
-        const int na = __popc(__ballot_sync(0xFFFFFFFFu, acc));
-        if (lane == 0 && na) atomicAdd(&sh.accepted, na);
         __syncthreads();
-        R.perf += sh.accepted;
+        const int na = sh.accepted;
+        R.perf += na;
         smax = __longlong_as_double(sh.last_max);
+        // scatter_vhs! of the accepted candidates on compacted threads; the
+        // batch's candidates share no particle, so the order is free
+        for (int q = tid; q < na; q += NTC_BLOCK) {
+            const int t = sh.list[q];
+            Stream sc;
+            sc.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)(j0 + t));
+            sc.n = sh.draws[t];
+            const int32_t ti = sh.slot1[t], tk = sh.slot2[t];
+            const PV ta = P1.wv[ti], tb = P2.wv[tk];
+            const double gt = sqrt(sh.g2[t]);
+            const double cx = I.mu1 * ta.vx + I.mu2 * tb.vx;
+            const double cy = I.mu1 * ta.vy + I.mu2 * tb.vy;
+            const double cz = I.mu1 * ta.vz + I.mu2 * tb.vz;
+            double sphi, cphi;
+            sincos_2pi_u52(trig, sc.u52(), sphi, cphi);
+            const double ct = fma(2.0, sc.uniform(), -1.0);
+            const double sth = sqrt(1.0 - ct * ct);
+            const double nx = gt * (sth * cphi), ny = gt * (sth * sphi), nz = gt * ct;
+            P1.wv[ti] = PV{ta.w, cx + I.mu2 * nx, cy + I.mu2 * ny, cz + I.mu2 * nz};
+            P2.wv[tk] = PV{tb.w, cx - I.mu1 * nx, cy - I.mu1 * ny, cz - I.mu1 * nz};
+        }
         j0 += B;
+        // the next batch reads the scattered velocities and resets the counters
         __syncthreads();
     }
     R.eqw = R.perf;

@@ -8,9 +8,10 @@
 // request's result does not depend on which slot it gets or on what runs
 // beside it.  One server step admits queued requests while slots and the
 // particle budget allow (compacting storage when dead slots block an
-// admission), runs one fused 0-D step (ntc! for every species pair, then
-// compute_props!) for all running requests at once, and retires requests that
-// reached their step count, keeping their final properties.
+// admission), runs fused 0-D steps (ntc! for every species pair) for all
+// running requests at once, and retires requests that reached their step
+// count with compute_props! of their last step (the only properties a request
+// returns).
 #include "mz_host.h"
 
 #include <algorithm>
@@ -78,6 +79,129 @@ __global__ void k_release(DomainView d, const int32_t* cells, int n)
     }
 }
 
+// compute_props! (physical_props.jl) of the finishing requests only, spread
+// over many SMs: one FP64 pipe per SM would take ~0.6 ms for the two passes
+// over one 200,000-particle cell.  Each (cell, species) list is cut into fixed
+// chunks of LP_CHUNK particles; the chunk sums are combined in chunk order, so
+// a request's result depends on its own particles only.
+constexpr int LP_CHUNK = 2048;
+constexpr int LP_THREADS = 256;
+
+struct ListProps {
+    const int32_t* cells;  // cells of the finishing requests
+    int n_items;           // cells x species, item = i * n_species + s
+    int kmax;              // chunks of the longest list
+    double* part;          // [item][chunk][5]: n, sum w vx, sum w vy, sum w vz, sum w |v - u|^2
+    double* out;           // [item][6]: np, n, ux, uy, uz, T
+};
+
+// block sum of four values in a fixed order (warp butterflies, then warps in order)
+__device__ __forceinline__ void lp_block_sum(double (&x)[4], int nv, double* red)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int q = 0; q < nv; ++q)
+        for (int o = 16; o > 0; o >>= 1) x[q] += __shfl_xor_sync(0xFFFFFFFFu, x[q], o);
+    if (lane == 0)
+        for (int q = 0; q < nv; ++q) red[4 * wid + q] = x[q];
+    __syncthreads();
+    for (int q = 0; q < nv; ++q) {
+        double t = 0.0;
+        for (int w = 0; w < LP_THREADS / 32; ++w) t += red[4 * w + q];
+        x[q] = t;
+    }
+}
+
+__device__ __forceinline__ void lp_mean(const ListProps& a, int item, int nk, double& n, double& ux, double& uy,
+                                        double& uz)
+{
+    const double* pp = a.part + (size_t)item * a.kmax * 5;
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    n = 0.0;
+    for (int k = 0; k < nk; ++k) {
+        n += pp[5 * k];
+        tx += pp[5 * k + 1];
+        ty += pp[5 * k + 2];
+        tz += pp[5 * k + 3];
+    }
+    ux = uy = uz = 0.0;
+    if (n > 0.0) {
+        ux = tx / n;
+        uy = ty / n;
+        uz = tz / n;
+    }
+}
+
+// pass 1: weight and momentum sums of each chunk
+__global__ void __launch_bounds__(LP_THREADS) k_lp_moments(DomainView d, ListProps a)
+{
+    __shared__ double red[4 * (LP_THREADS / 32)];
+    const int item = (int)(blockIdx.x / a.kmax), chunk = (int)(blockIdx.x % a.kmax), ns = d.n_species;
+    const SpeciesView& S = d.sp[item % ns];
+    const Indexer p = S.ind[a.cells[item / ns]];
+    const int32_t tot = p.n1 + p.n2, lo = chunk * LP_CHUNK;
+    if (lo >= tot && lo > 0) return;  // block 0 also writes the sums of an empty list
+    const int32_t hi = min(tot, lo + LP_CHUNK);
+    double x[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int32_t j = lo + threadIdx.x; j < hi; j += LP_THREADS) {
+        const PV r = S.A.wv[map_slot(p, j)];
+        x[0] += r.w;
+        x[1] += r.vx * r.w;
+        x[2] += r.vy * r.w;
+        x[3] += r.vz * r.w;
+    }
+    lp_block_sum(x, 4, red);
+    if (threadIdx.x == 0) {
+        double* q = a.part + ((size_t)item * a.kmax + chunk) * 5;
+        for (int k = 0; k < 4; ++k) q[k] = x[k];
+    }
+}
+
+// pass 2: sum w |v - u|^2 of each chunk about the list's mean velocity
+__global__ void __launch_bounds__(LP_THREADS) k_lp_energy(DomainView d, ListProps a)
+{
+    __shared__ double red[4 * (LP_THREADS / 32)];
+    const int item = (int)(blockIdx.x / a.kmax), chunk = (int)(blockIdx.x % a.kmax), ns = d.n_species;
+    const SpeciesView& S = d.sp[item % ns];
+    const Indexer p = S.ind[a.cells[item / ns]];
+    const int32_t tot = p.n1 + p.n2, lo = chunk * LP_CHUNK;
+    if (lo >= tot && lo > 0) return;  // block 0 also writes the sums of an empty list
+    const int32_t hi = min(tot, lo + LP_CHUNK);
+    const int nk = min(a.kmax, max(1, (int)((tot + LP_CHUNK - 1) / LP_CHUNK)));
+    double n, ux, uy, uz;
+    lp_mean(a, item, nk, n, ux, uy, uz);
+    double x[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int32_t j = lo + threadIdx.x; j < hi; j += LP_THREADS) {
+        const PV r = S.A.wv[map_slot(p, j)];
+        const double dx = r.vx - ux, dy = r.vy - uy, dz = r.vz - uz;
+        x[0] = fma(r.w, (dx * dx + dy * dy) + dz * dz, x[0]);
+    }
+    lp_block_sum(x, 1, red);
+    if (threadIdx.x == 0) a.part[((size_t)item * a.kmax + chunk) * 5 + 4] = x[0];
+}
+
+// the list's properties from its chunk sums, one thread per list
+__global__ void k_lp_finish(DomainView d, ListProps a)
+{
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.n_items) return;
+    const int ns = d.n_species;
+    const SpeciesView& S = d.sp[item % ns];
+    const Indexer p = S.ind[a.cells[item / ns]];
+    const int32_t tot = p.n1 + p.n2;
+    const int nk = min(a.kmax, max(1, (int)((tot + LP_CHUNK - 1) / LP_CHUNK)));
+    double n, ux, uy, uz;
+    lp_mean(a, item, nk, n, ux, uy, uz);
+    double E = 0.0;
+    for (int k = 0; k < nk; ++k) E += a.part[((size_t)item * a.kmax + k) * 5 + 4];
+    double* o = a.out + (size_t)item * 6;
+    o[0] = (double)tot;
+    o[1] = n;
+    o[2] = ux;
+    o[3] = uy;
+    o[4] = uz;
+    o[5] = n > 0.0 ? (2.0 / 3.0) * (E * (0.5 * S.mass / (n * K_B))) : 0.0;
+}
+
 // estimate_sigma_g_w_max (collision_utils.jl:418-423)
 double sigma_g_w_max_estimate(const Interaction& I, double m1, double m2, double T1, double T2, double Fnum)
 {
@@ -91,7 +215,6 @@ double sigma_g_w_max_estimate(const Interaction& I, double m1, double m2, double
 struct mz_server_s {
     mz_ctx* ctx = nullptr;
     mz_domain* dom = nullptr;
-    mz_props* props = nullptr;
     int32_t ns = 0;
     int64_t slots = 0;
     double dt = 0.0;
@@ -105,6 +228,9 @@ struct mz_server_s {
     std::vector<int64_t> retired;   // ids retired by the last mz_server_step
     // device scratch for admissions / retirements
     int32_t* d_cells = nullptr;
+    double* d_part = nullptr;  // chunk sums of the finishing requests' props
+    int64_t part_cap = 0;      // doubles in d_part
+    double* d_lp = nullptr;    // their properties, 6 per (request, species)
     uint64_t* d_seed = nullptr;
     uint32_t* d_off = nullptr;
     double* d_V = nullptr;
@@ -225,12 +351,12 @@ int mz_server_create(mz_ctx* c, int32_t n_species, const double* mass, const mz_
     if (rc != MZ_OK) throw MzError(rc, "mz_server_create: domain");
     rc = mz_set_species(sv->dom, mass);
     if (rc == MZ_OK) rc = mz_set_interactions(sv->dom, inter);
-    if (rc == MZ_OK) rc = mz_props_create(sv->dom, 0, nullptr, 300.0, 0, &sv->props);
     if (rc != MZ_OK) throw MzError(rc, "mz_server_create: set-up");
     ensure_rng_arrays(sv->dom);
     sv->slot_req.assign(max_requests, 0);
     for (int64_t s = max_requests - 1; s >= 0; --s) sv->free_slots.push_back(s);
     MZ_CK(cudaMalloc(&sv->d_cells, max_requests * sizeof(int32_t)));
+    MZ_CK(cudaMalloc(&sv->d_lp, max_requests * n_species * 6 * sizeof(double)));
     MZ_CK(cudaMalloc(&sv->d_seed, max_requests * sizeof(uint64_t)));
     MZ_CK(cudaMalloc(&sv->d_off, max_requests * sizeof(uint32_t)));
     MZ_CK(cudaMalloc(&sv->d_V, max_requests * sizeof(double)));
@@ -246,11 +372,13 @@ int mz_server_destroy(mz_server* sv)
     cudaSetDevice(sv->ctx->device);
     cudaStreamSynchronize(sv->ctx->stream);
     cudaFree(sv->d_cells);
+    cudaFree(sv->d_part);
+    cudaFree(sv->d_lp);
     cudaFree(sv->d_seed);
     cudaFree(sv->d_off);
     cudaFree(sv->d_V);
     cudaFree(sv->d_smax);
-    if (sv->dom) mz_domain_destroy(sv->dom);  // frees its props too
+    if (sv->dom) mz_domain_destroy(sv->dom);
     delete sv;
     return MZ_OK;
 }
@@ -292,7 +420,7 @@ int mz_server_step_many(mz_server* sv, int64_t max_steps, int64_t* n_steps, int6
         plan.dims = 0;
         plan.collide = 1;
         plan.equal_weight = 1;
-        plan.props = 1;
+        plan.props = 0;  // compute_props! of the finishing requests runs after the steps
         plan.dt = sv->dt;
         plan.dw_tol = 1e-16;
         plan.step0 = (uint64_t)sv->step;
@@ -306,7 +434,7 @@ int mz_server_step_many(mz_server* sv, int64_t max_steps, int64_t* n_steps, int6
         }
         ksteps = std::max<int64_t>(ksteps, 1);
         std::vector<int64_t> done;
-        launch_step(d, &plan, ksteps, sv->props, nullptr);
+        launch_step(d, &plan, ksteps, nullptr, nullptr);
         sv->step += ksteps;
         if (n_steps) *n_steps = ksteps;
         for (int64_t k : sv->running) {
@@ -316,39 +444,58 @@ int mz_server_step_many(mz_server* sv, int64_t max_steps, int64_t* n_steps, int6
             if (q.res.steps_done >= q.r.n_steps) done.push_back(k);
         }
         if (!done.empty()) {
-            // final properties of the finished requests: props of their last step
-            const int64_t nc = d->n_cells, ns = sv->ns;
-            std::vector<double> np(nc * ns), n(nc * ns), v(3 * nc * ns), T(nc * ns);
-            MZ_CK(cudaMemcpyAsync(np.data(), sv->props->np, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
-                                  sv->ctx->stream));
-            MZ_CK(cudaMemcpyAsync(n.data(), sv->props->n, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
-                                  sv->ctx->stream));
-            MZ_CK(cudaMemcpyAsync(v.data(), sv->props->v, 3 * nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
-                                  sv->ctx->stream));
-            MZ_CK(cudaMemcpyAsync(T.data(), sv->props->T, nc * ns * sizeof(double), cudaMemcpyDeviceToHost,
+            // final properties of the finished requests: compute_props! of
+            // their last step, for their cells only
+            const int ns = sv->ns;
+            std::vector<int32_t> cells;
+            int64_t kmax = 1;
+            for (int64_t k : done) {
+                const ReqRec& q = sv->reqs.at(k);
+                cells.push_back((int32_t)q.slot);
+                for (int s = 0; s < ns; ++s) kmax = std::max<int64_t>(kmax, div_up(q.r.count[s], LP_CHUNK));
+            }
+            const int n_items = (int)cells.size() * ns;
+            if ((int64_t)n_items * kmax * 5 > sv->part_cap) {
+                cudaFree(sv->d_part);
+                sv->d_part = nullptr;
+                sv->part_cap = 0;
+                const int64_t cap = std::max<int64_t>((int64_t)n_items * kmax * 5, 1 << 16);
+                MZ_CK(cudaMalloc(&sv->d_part, cap * sizeof(double)));
+                sv->part_cap = cap;
+            }
+            MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), cells.size() * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, sv->ctx->stream));
+            ListProps lp{sv->d_cells, n_items, (int)kmax, sv->d_part, sv->d_lp};
+            DomainView vp = make_view(d);
+            MZ_REQUIRE((int64_t)n_items * kmax < INT32_MAX, "mz_server_step: too many particles finishing at once");
+            const int lg = (int)(n_items * kmax);  // one block per (request, species, chunk)
+            MZ_LAUNCH(sv->ctx, "server_props_moments", k_lp_moments, lg, LP_THREADS, 0, vp, lp);
+            MZ_LAUNCH(sv->ctx, "server_props_energy", k_lp_energy, lg, LP_THREADS, 0, vp, lp);
+            MZ_LAUNCH(sv->ctx, "server_props_finish", k_lp_finish, (int)div_up(n_items, 128), 128, 0, vp, lp);
+            std::vector<double> o((size_t)n_items * 6);
+            MZ_CK(cudaMemcpyAsync(o.data(), sv->d_lp, o.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                   sv->ctx->stream));
             MZ_CK(cudaStreamSynchronize(sv->ctx->stream));
-            std::vector<int32_t> cells;
+            int i = 0;
             for (int64_t k : done) {
                 ReqRec& q = sv->reqs.at(k);
                 const int64_t c = q.slot;
                 for (int s = 0; s < ns; ++s) {
-                    q.res.np[s] = (int64_t)np[c + nc * s];
-                    q.res.n[s] = n[c + nc * s];
-                    for (int a = 0; a < 3; ++a) q.res.v[s][a] = v[a + 3 * (c + nc * s)];
-                    q.res.T[s] = T[c + nc * s];
+                    const double* r = o.data() + ((size_t)i * ns + s) * 6;
+                    q.res.np[s] = (int64_t)r[0];
+                    q.res.n[s] = r[1];
+                    for (int a = 0; a < 3; ++a) q.res.v[s][a] = r[2 + a];
+                    q.res.T[s] = r[5];
                 }
+                ++i;
                 q.res.steps_done = q.r.n_steps;
                 q.state = MZ_REQ_DONE;
                 sv->retired.push_back(k);
-                cells.push_back((int32_t)c);
                 sv->slot_req[c] = 0;
                 sv->free_slots.push_back(c);
                 for (int s = 0; s < ns; ++s) d->sp[s].n_total -= q.r.count[s];
                 ++retired;
             }
-            MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), cells.size() * sizeof(int32_t),
-                                  cudaMemcpyHostToDevice, sv->ctx->stream));
             DomainView vv = make_view(d);
             MZ_LAUNCH(sv->ctx, "server_release", k_release, (int)div_up((int64_t)cells.size() * 32, 256), 256, 0, vv,
                       sv->d_cells, (int)cells.size());

@@ -52,6 +52,8 @@ struct StepArgs {
     int4* hitq;           // particles that reach a wall: {slot, cell, position in cell, species}
     unsigned int* hit_n;  // entries in hitq
     unsigned int* hit_done;  // last-block counter of k_wall_hits
+    unsigned int* big_next;  // next cell k_ntc_big examines
+    unsigned int* big_done;  // last-block counter of k_ntc_big
     unsigned int hitq_cap;
     int32_t big_cell;     // cells with at least this many particles collide in k_ntc_big
     double* surf;         // wall sums of this step [species][2][11], or nullptr
@@ -336,18 +338,32 @@ __global__ void __launch_bounds__(256, 2) k_cell_physics(DomainView d, StepArgs 
 
 // ntc_equal_weight! and the 0-D compute_props! of the cells with at least
 // a.big_cell particles, one block per cell (ntc_cell_block, props_cell_block);
-// k_cell skips these cells' collisions and props.
-__global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
+// k_cell skips these cells' collisions and props.  Blocks take the next large
+// cell from a counter when they finish one, so a block never holds several
+// large cells while others idle (the last block resets the counter).
+__global__ void __launch_bounds__(NTC_BLOCK, 2) k_ntc_big(DomainView d, StepArgs a)
 {
     __shared__ NtcBlockShared sh;
     __shared__ double red[4 * (NTC_BLOCK / 32)];
+    __shared__ int next_cell;
     const uint32_t step = *a.step_ptr;
     const int ns = d.n_species;
     unsigned long long cand = 0, accd = 0;
-    for (int c = blockIdx.x; c < d.n_cells; c += gridDim.x) {
-        int32_t tot = 0;
-        for (int s = 0; s < ns; ++s) tot += d.sp[s].ind[c].n1;
-        if (tot < a.big_cell) continue;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            // skip small cells here, without block barriers
+            int c = (int)atomicAdd(a.big_next, 1u);
+            for (; c < d.n_cells; c = (int)atomicAdd(a.big_next, 1u)) {
+                int32_t tot = 0;
+                for (int s = 0; s < ns; ++s) tot += d.sp[s].ind[c].n1;
+                if (tot >= a.big_cell) break;
+            }
+            next_cell = c;
+        }
+        __syncthreads();
+        const int c = next_cell;
+        __syncthreads();
+        if (c >= d.n_cells) break;
         const uint64_t seed = cell_seed(d, c);
         const uint32_t rid = cell_rid(d, c), stp = cell_step(d, c, step);
         const double V = d.cell_V[c];
@@ -388,9 +404,17 @@ __global__ void __launch_bounds__(NTC_BLOCK) k_ntc_big(DomainView d, StepArgs a)
             }
         }
     }
-    if (threadIdx.x == 0 && (cand | accd)) {
-        atomicAdd(&d.counters->candidates, cand);
-        atomicAdd(&d.counters->accepted, accd);
+    if (threadIdx.x == 0) {
+        if (cand | accd) {
+            atomicAdd(&d.counters->candidates, cand);
+            atomicAdd(&d.counters->accepted, accd);
+        }
+        __threadfence();
+        if (atomicAdd(a.big_done, 1u) == gridDim.x - 1) {
+            *a.big_next = 0;
+            *a.big_done = 0;
+            __threadfence();
+        }
     }
 }
 
@@ -535,8 +559,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         if (plan->dims == 1 || d->sp[s].group2) launch_compact(d, s);
     if (!d->d_step) {
         MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
-        MZ_CK(cudaMalloc(&d->d_done, 4 * sizeof(unsigned int)));
-        MZ_CK(cudaMemsetAsync(d->d_done, 0, 4 * sizeof(unsigned int), c->stream));
+        MZ_CK(cudaMalloc(&d->d_done, 8 * sizeof(unsigned int)));
+        MZ_CK(cudaMemsetAsync(d->d_done, 0, 8 * sizeof(unsigned int), c->stream));
     }
     const uint32_t first = (uint32_t)(plan->step0 + 1);
     MZ_CK(cudaMemcpyAsync(d->d_step, &first, sizeof first, cudaMemcpyHostToDevice, c->stream));
@@ -580,6 +604,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.next = d->d_done + 1;
     a.hit_n = d->d_done + 2;
     a.hit_done = d->d_done + 3;
+    a.big_next = d->d_done + 4;
+    a.big_done = d->d_done + 5;
     if (plan->dims == 1) {
         // wall-hit queue: a fraction of the particles; overflow is handled inline
         int64_t n_all = 0;
