@@ -193,6 +193,9 @@ int mz_ctx_create(int device, mz_ctx** out)
     c->device = device;
     MZ_CK(cudaSetDevice(device));
     MZ_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    MZ_CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    MZ_CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    MZ_CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     MZ_CK(cudaEventCreate(&c->t0));
     MZ_CK(cudaEventCreate(&c->t1));
     MZ_CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
@@ -230,6 +233,12 @@ int mz_ctx_destroy(mz_ctx* c)
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->flush_buf) cudaFree(c->flush_buf);
     if (c->d_trig) cudaFree(c->d_trig);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     cudaStreamDestroy(c->stream);
     delete c;
     return MZ_OK;

@@ -39,6 +39,8 @@ struct KernelTiming {
 struct mz_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // a second stream for launches that overlap the main one
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string last_error;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     void* flush_buf = nullptr;

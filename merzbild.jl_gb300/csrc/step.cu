@@ -54,6 +54,7 @@ struct StepArgs {
     unsigned int* hit_done;  // last-block counter of k_wall_hits
     unsigned int* big_next;  // next cell k_ntc_big examines
     unsigned int* big_done;  // last-block counter of k_ntc_big
+    unsigned int join_blocks;  // k_cell and k_ntc_big overlap: their blocks together on `done` (0 = not)
     unsigned int hitq_cap;
     int32_t big_cell;     // cells with at least this many particles collide in k_ntc_big
     double* surf;         // wall sums of this step [species][2][11], or nullptr
@@ -302,9 +303,10 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned prev = atomicAdd(a.done, 1u);
-        if (prev == gridDim.x - 1) {
+        if (prev == (a.join_blocks ? a.join_blocks : gridDim.x) - 1) {
             *a.done = 0;
             *a.next = 0;
+            if (a.join_blocks) *a.big_next = 0;
             if (a.advance) *a.step_ptr = step + 1;
             __threadfence();
         }
@@ -410,7 +412,17 @@ __global__ void __launch_bounds__(NTC_BLOCK, 2) k_ntc_big(DomainView d, StepArgs
             atomicAdd(&d.counters->accepted, accd);
         }
         __threadfence();
-        if (atomicAdd(a.big_done, 1u) == gridDim.x - 1) {
+        if (a.join_blocks) {
+            // overlapping k_cell: the last block of either launch resets both
+            // cell counters and advances the RNG step
+            if (atomicAdd(a.done, 1u) == a.join_blocks - 1) {
+                *a.done = 0;
+                *a.next = 0;
+                *a.big_next = 0;
+                if (a.advance) *a.step_ptr = step + 1;
+                __threadfence();
+            }
+        } else if (atomicAdd(a.big_done, 1u) == gridDim.x - 1) {
             *a.big_next = 0;
             *a.big_done = 0;
             __threadfence();
@@ -648,8 +660,29 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // distinct names: the full step (gather + props + physics) is the one
         // the roofline is quoted on
         const char* name = !gather ? "step_cell_inplace" : (physics ? "step_cell" : "step_cell_final");
-        if ((physics || props) && b.big_cell < INT_MAX)
+        // 0-D: the large cells' blocks (k_ntc_big) and the warp-per-cell
+        // launch work on disjoint cells and run side by side (fork / join
+        // through events, also inside a graph capture); the last block of
+        // the two advances the step
+        const bool big_launch = (physics || props) && b.big_cell < INT_MAX;
+        const bool overlap = big_launch && a.dims == 0;
+        if (overlap) {
+            b.join_blocks = (unsigned)(c->num_sms * 2 + blocks_full);
+            MZ_CK(cudaEventRecord(c->ev_fork, c->stream));
+            MZ_CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+            {
+                struct OnSide {  // MZ_LAUNCH targets c->stream: the side stream for this launch
+                    mz_ctx* c;
+                    cudaStream_t main;
+                    ~OnSide() { c->stream = main; }
+                } on_side{c, c->stream};
+                c->stream = c->side;
+                MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
+            }
+            MZ_CK(cudaEventRecord(c->ev_join, c->side));
+        } else if (big_launch) {
             MZ_LAUNCH(c, "step_ntc_big", k_ntc_big, c->num_sms * 2, NTC_BLOCK, 0, v, b);
+        }
         if (physics && b.surf)
             MZ_CK(cudaMemsetAsync(b.surf, 0, (size_t)d->ns * 2 * SURF_Q * sizeof(double), c->stream));
         // 1-D launches that only sort + gather + props, or only collide and
@@ -660,6 +693,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             MZ_LAUNCH(c, name, kern_phys, blocks_phys, 256, CELL_SMEM, v, b);
         else
             MZ_LAUNCH(c, name, kern_full, blocks_full, 256, CELL_SMEM, v, b);
+        if (overlap) MZ_CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         if (physics && a.dims == 1) MZ_LAUNCH(c, "step_wall_hits", k_wall_hits, c->num_sms * 2, 256, 0, v, b);
         if (physics && b.surf) MZ_LAUNCH(c, "step_surf", k_surf_finish, 1, 128, 0, b, d->ns);
     };

@@ -120,6 +120,10 @@ def test_served_request_matches_the_oracle(ctx, orc):
         assert res["np"][s] == ref["np"][s, 0]
         assert abs(res["n"][s] - ref["n"][s, 0]) <= 1e-12 * ref["n"][s, 0]
         assert abs(res["T"][s] - ref["T"][s, 0]) <= 1e-11 * ref["T"][s, 0]
+        # mean velocities lie near zero: absolute bound, far below the
+        # thermal speed (hundreds of m/s); the He list spans two props chunks
+        for a in range(3):
+            assert abs(res["v"][s][a] - ref["v"][s, 0, a]) <= 1e-8, (s, a, res["v"][s][a], ref["v"][s, 0, a])
 
 
 def test_poisson_request_loop_completes_every_request(ctx):
