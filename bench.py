@@ -46,8 +46,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-extra", action="store_true",
-                   help="skip the batched 0-D, variable-weight Couette and serving measurements")
-    p.add_argument("--only-extra", default=None, choices=["batched_0d", "varweight", "serving"],
+                   help="skip the batched 0-D, variable-weight Couette, serving and largest-request measurements")
+    p.add_argument("--only-extra", default=None, choices=["batched_0d", "varweight", "serving", "largest_request"],
                    help="run one of the extra measurements alone and print its result")
     p.add_argument("--seed", type=int, default=1234)
     p.add_argument("--launches", type=int, default=0, choices=[0, 1, 2],
@@ -381,6 +381,38 @@ def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
             "batched_over_plain": (info["particle_steps"] / elapsed) / (ps / plain_s)}
 
 
+def largest_request(mz, ctx, seed, steps=20, warmup=3):
+    """The step of the serving mix's largest request alone: one 0-D Ar cell of
+    200,000 particles at 3000 K (Fnum = 2.2e16 / N, V = 1, dt = 2.5e-3),
+    collided block-per-cell (k_ntc_big) without per-step props, as the server
+    runs it.  Its candidate loop is sequential in batches, so this step time
+    is the floor of a serving step while the request runs."""
+    import numpy as np
+
+    sp = [mz.Species("Ar", mz.AR_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    n = 200_000
+    Fnum = 2.2e16 / n
+    dom = mz.Domain(ctx, 1, sp, n + 1024, interactions=inter, seed=seed)
+    dom.sample_cells(0, np.array([n], dtype=np.int64), [3000.0, 3000.0, 3000.0], Fnum, step=0)
+    dom.set_sigma_g_w_max(0, 0, mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], 3000.0, 3000.0, Fnum))
+    p = mz._lib.StepPlan()
+    p.dims, p.collide, p.equal_weight, p.props, p.dt, p.step0, p.use_graph = 0, 1, 1, 0, 2.5e-3, 0, 0
+    p.big_cell = 2048
+    dom.step(p, warmup)
+    dom.counters(reset=True)
+    ctx.synchronize()
+    ctx.timer_start()
+    p.step0 = warmup
+    dom.step(p, steps)
+    ms = ctx.timer_stop()
+    cnt = dom.counters(reset=True)
+    dom.close()
+    return {"workload": "one 0-D Ar cell, 200,000 particles, 3000 K, dt 2.5e-3, block-per-cell NTC, no per-step props",
+            "steps": steps, "ms_per_step": ms / steps, "value": n * steps / (ms / 1e3), "unit": "particle-steps/s",
+            "candidates_per_step": cnt["candidates"] / steps, "accepted_per_step": cnt["accepted"] / steps}
+
+
 def cpu_oracle_run(args, steps, time_budget=None, nthreads=None, warmup=0):
     """The oracle (C++ restatement of the reference path) on the host cores:
     the same workload, `warmup` untimed steps, then `steps` timed steps (or
@@ -463,7 +495,8 @@ def run_gpu(args):
     ctx = mz.Context(local)
     seed = args.seed + 7919 * rank  # independent replicas
     if args.only_extra:
-        fn = {"batched_0d": batched_0d, "varweight": varweight_couette, "serving": serving}[args.only_extra]
+        fn = {"batched_0d": batched_0d, "varweight": varweight_couette, "serving": serving,
+              "largest_request": largest_request}[args.only_extra]
         print(json.dumps({args.only_extra: fn(mz, ctx, seed)}), flush=True)
         ctx.close()
         return
@@ -616,7 +649,7 @@ def run_gpu(args):
         for a in (hw, hv, hx, hc, *snaps):
             a.close()
 
-    extra_0d = extra_srv = extra_vw = None
+    extra_0d = extra_srv = extra_vw = extra_big = None
     log(f"e2e: {e2e}")
     if not args.no_extra and rank == 0:
         extra_0d = batched_0d(mz, ctx, seed)
@@ -625,6 +658,8 @@ def run_gpu(args):
         log(f"variable-weight Couette: {extra_vw}")
         extra_srv = serving(mz, ctx, seed)
         log(f"serving: {extra_srv}")
+        extra_big = largest_request(mz, ctx, seed)
+        log(f"largest request: {extra_big}")
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
@@ -642,7 +677,8 @@ def run_gpu(args):
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-               "plain": plain, "batched_0d": extra_0d, "varweight_couette": extra_vw, "serving": extra_srv}
+               "plain": plain, "batched_0d": extra_0d, "varweight_couette": extra_vw, "serving": extra_srv,
+               "largest_request": extra_big}
         print(json.dumps(out), flush=True)
     ctx.close()
 
