@@ -78,6 +78,18 @@ __device__ __forceinline__ int32_t ntc_table_first(const NtcBlockShared& sh, int
 // Equal-weight candidate loop of one cell by the whole block (all threads call
 // it with identical arguments).  Returns the new running maximum and the
 // number of accepted collisions (valid in every thread).
+//
+// A batch's index draws and conflict detection depend only on where the batch
+// starts, so they run one batch ahead: while the block loads, screens, tests
+// and scatters batch b, it also draws the candidates of batch b+1 (which
+// starts where b ends), fills the conflict table with them and finds their
+// first conflict, in the same barrier-separated steps.  A batch then costs
+// five block barriers, and the Philox work overlaps the particle loads.
+//   step 1: b's loads, g^2, screening, exact list  | b+1's draws, table clear
+//   step 2: b's exact sigma*g*w (compacted)        | b+1's table inserts
+//   step 3: b's per-warp max-scan                  | b+1's first conflict
+//   step 4: b's scan across warps, acceptance, accepted list
+//   step 5: b's scattering (compacted); b+1's length is final
 __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const Interaction& I, bool single,
                                                     int32_t ncoll, double smax, const Cols& P1, const Cols& P2,
                                                     const Indexer& p1, const Indexer& p2, const double2* trig,
@@ -94,12 +106,17 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
     const int32_t tagk = single ? 0 : (int32_t)0x40000000;  // species 2 particles get their own keys
     NtcResult R;
     R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
-    for (int32_t j0 = 0; j0 < ncoll;) {
-        const int32_t j = j0 + tid;
+    R.smax = smax;
+    if (ncoll <= 0) return R;
+
+    // candidate jn + tid of the batch starting at jn: its index draws, and
+    // (whole block) the cleared conflict table and the batch's maximum length
+    auto draw = [&](int32_t jn, Stream& st, int32_t& i, int32_t& k) -> bool {
+        const int32_t j = jn + tid;
         const bool valid = j < ncoll;
-        Stream st;
         st.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)j);
-        int32_t i = -1, k = -1;
+        i = -1;
+        k = -1;
         if (valid) {
             i = floor_u52_times(st.u52(), nl1);
             k = floor_u52_times(st.u52(), nl2);
@@ -112,37 +129,53 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
             sh.key[q] = -1;
             sh.first[q] = INT_MAX;
         }
-        if (tid == 0) {
-            sh.end = min(NTC_BLOCK, ncoll - j0);
-            sh.accepted = 0;
-            sh.n_exact = 0;
-        }
-        __syncthreads();
+        if (tid == 0) sh.end = max(0, min(NTC_BLOCK, ncoll - jn));
+        return valid;
+    };
+    auto insert = [&](bool valid, int32_t i, int32_t k) {
         if (valid) {
             ntc_table_insert(sh, i, tid);
             ntc_table_insert(sh, k | tagk, tid);
         }
-        __syncthreads();
+    };
+    // the batch ends before the first candidate that touches a particle of an
+    // earlier candidate in the batch
+    auto first_conflict = [&](bool valid, int32_t i, int32_t k) {
         const bool conflict = valid && (ntc_table_first(sh, i) < tid || ntc_table_first(sh, k | tagk) < tid);
         const int cmin = __reduce_min_sync(0xFFFFFFFFu, conflict ? tid : INT_MAX);
         if (lane == 0 && cmin != INT_MAX) atomicMin(&sh.end, cmin);
-        __syncthreads();
-        const int B = sh.end;
-        const bool act = tid < B;
+    };
 
+    // batch 0's draws and length
+    Stream st;
+    int32_t i, k;
+    if (tid == 0) sh.n_exact = 0;
+    {
+        const bool valid = draw(0, st, i, k);
+        __syncthreads();
+        insert(valid, i, k);
+        __syncthreads();
+        first_conflict(valid, i, k);
+        __syncthreads();
+    }
+    int B = sh.end;
+    __syncthreads();  // every thread has read sh.end before step 1 rewrites it
+    for (int32_t j0 = 0; j0 < ncoll;) {  // j0 and B are the same in every thread
+        const int32_t jn = j0 + B;
+        const bool act = tid < B;
+        // ---- step 1
+        if (tid == 0) sh.accepted = 0;
         const float l_smax = log2_pos(smax);
         const bool screen_b = screen && fabsf(l_smax) < 2.0f * LOG_RANGE;
         int32_t si = 0, sk = 0;
-        PV a, b;
-        a.w = b.w = 0.0;
         double g2 = 0.0, g = 0.0, sgw = -1.0, wmax = 0.0;
         bool has = false, exact = false, have_g = false;
         float ls = 0.0f;
         if (act) {
             si = map_slot(p1, i);
             sk = map_slot(p2, k);
-            a = P1.wv[si];
-            b = P2.wv[sk];
+            const PV a = P1.wv[si];
+            const PV b = P2.wv[sk];
             const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
             g2 = (gx * gx + gy * gy) + gz * gz;
             wmax = dmax_pos(a.w, b.w);
@@ -165,20 +198,22 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
                 sh.list[atomicAdd(&sh.n_exact, 1)] = tid;
             }
         }
+        Stream sn;
+        int32_t ni, nk;
+        const bool nvalid = draw(jn, sn, ni, nk);
         __syncthreads();
-        // exact sigma*g*w on compacted threads (list order does not matter:
-        // each value depends on its own candidate only)
+        // ---- step 2: exact sigma*g*w on compacted threads (each value
+        // depends on its own candidate only)
         const int ne = sh.n_exact;
-        if (ne > 0) {
-            for (int q = tid; q < ne; q += NTC_BLOCK) {
-                const int t = sh.list[q];
-                const double gt = sqrt(sh.g2[t]);
-                sh.val[t] = I.vhs_factor * pow(gt, vexp) * gt * sh.val[t];
-            }
-            __syncthreads();
-            if (act && exact) sgw = sh.val[tid];
+        for (int q = tid; q < ne; q += NTC_BLOCK) {
+            const int t = sh.list[q];
+            const double gt = sqrt(sh.g2[t]);
+            sh.val[t] = I.vhs_factor * pow(gt, vexp) * gt * sh.val[t];
         }
-        // block inclusive max-scan of the sigma*g*w bit patterns
+        insert(nvalid, ni, nk);
+        __syncthreads();
+        // ---- step 3: inclusive max-scan of the sigma*g*w bit patterns, per warp
+        if (act && exact) sgw = sh.val[tid];
         long long mk = max_key(sgw, act && exact);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -186,7 +221,10 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
             if (lane >= o) mk = max(mk, t);
         }
         if (lane == 31) sh.wmax[wid] = mk;
+        first_conflict(nvalid, ni, nk);
         __syncthreads();
+        // ---- step 4: the scan across warps and the acceptance tests
+        if (tid == 0) sh.n_exact = 0;
         long long before = __double_as_longlong(smax);
         for (int w = 0; w < wid; ++w) before = max(before, sh.wmax[w]);
         mk = max(mk, before);
@@ -217,11 +255,12 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
             sh.list[atomicAdd(&sh.accepted, 1)] = tid;
         }
         __syncthreads();
+        // ---- step 5: scatter_vhs! of the accepted candidates on compacted
+        // threads; the batch's candidates share no particle, so the order is free
         const int na = sh.accepted;
+        const int Bn = sh.end;
         R.perf += na;
         smax = __longlong_as_double(sh.last_max);
-        // scatter_vhs! of the accepted candidates on compacted threads; the
-        // batch's candidates share no particle, so the order is free
         for (int q = tid; q < na; q += NTC_BLOCK) {
             const int t = sh.list[q];
             Stream sc;
@@ -241,9 +280,14 @@ __device__ __forceinline__ NtcResult ntc_cell_block(NtcBlockShared& sh, const In
             P1.wv[ti] = PV{ta.w, cx + I.mu2 * nx, cy + I.mu2 * ny, cz + I.mu2 * nz};
             P2.wv[tk] = PV{tb.w, cx - I.mu1 * nx, cy - I.mu1 * ny, cz - I.mu1 * nz};
         }
-        j0 += B;
-        // the next batch reads the scattered velocities and resets the counters
+        // the next batch reads the scattered velocities; the shared counters
+        // and lists are rewritten from here on
         __syncthreads();
+        j0 = jn;
+        B = Bn;
+        st = sn;
+        i = ni;
+        k = nk;
     }
     R.eqw = R.perf;
     R.smax = smax;
