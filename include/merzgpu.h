@@ -383,9 +383,12 @@ int mz_step(mz_domain* dom, const mz_step_plan* plan, int64_t n_steps, mz_props*
  * then n_steps of ntc! for every species pair and compute_props!.  Each
  * request occupies one cell of a server domain while it runs; requests are
  * admitted first come first served while a cell and the per-species particle
- * budget (capacity) are free, all running requests advance together in one
- * fused step per mz_server_step, and a request's result depends only on the
- * request (its seed), not on the requests beside it or its cell. */
+ * budget (capacity) are free, running requests advance together in fused
+ * steps, and a request's result depends only on the request (its seed), not
+ * on the requests beside it or its cell.  Requests of at least 4,096
+ * particles (mz_server_set_lane_split) run in a second lane -- a domain of
+ * its own on a stream of its own -- while the smaller ones step on another
+ * stream meanwhile, several of their steps per step of the large ones. */
 typedef struct mz_server_s mz_server;
 
 enum { MZ_REQ_QUEUED = 0, MZ_REQ_RUNNING = 1, MZ_REQ_DONE = 2 };
@@ -421,10 +424,12 @@ int mz_server_submit(mz_server* server, const mz_request* request, int64_t* id);
 /* admit what fits, advance every running request by one step, retire the
  * finished ones; counts after the step */
 int mz_server_step(mz_server* server, int64_t* n_running, int64_t* n_queued, int64_t* n_retired);
-/* The same for up to max_steps steps in one call: the call runs k steps, k =
- * the fewest steps any running request still needs (at most max_steps), so
- * no request steps past its end; queued requests are admitted at the start
- * of the call.  *n_steps receives k.  Results are those of k single steps. */
+/* The same for up to max_steps steps in one call.  The lane of large
+ * requests runs k steps, k = the fewest steps any of its running requests
+ * still needs (at most max_steps), so no request steps past its end; while
+ * they run, the lane of small requests runs such batches of steps one after
+ * another, retiring and admitting between them.  *n_steps receives the
+ * larger of the two lanes' step counts.  Results are those of single steps. */
 int mz_server_step_many(mz_server* server, int64_t max_steps, int64_t* n_steps, int64_t* n_running,
                         int64_t* n_queued, int64_t* n_retired);
 /* state of a request and, once done, its final properties */
@@ -432,8 +437,12 @@ int mz_server_result(mz_server* server, int64_t id, mz_request_result* out);
 /* ids of the requests the last mz_server_step retired (*n of them; up to
  * max_ids written) */
 int mz_server_retired(mz_server* server, int64_t max_ids, int64_t* ids, int64_t* n);
-/* server steps run and particle-steps done so far */
+/* steps run (by the lane that ran more) and particle-steps done so far */
 int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_steps);
+/* requests of at least `particles` particles (all species together) run in
+ * the lane of large requests; 0 puts all requests in one lane.  Applies to
+ * requests submitted afterwards.  Results do not depend on the lane. */
+int mz_server_set_lane_split(mz_server* server, int64_t particles);
 
 /* Choose the fused step's mapping by timing it: every combination of lanes
  * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the

@@ -12,6 +12,13 @@
 // running requests at once, and retires requests that reached their step
 // count with compute_props! of their last step (the only properties a request
 // returns).
+//
+// Large requests' steps take ~100x longer than small ones' (the candidate
+// loop of a cell is a sequential chain of batches whose length grows with
+// the cell), so requests run in two lanes by size, each its own domain on its
+// own stream: while the large lane runs its steps, the small lane runs batch
+// after batch of steps.  A small request then waits for neither the large
+// requests' chains nor their admission.
 #include "mz_host.h"
 
 #include <algorithm>
@@ -26,6 +33,7 @@ namespace {
 struct ReqRec {
     mz_request r;
     int32_t state = MZ_REQ_QUEUED;
+    int32_t lane = 0;  // 0: small requests, 1: large ones
     int32_t slot = -1;
     int64_t start_step = 0;  // server step before the request's first step
     mz_request_result res{};
@@ -212,20 +220,18 @@ double sigma_g_w_max_estimate(const Interaction& I, double m1, double m2, double
 
 }  // namespace
 
-struct mz_server_s {
-    mz_ctx* ctx = nullptr;
+// One lane: a domain of max_requests cells on its own stream, with its own
+// admission queue, slots and step count.
+struct ServerLane {
+    mz_ctx* ctx = nullptr;     // the lane's own context (streams, events)
+    bool own_ctx = false;
     mz_domain* dom = nullptr;
-    int32_t ns = 0;
-    int64_t slots = 0;
-    double dt = 0.0;
-    int64_t step = 0;  // server steps run
-    int64_t next_id = 1;
+    int64_t step = 0;          // steps this lane has run
     std::deque<int64_t> queue;
-    std::unordered_map<int64_t, ReqRec> reqs;
     std::vector<int64_t> slot_req;  // request id per slot, 0 = free
     std::vector<int64_t> free_slots;
     std::vector<int64_t> running;   // ids of admitted, unfinished requests
-    std::vector<int64_t> retired;   // ids retired by the last mz_server_step
+    cudaEvent_t done = nullptr;     // end of the lane's last launched steps
     // device scratch for admissions / retirements
     int32_t* d_cells = nullptr;
     double* d_part = nullptr;  // chunk sums of the finishing requests' props
@@ -235,6 +241,20 @@ struct mz_server_s {
     uint32_t* d_off = nullptr;
     double* d_V = nullptr;
     double* d_smax = nullptr;
+};
+
+struct mz_server_s {
+    mz_ctx* ctx = nullptr;
+    int32_t ns = 0;
+    int64_t slots = 0;
+    double dt = 0.0;
+    int64_t next_id = 1;
+    // requests of at least `split` particles (all species) run in lane 1,
+    // smaller ones in lane 0, each lane stepping at its own pace; 0: lane 0 only
+    int64_t split = 4096;
+    ServerLane lane[2];
+    std::unordered_map<int64_t, ReqRec> reqs;
+    std::vector<int64_t> retired;   // ids retired by the last mz_server_step
     int64_t particle_steps = 0;
 };
 
@@ -258,9 +278,9 @@ void ensure_rng_arrays(mz_domain* d)
 }
 
 // admit queued requests while slots and storage allow; FIFO, no overtaking
-void admit(mz_server* sv)
+void admit(mz_server* sv, ServerLane& L)
 {
-    mz_domain* d = sv->dom;
+    mz_domain* d = L.dom;
     const int ns = sv->ns;
     std::vector<int32_t> cells;
     std::vector<uint64_t> seeds;
@@ -269,8 +289,8 @@ void admit(mz_server* sv)
     std::vector<std::vector<int64_t>> counts(ns, std::vector<int64_t>(d->n_cells, 0));
     std::vector<double> T3(3 * d->n_cells * ns, 0.0), F(d->n_cells * ns, 0.0);
     int64_t need[MZ_MAX_SPECIES] = {0, 0, 0, 0};
-    while (!sv->queue.empty() && !sv->free_slots.empty()) {
-        const int64_t id = sv->queue.front();
+    while (!L.queue.empty() && !L.free_slots.empty()) {
+        const int64_t id = L.queue.front();
         ReqRec& q = sv->reqs.at(id);
         bool fits = true;
         for (int s = 0; s < ns && fits; ++s) {
@@ -283,17 +303,17 @@ void admit(mz_server* sv)
             }
         }
         if (!fits) break;
-        sv->queue.pop_front();
-        const int32_t slot = (int32_t)sv->free_slots.back();
-        sv->free_slots.pop_back();
+        L.queue.pop_front();
+        const int32_t slot = (int32_t)L.free_slots.back();
+        L.free_slots.pop_back();
         q.state = MZ_REQ_RUNNING;
         q.slot = slot;
-        q.start_step = sv->step;
-        sv->slot_req[slot] = id;
-        sv->running.push_back(id);
+        q.start_step = L.step;
+        L.slot_req[slot] = id;
+        L.running.push_back(id);
         cells.push_back(slot);
         seeds.push_back(q.r.seed);
-        offs.push_back((uint32_t)sv->step);
+        offs.push_back((uint32_t)L.step);
         Vs.push_back(q.r.V);
         for (int s2 = 0; s2 < ns; ++s2)
             for (int s1 = 0; s1 < ns; ++s1) {
@@ -310,13 +330,13 @@ void admit(mz_server* sv)
     }
     if (cells.empty()) return;
     const int n = (int)cells.size();
-    mz_ctx* c = sv->ctx;
-    MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-    MZ_CK(cudaMemcpyAsync(sv->d_seed, seeds.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
-    MZ_CK(cudaMemcpyAsync(sv->d_off, offs.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
-    MZ_CK(cudaMemcpyAsync(sv->d_V, Vs.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    MZ_CK(cudaMemcpyAsync(sv->d_smax, smax.data(), smax.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    AdmitArgs a{sv->d_cells, n, sv->d_seed, sv->d_off, sv->d_V, sv->d_smax};
+    mz_ctx* c = L.ctx;
+    MZ_CK(cudaMemcpyAsync(L.d_cells, cells.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(L.d_seed, seeds.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(L.d_off, offs.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(L.d_V, Vs.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    MZ_CK(cudaMemcpyAsync(L.d_smax, smax.data(), smax.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AdmitArgs a{L.d_cells, n, L.d_seed, L.d_off, L.d_V, L.d_smax};
     DomainView v = make_view(d);
     MZ_LAUNCH(c, "server_admit", k_admit, (int)div_up(n, 128), 128, 0, v, a, d->d_cell_seed, d->d_cell_rid,
               d->d_cell_step, d->d_V);
@@ -324,9 +344,149 @@ void admit(mz_server* sv)
     for (int s = 0; s < ns; ++s) {
         if (need[s] == 0) continue;
         launch_sample_cells(d, s, counts[s].data(), nullptr, T3.data() + (size_t)s * 3 * d->n_cells, nullptr,
-                            F.data() + (size_t)s * d->n_cells, 0.0, nullptr, 0, (uint64_t)sv->step);
+                            F.data() + (size_t)s * d->n_cells, 0.0, nullptr, 0, (uint64_t)L.step);
         d->sp[s].compact = false;
     }
+}
+
+// Launch the lane's next steps on its stream without waiting: as many as
+// every running request still needs, at most max_steps (no request steps
+// past its end).  Returns the number of steps (0: nothing runs).
+int64_t launch_lane(mz_server* sv, ServerLane& L, int64_t max_steps)
+{
+    if (L.running.empty()) return 0;
+    mz_step_plan plan;
+    memset(&plan, 0, sizeof plan);
+    plan.dims = 0;
+    plan.collide = 1;
+    plan.equal_weight = 1;
+    plan.props = 0;  // compute_props! of the finishing requests runs after the steps
+    plan.dt = sv->dt;
+    plan.dw_tol = 1e-16;
+    plan.step0 = (uint64_t)L.step;
+    plan.use_graph = 0;
+    int64_t k = max_steps;
+    for (int64_t id : L.running) {
+        const ReqRec& q = sv->reqs.at(id);
+        k = std::min<int64_t>(k, q.r.n_steps - (L.step - q.start_step));
+    }
+    k = std::max<int64_t>(k, 1);
+    launch_step(L.dom, &plan, k, nullptr, nullptr);
+    MZ_CK(cudaEventRecord(L.done, L.ctx->stream));
+    return k;
+}
+
+// Book the lane's k launched steps and retire the requests they finished:
+// compute_props! of their last step over their cells only, then release.
+// Returns the number retired.
+int64_t finish_lane(mz_server* sv, ServerLane& L, int64_t k)
+{
+    if (k <= 0) return 0;
+    mz_domain* d = L.dom;
+    mz_ctx* c = L.ctx;
+    const int ns = sv->ns;
+    L.step += k;
+    std::vector<int64_t> done;
+    for (int64_t id : L.running) {
+        ReqRec& q = sv->reqs.at(id);
+        q.res.steps_done = L.step - q.start_step;
+        for (int s = 0; s < ns; ++s) sv->particle_steps += q.r.count[s] * k;
+        if (q.res.steps_done >= q.r.n_steps) done.push_back(id);
+    }
+    if (done.empty()) return 0;
+    std::vector<int32_t> cells;
+    int64_t kmax = 1;
+    for (int64_t id : done) {
+        const ReqRec& q = sv->reqs.at(id);
+        cells.push_back((int32_t)q.slot);
+        for (int s = 0; s < ns; ++s) kmax = std::max<int64_t>(kmax, div_up(q.r.count[s], LP_CHUNK));
+    }
+    const int n_items = (int)cells.size() * ns;
+    MZ_REQUIRE((int64_t)n_items * kmax < INT32_MAX, "mz_server_step: too many particles finishing at once");
+    if ((int64_t)n_items * kmax * 5 > L.part_cap) {
+        cudaFree(L.d_part);
+        L.d_part = nullptr;
+        L.part_cap = 0;
+        const int64_t cap = std::max<int64_t>((int64_t)n_items * kmax * 5, 1 << 16);
+        MZ_CK(cudaMalloc(&L.d_part, cap * sizeof(double)));
+        L.part_cap = cap;
+    }
+    MZ_CK(cudaMemcpyAsync(L.d_cells, cells.data(), cells.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                          c->stream));
+    ListProps lp{L.d_cells, n_items, (int)kmax, L.d_part, L.d_lp};
+    DomainView vp = make_view(d);
+    const int lg = (int)(n_items * kmax);  // one block per (request, species, chunk)
+    MZ_LAUNCH(c, "server_props_moments", k_lp_moments, lg, LP_THREADS, 0, vp, lp);
+    MZ_LAUNCH(c, "server_props_energy", k_lp_energy, lg, LP_THREADS, 0, vp, lp);
+    MZ_LAUNCH(c, "server_props_finish", k_lp_finish, (int)div_up(n_items, 128), 128, 0, vp, lp);
+    std::vector<double> o((size_t)n_items * 6);
+    MZ_CK(cudaMemcpyAsync(o.data(), L.d_lp, o.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MZ_CK(cudaStreamSynchronize(c->stream));
+    int i = 0;
+    for (int64_t id : done) {
+        ReqRec& q = sv->reqs.at(id);
+        const int64_t slot = q.slot;
+        for (int s = 0; s < ns; ++s) {
+            const double* r = o.data() + ((size_t)i * ns + s) * 6;
+            q.res.np[s] = (int64_t)r[0];
+            q.res.n[s] = r[1];
+            for (int a = 0; a < 3; ++a) q.res.v[s][a] = r[2 + a];
+            q.res.T[s] = r[5];
+        }
+        ++i;
+        q.res.steps_done = q.r.n_steps;
+        q.state = MZ_REQ_DONE;
+        sv->retired.push_back(id);
+        L.slot_req[slot] = 0;
+        L.free_slots.push_back(slot);
+        for (int s = 0; s < ns; ++s) d->sp[s].n_total -= q.r.count[s];
+    }
+    DomainView vv = make_view(d);
+    MZ_LAUNCH(c, "server_release", k_release, (int)div_up((int64_t)cells.size() * 32, 256), 256, 0, vv, L.d_cells,
+              (int)cells.size());
+    for (int s = 0; s < ns; ++s) d->sp[s].compact = false;
+    L.running.erase(std::remove_if(L.running.begin(), L.running.end(),
+                                   [&](int64_t id) { return sv->reqs.at(id).state == MZ_REQ_DONE; }),
+                    L.running.end());
+    return (int64_t)done.size();
+}
+
+void lane_init(mz_server* sv, ServerLane& L, mz_ctx* c, bool own, int64_t max_requests, const int64_t* capacity,
+               const double* mass, const mz_interaction* inter)
+{
+    L.ctx = c;
+    L.own_ctx = own;
+    int rc = mz_domain_create(c, max_requests, sv->ns, capacity, &L.dom);
+    if (rc == MZ_OK) rc = mz_set_species(L.dom, mass);
+    if (rc == MZ_OK) rc = mz_set_interactions(L.dom, inter);
+    if (rc != MZ_OK) throw MzError(rc, "mz_server_create: " + c->last_error);
+    ensure_rng_arrays(L.dom);
+    L.slot_req.assign(max_requests, 0);
+    for (int64_t s = max_requests - 1; s >= 0; --s) L.free_slots.push_back(s);
+    MZ_CK(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+    MZ_CK(cudaMalloc(&L.d_cells, max_requests * sizeof(int32_t)));
+    MZ_CK(cudaMalloc(&L.d_lp, max_requests * sv->ns * 6 * sizeof(double)));
+    MZ_CK(cudaMalloc(&L.d_seed, max_requests * sizeof(uint64_t)));
+    MZ_CK(cudaMalloc(&L.d_off, max_requests * sizeof(uint32_t)));
+    MZ_CK(cudaMalloc(&L.d_V, max_requests * sizeof(double)));
+    MZ_CK(cudaMalloc(&L.d_smax, max_requests * sv->ns * sv->ns * sizeof(double)));
+}
+
+void lane_free(ServerLane& L)
+{
+    if (!L.ctx) return;
+    cudaStreamSynchronize(L.ctx->stream);
+    cudaFree(L.d_cells);
+    cudaFree(L.d_part);
+    cudaFree(L.d_lp);
+    cudaFree(L.d_seed);
+    cudaFree(L.d_off);
+    cudaFree(L.d_V);
+    cudaFree(L.d_smax);
+    if (L.done) cudaEventDestroy(L.done);
+    if (L.dom) mz_domain_destroy(L.dom);
+    if (L.own_ctx) mz_ctx_destroy(L.ctx);
+    L = ServerLane();
 }
 
 }  // namespace
@@ -336,33 +496,37 @@ extern "C" {
 int mz_server_create(mz_ctx* c, int32_t n_species, const double* mass, const mz_interaction* inter, double dt,
                      int64_t max_requests, const int64_t* capacity, mz_server** out)
 {
-    mz_server* sv = nullptr;
     API_TRY
     MZ_REQUIRE(c && out && mass && inter && capacity, "mz_server_create: NULL argument");
     MZ_REQUIRE(n_species >= 1 && n_species <= MZ_MAX_SPECIES, "mz_server_create: bad species count");
     MZ_REQUIRE(max_requests >= 1 && max_requests < (1 << 24), "mz_server_create: bad max_requests");
     MZ_REQUIRE(dt > 0.0, "mz_server_create: dt must be positive");
-    sv = new mz_server_s();
+    struct Guard {  // frees a partly built server when set-up throws
+        mz_server* p = nullptr;
+        ~Guard()
+        {
+            if (!p) return;
+            lane_free(p->lane[0]);
+            lane_free(p->lane[1]);
+            delete p;
+        }
+    } guard;
+    mz_server* sv = guard.p = new mz_server_s();
     sv->ctx = c;
     sv->ns = n_species;
     sv->slots = max_requests;
     sv->dt = dt;
-    int rc = mz_domain_create(c, max_requests, n_species, capacity, &sv->dom);
-    if (rc != MZ_OK) throw MzError(rc, "mz_server_create: domain");
-    rc = mz_set_species(sv->dom, mass);
-    if (rc == MZ_OK) rc = mz_set_interactions(sv->dom, inter);
-    if (rc != MZ_OK) throw MzError(rc, "mz_server_create: set-up");
-    ensure_rng_arrays(sv->dom);
-    sv->slot_req.assign(max_requests, 0);
-    for (int64_t s = max_requests - 1; s >= 0; --s) sv->free_slots.push_back(s);
-    MZ_CK(cudaMalloc(&sv->d_cells, max_requests * sizeof(int32_t)));
-    MZ_CK(cudaMalloc(&sv->d_lp, max_requests * n_species * 6 * sizeof(double)));
-    MZ_CK(cudaMalloc(&sv->d_seed, max_requests * sizeof(uint64_t)));
-    MZ_CK(cudaMalloc(&sv->d_off, max_requests * sizeof(uint32_t)));
-    MZ_CK(cudaMalloc(&sv->d_V, max_requests * sizeof(double)));
-    MZ_CK(cudaMalloc(&sv->d_smax, max_requests * n_species * n_species * sizeof(double)));
+    // each lane on streams of its own, so that the two overlap
+    for (int l = 0; l < 2; ++l) {
+        mz_ctx* cl = nullptr;
+        const int rc = mz_ctx_create(c->device, &cl);
+        if (rc != MZ_OK) throw MzError(rc, "mz_server_create: lane streams");
+        sv->lane[l].ctx = cl;  // freed with the lane if the set-up throws
+        sv->lane[l].own_ctx = true;
+        lane_init(sv, sv->lane[l], cl, true, max_requests, capacity, mass, inter);
+    }
     *out = sv;
-    sv = nullptr;
+    guard.p = nullptr;
     API_CATCH(c)
 }
 
@@ -370,17 +534,20 @@ int mz_server_destroy(mz_server* sv)
 {
     if (!sv) return MZ_OK;
     cudaSetDevice(sv->ctx->device);
-    cudaStreamSynchronize(sv->ctx->stream);
-    cudaFree(sv->d_cells);
-    cudaFree(sv->d_part);
-    cudaFree(sv->d_lp);
-    cudaFree(sv->d_seed);
-    cudaFree(sv->d_off);
-    cudaFree(sv->d_V);
-    cudaFree(sv->d_smax);
-    if (sv->dom) mz_domain_destroy(sv->dom);
+    lane_free(sv->lane[0]);
+    lane_free(sv->lane[1]);
     delete sv;
     return MZ_OK;
+}
+
+/* requests of at least `particles` particles (all species) run in the lane
+ * of large requests; 0 puts every request in one lane */
+int mz_server_set_lane_split(mz_server* sv, int64_t particles)
+{
+    API_TRY
+    MZ_REQUIRE(sv && particles >= 0, "mz_server_set_lane_split: bad argument");
+    sv->split = particles;
+    API_CATCH(sv ? sv->ctx : nullptr)
 }
 
 int mz_server_submit(mz_server* sv, const mz_request* r, int64_t* id)
@@ -389,16 +556,19 @@ int mz_server_submit(mz_server* sv, const mz_request* r, int64_t* id)
     MZ_REQUIRE(sv && r && id, "mz_server_submit: NULL argument");
     MZ_REQUIRE(r->n_steps >= 1 && r->Fnum > 0.0 && r->V > 0.0, "mz_server_submit: bad request");
     for (int s = 0; s < sv->ns; ++s) {
-        MZ_REQUIRE(r->count[s] >= 0 && r->count[s] <= sv->dom->sp[s].capacity,
+        MZ_REQUIRE(r->count[s] >= 0 && r->count[s] <= sv->lane[0].dom->sp[s].capacity,
                    "mz_server_submit: request larger than the particle budget");
         MZ_REQUIRE(r->count[s] == 0 || r->T[s] > 0.0, "mz_server_submit: temperature must be positive");
     }
+    int64_t total = 0;
+    for (int s = 0; s < sv->ns; ++s) total += r->count[s];
     ReqRec q;
     q.r = *r;
+    q.lane = sv->split > 0 && total >= sv->split ? 1 : 0;
     q.res.id = sv->next_id;
     const int64_t k = sv->next_id++;
     sv->reqs.emplace(k, q);
-    sv->queue.push_back(k);
+    sv->lane[q.lane].queue.push_back(k);
     *id = k;
     API_CATCH(sv->ctx)
 }
@@ -410,106 +580,40 @@ int mz_server_step_many(mz_server* sv, int64_t max_steps, int64_t* n_steps, int6
     MZ_REQUIRE(sv && max_steps >= 1, "mz_server_step_many: bad argument");
     if (n_steps) *n_steps = 0;
     MZ_CK(cudaSetDevice(sv->ctx->device));
-    mz_domain* d = sv->dom;
-    admit(sv);
-    int64_t running = (int64_t)sv->running.size(), retired = 0;
     sv->retired.clear();
-    if (running > 0) {
-        mz_step_plan plan;
-        memset(&plan, 0, sizeof plan);
-        plan.dims = 0;
-        plan.collide = 1;
-        plan.equal_weight = 1;
-        plan.props = 0;  // compute_props! of the finishing requests runs after the steps
-        plan.dt = sv->dt;
-        plan.dw_tol = 1e-16;
-        plan.step0 = (uint64_t)sv->step;
-        plan.use_graph = 0;
-        // as many steps as every running request still needs, at most max_steps:
-        // no request steps past its end, and admissions wait for the next call
-        int64_t ksteps = max_steps;
-        for (int64_t k : sv->running) {
-            const ReqRec& q = sv->reqs.at(k);
-            ksteps = std::min<int64_t>(ksteps, q.r.n_steps - (sv->step - q.start_step));
+    ServerLane& small = sv->lane[0];
+    ServerLane& large = sv->lane[1];
+    // the large requests' steps run on their stream; meanwhile the small
+    // requests' lane steps again and again (retiring and admitting between
+    // its launches) until the large lane is done, so small requests do not
+    // wait for the long collision chains of large cells
+    admit(sv, large);
+    const int64_t kl = launch_lane(sv, large, max_steps);
+    int64_t ks = 0;
+    for (;;) {
+        admit(sv, small);
+        const int64_t k = launch_lane(sv, small, max_steps);
+        if (k > 0) {
+            MZ_CK(cudaEventSynchronize(small.done));
+            finish_lane(sv, small, k);
+            ks += k;
         }
-        ksteps = std::max<int64_t>(ksteps, 1);
-        std::vector<int64_t> done;
-        launch_step(d, &plan, ksteps, nullptr, nullptr);
-        sv->step += ksteps;
-        if (n_steps) *n_steps = ksteps;
-        for (int64_t k : sv->running) {
-            ReqRec& q = sv->reqs.at(k);
-            q.res.steps_done = sv->step - q.start_step;
-            for (int s = 0; s < sv->ns; ++s) sv->particle_steps += q.r.count[s] * ksteps;
-            if (q.res.steps_done >= q.r.n_steps) done.push_back(k);
-        }
-        if (!done.empty()) {
-            // final properties of the finished requests: compute_props! of
-            // their last step, for their cells only
-            const int ns = sv->ns;
-            std::vector<int32_t> cells;
-            int64_t kmax = 1;
-            for (int64_t k : done) {
-                const ReqRec& q = sv->reqs.at(k);
-                cells.push_back((int32_t)q.slot);
-                for (int s = 0; s < ns; ++s) kmax = std::max<int64_t>(kmax, div_up(q.r.count[s], LP_CHUNK));
-            }
-            const int n_items = (int)cells.size() * ns;
-            if ((int64_t)n_items * kmax * 5 > sv->part_cap) {
-                cudaFree(sv->d_part);
-                sv->d_part = nullptr;
-                sv->part_cap = 0;
-                const int64_t cap = std::max<int64_t>((int64_t)n_items * kmax * 5, 1 << 16);
-                MZ_CK(cudaMalloc(&sv->d_part, cap * sizeof(double)));
-                sv->part_cap = cap;
-            }
-            MZ_CK(cudaMemcpyAsync(sv->d_cells, cells.data(), cells.size() * sizeof(int32_t),
-                                  cudaMemcpyHostToDevice, sv->ctx->stream));
-            ListProps lp{sv->d_cells, n_items, (int)kmax, sv->d_part, sv->d_lp};
-            DomainView vp = make_view(d);
-            MZ_REQUIRE((int64_t)n_items * kmax < INT32_MAX, "mz_server_step: too many particles finishing at once");
-            const int lg = (int)(n_items * kmax);  // one block per (request, species, chunk)
-            MZ_LAUNCH(sv->ctx, "server_props_moments", k_lp_moments, lg, LP_THREADS, 0, vp, lp);
-            MZ_LAUNCH(sv->ctx, "server_props_energy", k_lp_energy, lg, LP_THREADS, 0, vp, lp);
-            MZ_LAUNCH(sv->ctx, "server_props_finish", k_lp_finish, (int)div_up(n_items, 128), 128, 0, vp, lp);
-            std::vector<double> o((size_t)n_items * 6);
-            MZ_CK(cudaMemcpyAsync(o.data(), sv->d_lp, o.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                                  sv->ctx->stream));
-            MZ_CK(cudaStreamSynchronize(sv->ctx->stream));
-            int i = 0;
-            for (int64_t k : done) {
-                ReqRec& q = sv->reqs.at(k);
-                const int64_t c = q.slot;
-                for (int s = 0; s < ns; ++s) {
-                    const double* r = o.data() + ((size_t)i * ns + s) * 6;
-                    q.res.np[s] = (int64_t)r[0];
-                    q.res.n[s] = r[1];
-                    for (int a = 0; a < 3; ++a) q.res.v[s][a] = r[2 + a];
-                    q.res.T[s] = r[5];
-                }
-                ++i;
-                q.res.steps_done = q.r.n_steps;
-                q.state = MZ_REQ_DONE;
-                sv->retired.push_back(k);
-                sv->slot_req[c] = 0;
-                sv->free_slots.push_back(c);
-                for (int s = 0; s < ns; ++s) d->sp[s].n_total -= q.r.count[s];
-                ++retired;
-            }
-            DomainView vv = make_view(d);
-            MZ_LAUNCH(sv->ctx, "server_release", k_release, (int)div_up((int64_t)cells.size() * 32, 256), 256, 0, vv,
-                      sv->d_cells, (int)cells.size());
-            for (int s = 0; s < ns; ++s) d->sp[s].compact = false;
-            sv->running.erase(std::remove_if(sv->running.begin(), sv->running.end(),
-                                             [&](int64_t k) { return sv->reqs.at(k).state == MZ_REQ_DONE; }),
-                              sv->running.end());
-            running -= retired;
-        }
+        if (kl == 0 || k == 0) break;
+        const cudaError_t q = cudaEventQuery(large.done);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) MZ_CK(q);
+        if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();  // not a failure
     }
-    if (n_running) *n_running = running;
-    if (n_queued) *n_queued = (int64_t)sv->queue.size();
-    if (n_retired) *n_retired = retired;
-    check_status(d);
+    if (kl > 0) {
+        MZ_CK(cudaEventSynchronize(large.done));
+        finish_lane(sv, large, kl);
+    }
+    if (n_steps) *n_steps = std::max(kl, ks);
+    if (n_running) *n_running = (int64_t)(small.running.size() + large.running.size());
+    if (n_queued) *n_queued = (int64_t)(small.queue.size() + large.queue.size());
+    if (n_retired) *n_retired = (int64_t)sv->retired.size();
+    check_status(small.dom);
+    check_status(large.dom);
     API_CATCH(sv->ctx)
 }
 
@@ -527,7 +631,8 @@ int mz_server_result(mz_server* sv, int64_t id, mz_request_result* out)
     *out = it->second.res;
     out->id = id;
     out->state = it->second.state;
-    if (it->second.state == MZ_REQ_RUNNING) out->steps_done = sv->step - it->second.start_step;
+    if (it->second.state == MZ_REQ_RUNNING)
+        out->steps_done = sv->lane[it->second.lane].step - it->second.start_step;
     API_CATCH(sv->ctx)
 }
 
@@ -544,7 +649,7 @@ int mz_server_info(mz_server* sv, int64_t* steps_run, int64_t* particle_steps)
 {
     API_TRY
     MZ_REQUIRE(sv, "mz_server_info: NULL server");
-    if (steps_run) *steps_run = sv->step;
+    if (steps_run) *steps_run = std::max(sv->lane[0].step, sv->lane[1].step);
     if (particle_steps) *particle_steps = sv->particle_steps;
     API_CATCH(sv->ctx)
 }

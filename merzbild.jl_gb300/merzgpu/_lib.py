@@ -138,6 +138,7 @@ _SIGS = {
     "mz_server_result": (i32, [vp, i64, P(RequestResult)]),
     "mz_server_retired": (i32, [vp, i64, P(i64), P(i64)]),
     "mz_server_info": (i32, [vp, P(i64), P(i64)]),
+    "mz_server_set_lane_split": (i32, [vp, i64]),
     "mz_swpm": (i32, [vp, i32, d, d, i64, i64, u64]),
     "mz_props_snapshot": (i32, [vp, i32, P(d)]),
     "mz_props_snapshot_wait": (i32, [vp, i32]),

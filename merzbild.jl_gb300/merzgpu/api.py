@@ -609,9 +609,11 @@ class Server:
     """Continuous-batching server of independent 0-D solves (mz_server_*).
 
     Each request is the README relaxation problem for given particle counts
-    and temperatures per species; requests run side by side in one domain,
-    one cell each, and advance together one fused step per `step()`.  A
-    request's result depends only on the request itself (its seed)."""
+    and temperatures per species; requests run side by side, one cell each,
+    and advance together in fused steps.  Requests of at least 4,096
+    particles (`set_lane_split`) run in a second lane (domain and stream) while the smaller ones
+    take several steps per step of the large ones.  A request's result
+    depends only on the request itself (its seed)."""
 
     def __init__(self, ctx: Context, species_data, interactions, dt, max_requests, capacity):
         self.ctx = ctx
@@ -641,6 +643,11 @@ class Server:
 
     def _ck(self, rc):
         check(rc, self.ctx.h)
+
+    def set_lane_split(self, particles):
+        """mz_server_set_lane_split: requests of at least `particles` particles
+        go to the lane of large requests (0: one lane for all)."""
+        self._ck(lib().mz_server_set_lane_split(self.h, int(particles)))
 
     def submit(self, counts, T, Fnum, n_steps, seed, V=1.0):
         r = L.Request()

@@ -146,3 +146,21 @@ def test_poisson_request_loop_completes_every_request(ctx):
     info = sv.info()
     assert info["particle_steps"] == sum(sum(kw["counts"]) * kw["n_steps"] for _, kw in reqs)
     sv.close()
+
+
+def test_two_lanes_give_the_results_of_one(ctx):
+    """Requests of at least 3,000 particles in the lane of large requests (its
+    own domain and stream, stepping while the small lane takes batches of
+    steps) against all requests in one lane: identical results."""
+    out = []
+    for split in (0, 3000):
+        sv = _server(ctx, max_requests=4, capacity=16_000)
+        sv.set_lane_split(split)
+        out.append(_run(sv, REQUESTS, stagger=True, max_steps=5))
+        sv.close()
+    one, two = out
+    for seed, a in one.items():
+        m = two[seed]
+        assert m["state"] == mz._lib.MZ_REQ_DONE and a["steps_done"] == m["steps_done"]
+        for key in ("np", "n", "T", "v"):
+            assert a[key] == m[key], (seed, key)
