@@ -434,7 +434,7 @@ int mz_server_step_many(mz_server* server, int64_t max_steps, int64_t* n_steps, 
                         int64_t* n_queued, int64_t* n_retired);
 /* state of a request and, once done, its final properties */
 int mz_server_result(mz_server* server, int64_t id, mz_request_result* out);
-/* ids of the requests the last mz_server_step retired (*n of them; up to
+/* ids of the requests the last mz_server_step(_many) call retired (*n of them; up to
  * max_ids written) */
 int mz_server_retired(mz_server* server, int64_t max_ids, int64_t* ids, int64_t* n);
 /* steps run (by the lane that ran more) and particle-steps done so far */

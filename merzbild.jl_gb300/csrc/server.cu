@@ -35,7 +35,7 @@ struct ReqRec {
     int32_t state = MZ_REQ_QUEUED;
     int32_t lane = 0;  // 0: small requests, 1: large ones
     int32_t slot = -1;
-    int64_t start_step = 0;  // server step before the request's first step
+    int64_t start_step = 0;  // its lane's step count before the request's first step
     mz_request_result res{};
 };
 
@@ -254,7 +254,7 @@ struct mz_server_s {
     int64_t split = 4096;
     ServerLane lane[2];
     std::unordered_map<int64_t, ReqRec> reqs;
-    std::vector<int64_t> retired;   // ids retired by the last mz_server_step
+    std::vector<int64_t> retired;   // ids retired by the last mz_server_step(_many) call
     int64_t particle_steps = 0;
 };
 
