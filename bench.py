@@ -582,6 +582,28 @@ def run_gpu(args):
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": ALG_BYTES * n,
                 "kernel_share": {k: v[0] / tot for k, v in sorted(timings.items(), key=lambda kv: -kv[1][0])}}
+    # secondary bound: the FP64 pipe.  GB300 spends 16 SM cycles on every FP64
+    # warp instruction (2 DFMA per SM per clock); the step's FP64 warp
+    # instructions per particle come from the committed ncu capture of the
+    # full-step kernel (0.81: collisions, convection, both props passes), so
+    # their pipe time at the clock seen during the timed region is a floor
+    ffile = os.path.join(ROOT, "profiles", "step_cell_couette_4e6.md")
+    if os.path.exists(ffile):
+        with open(ffile) as f:
+            m = re.search(r"^fp64_warp_inst_per_particle:\s*([0-9.eE+-]+)", f.read(), re.M)
+        if m:
+            inst_pp = float(m.group(1))
+            ck = clk if isinstance(clk, dict) else {}
+            sm_hz = 1e6 * (ck.get("sm_mhz") or ck.get("sm_max_mhz") or 2070.0)
+            import torch
+
+            n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+            floor_s = inst_pp * n * 16.0 / (n_sms * sm_hz)
+            roofline["secondary"] = {
+                "bound": "fp64", "fp64_warp_inst_per_particle": inst_pp, "pipe_cycles_per_warp_inst": 16,
+                "sm_mhz": sm_hz / 1e6, "floor_ms_per_step": floor_s * 1e3,
+                "frac": floor_s / (ms / K / 1e3),
+                "source": "ncu capture of the full-step kernel, 4e6 particles (profiles/step_cell_couette_4e6.md)"}
 
     # plain form: the reference's call granularity -- one ntc launch per cell,
     # then convect, sort and props as separate calls
