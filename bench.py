@@ -257,7 +257,9 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
     out = {"workload": "0-D Ar relaxation, 65,536 cells, N log-uniform [50, 4000], bi-Maxwellian 2000/300/300 K",
            "particles": n, "steps": steps, "mapping": {"lanes_per_cell": lanes, "block_per_cell_from": big}, "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
            "collisions_per_s": cnt["accepted"] / (ms / 1e3), "plain_value": n / plain_s,
-           "batched_over_plain": value / (n / plain_s)}
+           "batched_over_plain": value / (n / plain_s),
+           # 0-D step: v and w read (32 B) and v written (24 B) per particle-step
+           "hbm_frac_algorithmic": 56.0 * value / (measured_peaks()[0] * 1e9)}
     dom.close()
     return out
 
@@ -330,7 +332,9 @@ def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
            "mean_live_particles": live / steps, "steps": steps, "value": value, "unit": "particle-steps/s",
            "ms_per_step": ms / steps, "collisions_per_s": cnt["accepted"] / (ms / 1e3),
            "splits_per_step": cnt["splits"] / steps, "merged_cells_per_step": cnt["merges"] / steps,
-           "plain_value": n_plain / plain_s, "batched_over_plain": value / (n_plain / plain_s)}
+           "plain_value": n_plain / plain_s, "batched_over_plain": value / (n_plain / plain_s),
+           # 1-D step: every live particle read and written once (56 B each way)
+           "hbm_frac_algorithmic": 112.0 * value / (measured_peaks()[0] * 1e9)}
     dom.close()
     return out
 
