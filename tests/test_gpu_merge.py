@@ -182,3 +182,41 @@ def test_merge_cells_vs_oracle(ctx, orc, init, bounds, max_bins, max_depth, targ
         dom.sort(0, g)
         assert dom.info(0)["n_total"] == nt
         assert dom.info(0)["high_water"] == nt
+
+
+def test_merge_1d_keeps_particles_in_the_grid(ctx, orc):
+    """test/test_octree_merging_1D.jl: 4 particles in each of 2 unit-grid cells
+    placed so that mean(x) -/+ std(x) leaves the domain; merged to 2 per cell
+    without the grid some land outside, with the grid none does, and the
+    device matches the oracle's merge with the same streams."""
+    x1, x2 = [0.05, 0.05, 0.05, 0.45], [0.55, 0.95, 0.85, 0.99]
+    parts = np.array([[2.0, 0.5, -3.0, 4.0, x, 0.0, 0.0] for x in x1] +
+                     [[3.0, 0.5, -3.0, 4.0, x, 0.0, 0.0] for x in x2])
+    cells = np.array([0, 0, 0, 0, 1, 1, 1, 1], np.int32)
+    g = mz.Grid1DUniform(1.0, 2)
+    for with_grid in (False, True):
+        dom = mz.Domain(ctx, 2, species(["Ar"]), 64, seed=1234)
+        dom.upload(0, parts[:, 0], parts[:, 1:4], parts[:, 4:7], cells)
+        octree = mz.OctreeN2Merge(init_bin_bounds=mz.OctreeInitBinC)
+        merged = dom.merge_octree(0, octree, 2, threshold=-1, grid=g if with_grid else None, step=0)
+        assert merged == 2
+        ind, nt = dom.indexer(0)
+        assert nt == 4 and ind[:, 3].tolist() == [2, 2]
+        drows, dcells = device_logical(dom, 0)
+        for c in (0, 1):
+            x = drows[dcells == c, 4]
+            assert bool(np.any((x < 0.0) | (x > 1.0))) == (not with_grid), (with_grid, c, x)
+        o = orc.Oracle(2, 1, [mz.AR_MASS])
+        o.set_particles_simple(0, cells + 1, parts)
+        oc = orc.Octree(orc.SPLIT_MID, orc.INIT_C)
+        for c in (1, 2):
+            o.merge_octree(oc, 0, c, 2, L=1.0 if with_grid else None, nx=2, seed=1234, step=0)
+        orows, ocells = oracle_logical(o, 0)
+        assert np.array_equal(ocells, dcells)
+        assert_close_rows(orows, drows, RTOL, "1-D merge")
+        if with_grid:
+            dom.sort(0, g)
+            p = _props(dom)
+            assert p["np"][:, 0].tolist() == [2, 2]
+            assert p["n"][:, 0].tolist() == [8.0, 12.0]
+        dom.close()

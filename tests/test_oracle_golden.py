@@ -509,3 +509,45 @@ def test_surface_props_known_answers(orc):
     assert q[:, NP].tolist() == [1.0, 1.0]
     for k in range(1, 11):
         assert np.all(np.abs(q[:, k] - f * kept[:, k]) <= EPS2 * np.maximum(1.0, np.abs(f * kept[:, k])))
+
+
+def _two_cells_spread(orc, ar):
+    """test/test_octree_merging_1D.jl:4-44: 4 particles in each of 2 cells of a
+    unit grid, placed so that mean(x) -/+ std(x) leaves the domain."""
+    x1, x2 = [0.05, 0.05, 0.05, 0.45], [0.55, 0.95, 0.85, 0.99]
+    parts = [[2.0, 0.5, -3.0, 4.0, x, 0.0, 0.0] for x in x1] + [[3.0, 0.5, -3.0, 4.0, x, 0.0, 0.0] for x in x2]
+    o = orc.Oracle(2, 1, [ar])
+    o.pv_set(0, parts, nbuffer=0)
+    ind, nt, cg = o.pia_get()
+    ind[0, 0] = [4, 1, 4, 4, 0, -1, 0]
+    ind[0, 1] = [4, 5, 8, 4, 0, -1, 0]
+    nt[0] = 8
+    o.pia_set(ind, nt, cg)
+    return o
+
+
+def test_octree_merge_1d_keeps_particles_in_the_grid(orc, golden):
+    # test/test_octree_merging_1D.jl:46-133
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    for with_grid in (False, True):
+        o = _two_cells_spread(orc, ar)
+        oc = orc.Octree(orc.SPLIT_MID, orc.INIT_C)
+        for cell in (1, 2):
+            if with_grid:
+                o.merge_octree(oc, 0, cell, 2, L=1.0, nx=2, seed=1234, step=0)
+            else:
+                o.merge_octree(oc, 0, cell, 2, seed=1234, step=0)
+        ind, _, cg = o.pia_get()
+        assert ind[0, 0, :4].tolist() == [2, 1, 2, 2]
+        assert ind[0, 1, :4].tolist() == [2, 5, 6, 2]
+        logical, cells = o.logical(0)
+        for c in (1, 2):
+            x = logical[cells == c, 4]
+            outside = bool(np.any((x < 0.0) | (x > 1.0)))
+            assert outside == (not with_grid), (with_grid, c, x)
+        if with_grid:
+            assert cg[0] == 0  # merging leaves the indexer non-contiguous
+            o.sort(0, L=1.0, nx=2)
+            pr = o.compute_props(mode=0)
+            assert pr["np"][0].tolist() == [2, 2]
+            assert pr["n"][0].tolist() == [8.0, 12.0]
