@@ -1630,6 +1630,13 @@ void orc_sort(void* h, int32_t s, double L, int64_t nx, double wall_offset)
 void orc_squash(void* h, int32_t s) { squash_pia(*(Orc*)h, s); }
 void orc_restore_ordering(void* h, int32_t s) { restore_particle_ordering(((Orc*)h)->pv[s]); }
 void orc_delete_particle_end(void* h, int32_t s, int64_t cell) { delete_particle_end(*(Orc*)h, cell, s); }
+void orc_delete_particle_end_group(void* h, int32_t s, int64_t cell, int32_t group)
+{
+    if (group == 1)
+        delete_particle_end_group1(*(Orc*)h, cell, s);
+    else
+        delete_particle_end_group2(*(Orc*)h, cell, s);
+}
 
 void* orc_octree_create(int32_t split, int32_t init_bounds, int32_t bounds_mode, int64_t max_Nbins, int64_t max_depth)
 {

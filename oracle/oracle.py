@@ -80,6 +80,7 @@ def lib():
             "orc_squash": (None, [vp, i32]),
             "orc_restore_ordering": (None, [vp, i32]),
             "orc_delete_particle_end": (None, [vp, i32, i64]),
+            "orc_delete_particle_end_group": (None, [vp, i32, i64, i32]),
             "orc_octree_create": (vp, [i32, i32, i32, i64, i64]),
             "orc_octree_destroy": (None, [vp]),
             "orc_octree_init": (None, [vp, vp, i32, i64]),
@@ -339,6 +340,10 @@ class Oracle:
 
     def delete_particle_end(self, s, cell):
         self.L.orc_delete_particle_end(self.h, s, cell)
+
+    def delete_particle_end_group(self, s, cell, group):
+        """delete_particle_end_group1! / _group2! (particles.jl:501-566)"""
+        self.L.orc_delete_particle_end_group(self.h, s, cell, group)
 
     def convect_surf(self, s, L, nx, walls, dt, seed, step, wall_offset=1e-12):
         """convect_particles! with SurfProps (convection_1D.jl:176-206): returns

@@ -375,3 +375,60 @@ def test_close_order_is_safe(ctx):
     c2.close()
     assert not dom.h and not p.h
     del p, dom
+
+
+# ---------------------------------------------------------------- squash_pia!
+SQUASH_CASES = [
+    # (cell positions, 1-based indexer rows, deletions (cell, group or 0 for delete_particle_end!))
+    # test/test_pia_contiguous.jl:1-320
+    ([10.0] * 10, [[10, 1, 10, 10, -1, -1, 0]], [(1, 1)]),
+    ([10.0] * 10, [[10, 1, 5, 5, 6, 10, 5]], [(1, 1), (1, 2)]),
+    ([1.0, 1.0, 1.0, 2.0, 2.0, 3.0, 3.0, 1.0, 3.0, 3.0],
+     [[4, 1, 3, 3, 8, 8, 1], [2, 4, 5, 2, -1, -1, 0], [4, 6, 7, 2, 9, 10, 2]], [(1, 0), (1, 0), (1, 0), (3, 1)]),
+    ([1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0],
+     [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]], [(1, 0), (3, 0), (3, 0), (2, 1)]),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SQUASH_CASES)))
+def test_squash_known_answers_vs_oracle(ctx, orc, case):
+    """The reference's hand-built states after deletions, squashed on the
+    device (every cell into one contiguous list, logical order kept) and by
+    the oracle's squash_pia!: the same particles in the same cell order."""
+    x, rows, dels = SQUASH_CASES[case]
+    n, nc = len(x), len(rows)
+    parts = np.array([[float(i + 1), 0.0, 0.0, 0.0, x[i], 0.0, 1.0] for i in range(n)])
+    o = orc.Oracle(nc, 1, [mz.AR_MASS])
+    o.pv_set(0, parts, nbuffer=0)
+    ind, nt, cg = o.pia_get()
+    for c, r in enumerate(rows):
+        ind[0, c] = r
+    nt[0] = n
+    o.pia_set(ind, nt, cg)
+    for cell, group in dels:
+        if group:
+            o.delete_particle_end_group(0, cell, group)
+        else:
+            o.delete_particle_end(0, cell)
+    # the device gets the post-deletion state: logical position p holds
+    # particle index[p]; positions no indexer entry covers (the deleted ones,
+    # which may lie below the last position in use) are dead slots
+    pv = o.pv_get(0)
+    ind, nt, cg = o.pia_get()
+    slots = parts[pv["index"] - 1]
+    dev_rows = [[r[0], r[1] - 1, r[2] - 1, r[3], (r[4] - 1) if r[6] else 0, (r[5] - 1) if r[6] else -1, r[6]]
+                for r in ind[0]]
+    dom = mz.Domain(ctx, nc, species(["Ar"]), n + 16)
+    dom.upload_indexed(0, slots[:, 0], slots[:, 1:4], slots[:, 4:7], dev_rows)
+    cg[0] = 0
+    o.pia_set(ind, nt, cg)
+    o.squash(0)
+    dom.squash(0)
+    orows, ocells = oracle_logical(o, 0)
+    drows, dcells = device_logical(dom, 0)
+    assert np.array_equal(ocells, dcells)
+    assert np.array_equal(orows, drows)
+    dind, dnt = dom.indexer(0)
+    oind, ont, _ = o.pia_get()
+    assert dnt == ont[0] and dind[:, 0].tolist() == oind[0, :, 0].tolist()
+    dom.close()

@@ -551,3 +551,105 @@ def test_octree_merge_1d_keeps_particles_in_the_grid(orc, golden):
             pr = o.compute_props(mode=0)
             assert pr["np"][0].tolist() == [2, 2]
             assert pr["n"][0].tolist() == [8.0, 12.0]
+
+
+def _pia_state(orc, ar, n_cells, x, indexer, cell=None):
+    """ParticleVector(10) with particle i = (w i, v 0, x_i) and nbuffer set to
+    0, plus a hand-built indexer (test/test_pia_contiguous.jl)."""
+    n = len(x)
+    parts = [[float(i + 1), 0.0, 0.0, 0.0, x[i], 0.0, 1.0] for i in range(n)]
+    o = orc.Oracle(n_cells, 1, [ar])
+    o.pv_set(0, parts, cell=cell, nbuffer=0)
+    ind, nt, cg = o.pia_get()
+    for c, row in enumerate(indexer):
+        ind[0, c] = row
+    nt[0] = n
+    o.pia_set(ind, nt, cg)
+    return o
+
+
+def _mark_noncontiguous(o):
+    ind, nt, cg = o.pia_get()
+    cg[0] = 0
+    o.pia_set(ind, nt, cg)
+
+
+def test_squash_pia_known_answers(orc, golden):
+    # test/test_pia_contiguous.jl:1-320
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    cells = list(range(11, 21))
+
+    # 1 cell, 1 group: delete the last particle of group 1
+    o = _pia_state(orc, ar, 1, [10.0] * 10, [[10, 1, 10, 10, -1, -1, 0]], cell=cells)
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0, 0] == 10 and abs(pr["n"][0, 0] - 55.0) / 55.0 < 1e-15
+    o.delete_particle_end_group(0, 1, 1)
+    _mark_noncontiguous(o)
+    pv = o.pv_get(0)
+    assert pv["nbuffer"] == 1
+    freed = pv["buffer"][0]
+    o.squash(0)
+    ind, _, cg = o.pia_get()
+    assert cg[0] == 1
+    assert ind[0, 0, 3] == 9 and ind[0, 0, 2] == 9 and ind[0, 0, 6] == 0
+    pv = o.pv_get(0)
+    assert pv["cell"][:9].tolist() == cells[:9]
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0, 0] == 9 and abs(pr["n"][0, 0] - 45.0) / 45.0 < 1e-15
+    assert freed not in pv["index"][:9]
+
+    # 1 cell, 2 groups: delete the last particle of each group
+    o = _pia_state(orc, ar, 1, [10.0] * 10, [[10, 1, 5, 5, 6, 10, 5]], cell=cells)
+    o.delete_particle_end_group(0, 1, 1)
+    o.delete_particle_end_group(0, 1, 2)
+    _mark_noncontiguous(o)
+    pv = o.pv_get(0)
+    assert pv["nbuffer"] == 2
+    freed = pv["buffer"][:2].tolist()
+    o.squash(0)
+    pv = o.pv_get(0)
+    assert pv["cell"][:8].tolist() == [11, 12, 13, 14, 16, 17, 18, 19]
+    ind, _, cg = o.pia_get()
+    assert cg[0] == 1 and ind[0, 0, 3] == 4 and ind[0, 0, 2] == 4 and ind[0, 0, 6] == 4
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0, 0] == 8 and abs(pr["n"][0, 0] - 40.0) / 40.0 < 1e-15
+    assert not any(f in pv["index"][:8] for f in freed)
+
+    # 3 cells laid out 111 22 33 1 33; delete 3 from cell 1, 1 from cell 3's group 1
+    x = [1.0, 1.0, 1.0, 2.0, 2.0, 3.0, 3.0, 1.0, 3.0, 3.0]
+    o = _pia_state(orc, ar, 3, x, [[4, 1, 3, 3, 8, 8, 1], [2, 4, 5, 2, -1, -1, 0], [4, 6, 7, 2, 9, 10, 2]])
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0].tolist() == [4, 2, 4] and pr["n"][0].tolist() == [14.0, 9.0, 32.0]
+    for _ in range(3):
+        o.delete_particle_end(0, 1)
+    o.delete_particle_end_group(0, 3, 1)
+    _mark_noncontiguous(o)
+    o.squash(0)
+    ind, _, _ = o.pia_get()
+    assert ind[0, 0].tolist()[:4] == [1, 1, 1, 1] and ind[0, 0, 6] == 0
+    assert ind[0, 1].tolist()[:4] == [2, 2, 3, 2] and ind[0, 1, 6] == 0
+    assert ind[0, 2].tolist() == [3, 4, 4, 1, 5, 6, 2]
+    pv = o.pv_get(0)
+    assert not any(b in pv["index"][:6] for b in pv["buffer"][:pv["nbuffer"]])
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0].tolist() == [1, 2, 3] and pr["n"][0].tolist() == [1.0, 9.0, 25.0]
+
+    # 3 cells laid out 111 2 333 222; cell 2 ends with group 2 only
+    x = [1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0]
+    o = _pia_state(orc, ar, 3, x, [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]])
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0].tolist() == [3, 4, 3] and pr["n"][0].tolist() == [6.0, 31.0, 18.0]
+    o.delete_particle_end(0, 1)
+    o.delete_particle_end(0, 3)
+    o.delete_particle_end(0, 3)
+    o.delete_particle_end_group(0, 2, 1)
+    _mark_noncontiguous(o)
+    o.squash(0)
+    ind, _, _ = o.pia_get()
+    assert ind[0, 0].tolist()[:4] == [2, 1, 2, 2] and ind[0, 0, 6] == 0
+    assert ind[0, 1, 0] == 3 and ind[0, 1, 3] == 0 and ind[0, 1].tolist()[4:] == [4, 6, 3]
+    assert ind[0, 2].tolist()[:4] == [1, 3, 3, 1] and ind[0, 2, 6] == 0
+    pv = o.pv_get(0)
+    assert not any(i in pv["buffer"][:pv["nbuffer"]] for i in pv["index"][:6])
+    pr = o.compute_props(mode=0)
+    assert pr["np"][0].tolist() == [2, 3, 1] and pr["n"][0].tolist() == [3.0, 27.0, 5.0]
