@@ -338,6 +338,8 @@ __global__ void __launch_bounds__(256, 2) k_cell_physics(DomainView d, StepArgs 
     cell_body<G, 2>(d, a, cell_hist);
 }
 
+__global__ void k_set_step(uint32_t* step, uint32_t value) { *step = value; }
+
 // ntc_equal_weight! and the 0-D compute_props! of the cells with at least
 // a.big_cell particles, one block per cell (ntc_cell_block, props_cell_block);
 // k_cell skips these cells' collisions and props.  Blocks take the next large
@@ -575,7 +577,10 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         MZ_CK(cudaMemsetAsync(d->d_done, 0, 8 * sizeof(unsigned int), c->stream));
     }
     const uint32_t first = (uint32_t)(plan->step0 + 1);
-    MZ_CK(cudaMemcpyAsync(d->d_step, &first, sizeof first, cudaMemcpyHostToDevice, c->stream));
+    // a one-thread kernel, not a copy from pageable host memory: such a copy
+    // waits for the stream to drain, and the host would then launch the next
+    // step's kernels on an idle GPU
+    MZ_LAUNCH(c, "step_set_index", k_set_step, 1, 1, 0, d->d_step, first);
 
     StepArgs a;
     memset(&a, 0, sizeof a);
