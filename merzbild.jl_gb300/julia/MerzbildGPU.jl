@@ -34,7 +34,7 @@ export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, Dev
        avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
        DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf,
        swpm!, create_collision_factors_swpm_array!, snapshot!, snapshot_wait, unpack_snapshot!, pinned_vector,
-       free_pinned!
+       free_pinned!, DeviceServer, submit!, server_step!, request_result, retired_requests, set_lane_split!
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -552,5 +552,99 @@ function counters(dp::DeviceParticles; reset=false)
     check(ccall((:mz_get_counters, libmz), Cint, (Ptr{Cvoid}, Ref{MzCounters}, Int32), dp.ptr, c, reset), dp.ctx)
     c[]
 end
+
+# ------------------------------------------------------------------ serving
+# Continuous batching of independent 0-D relaxation requests (mz_server_*);
+# no reference counterpart: each request is the README's 0-D loop.
+struct MzRequest
+    count::NTuple{MZ_MAX_SPECIES,Int64}
+    T::NTuple{MZ_MAX_SPECIES,Float64}
+    Fnum::Float64
+    V::Float64
+    n_steps::Int64
+    seed::UInt64
+end
+
+struct MzRequestResult
+    id::Int64
+    state::Int32
+    reserved::Int32
+    steps_done::Int64
+    np::NTuple{MZ_MAX_SPECIES,Int64}
+    n::NTuple{MZ_MAX_SPECIES,Float64}
+    v::NTuple{3 * MZ_MAX_SPECIES,Float64}  # species-major: v[3(s-1) + k]
+    T::NTuple{MZ_MAX_SPECIES,Float64}
+end
+
+mutable struct DeviceServer
+    ctx::DeviceContext
+    ptr::Ptr{Cvoid}
+    n_species::Int
+end
+
+"""
+    DeviceServer(ctx, species_data, interactions, Δt, max_requests, capacity)
+
+A server for up to `max_requests` concurrent requests with `capacity`
+particles of each species in device memory.
+"""
+function DeviceServer(ctx::DeviceContext, species_data, interactions, Δt, max_requests, capacity)
+    ns = length(species_data)
+    tab = [MzInteraction(interactions[s1, s2].m_r, interactions[s1, s2].μ1, interactions[s1, s2].μ2,
+                         interactions[s1, s2].vhs_d, interactions[s1, s2].vhs_o, interactions[s1, s2].vhs_Tref,
+                         interactions[s1, s2].vhs_muref, interactions[s1, s2].vhs_factor) for s1 in 1:ns, s2 in 1:ns]
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mz_server_create, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{MzInteraction}, Float64, Int64, Ptr{Int64}, Ref{Ptr{Cvoid}}),
+                ctx.ptr, ns, [s.mass for s in species_data], tab, Δt, max_requests, fill(Int64(capacity), ns), r),
+          ctx)
+    srv = DeviceServer(ctx, r[], ns)
+    finalizer(v -> ccall((:mz_server_destroy, libmz), Cint, (Ptr{Cvoid},), v.ptr), srv)
+    srv
+end
+
+"""Queue a request (particles and temperature per species); returns its id."""
+function submit!(srv::DeviceServer, counts, T, Fnum, n_steps, seed; V=1.0)
+    pad(a, z) = ntuple(i -> i <= length(a) ? a[i] : z, MZ_MAX_SPECIES)
+    req = MzRequest(pad(Int64.(counts), Int64(0)), pad(Float64.(T), 0.0), Fnum, V, n_steps, UInt64(seed))
+    id = Ref{Int64}(0)
+    check(ccall((:mz_server_submit, libmz), Cint, (Ptr{Cvoid}, Ref{MzRequest}, Ref{Int64}), srv.ptr, req, id),
+          srv.ctx)
+    id[]
+end
+
+"""Admit, run up to `max_steps` steps, retire; returns (running, queued, retired)."""
+function server_step!(srv::DeviceServer; max_steps=16)
+    k, run, que, ret = Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0)
+    check(ccall((:mz_server_step_many, libmz), Cint,
+                (Ptr{Cvoid}, Int64, Ref{Int64}, Ref{Int64}, Ref{Int64}, Ref{Int64}), srv.ptr, max_steps, k, run, que,
+                ret), srv.ctx)
+    (run[], que[], ret[])
+end
+
+"""State of request `id` and, once done, compute_props! of its last step."""
+function request_result(srv::DeviceServer, id)
+    r = Ref{MzRequestResult}()
+    check(ccall((:mz_server_result, libmz), Cint, (Ptr{Cvoid}, Int64, Ref{MzRequestResult}), srv.ptr, id, r),
+          srv.ctx)
+    x, ns = r[], srv.n_species
+    (state=x.state, steps_done=x.steps_done, np=collect(x.np[1:ns]), n=collect(x.n[1:ns]),
+     v=[x.v[3 * (s - 1) + k] for k in 1:3, s in 1:ns], T=collect(x.T[1:ns]))
+end
+
+"""Ids of the requests the last server_step! retired."""
+function retired_requests(srv::DeviceServer)
+    n = Ref{Int64}(0)
+    check(ccall((:mz_server_retired, libmz), Cint, (Ptr{Cvoid}, Int64, Ptr{Int64}, Ref{Int64}), srv.ptr, 0,
+                C_NULL, n), srv.ctx)
+    ids = zeros(Int64, n[])
+    check(ccall((:mz_server_retired, libmz), Cint, (Ptr{Cvoid}, Int64, Ptr{Int64}, Ref{Int64}), srv.ptr, n[],
+                ids, n), srv.ctx)
+    ids
+end
+
+"""Requests of at least `particles` particles run in the lane of large requests (0: one lane)."""
+set_lane_split!(srv::DeviceServer, particles) =
+    check(ccall((:mz_server_set_lane_split, libmz), Cint, (Ptr{Cvoid}, Int64), srv.ptr, particles), srv.ctx)
 
 end # module
