@@ -38,6 +38,15 @@ def test_library_exports_every_declared_symbol(built):
     assert merzgpu.lib().mz_version() == 1
 
 
+def test_julia_binding_calls_only_declared_symbols():
+    """Every ccall in the Julia binding names an entry point of the header
+    (the binding cannot run here: no Julia toolchain)."""
+    jl = open(os.path.join(ROOT, "merzbild.jl_gb300", "julia", "MerzbildGPU.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(mz_\w+),\s*libmz\)", jl))
+    assert len(called) > 30
+    assert not called - set(declared_symbols()), sorted(called - set(declared_symbols()))
+
+
 def test_library_is_built_for_sm103a_only():
     from merzgpu import build as b
 
