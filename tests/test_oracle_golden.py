@@ -653,3 +653,32 @@ def test_squash_pia_known_answers(orc, golden):
     assert not any(i in pv["buffer"][:pv["nbuffer"]] for i in pv["index"][:6])
     pr = o.compute_props(mode=0)
     assert pr["np"][0].tolist() == [2, 3, 1] and pr["n"][0].tolist() == [3.0, 27.0, 5.0]
+
+
+RESTORE_CASES = [
+    # (index, particles written through the index, buffer, nbuffer, expected buffer head)
+    # test/test_particle_index_sorting.jl:13-168
+    (list(range(1, 11)), 10, list(range(10, 0, -1)), 10, list(range(10, 0, -1))),
+    ([5, 1, 7, 3, 2, 4, 10, 8, 6, 9], 2, [7, 3, 2, 4, 10, 8, 6, 9, 5, 1], 8, [10, 9, 8, 7, 6, 5, 4, 3]),
+    ([10, 9, 5, 6, 1, 8, 3, 7, 2, 4], 7, [4, 7, 2, 10, 9, 5, 6, 1, 8, 3], 3, [10, 9, 8]),
+    ([4, 10, 7, 3, 1, 2, 9, 8, 5, 6], 10, [4, 7, 2, 10, 9, 5, 6, 1, 8, 3], 0, []),
+    ([10, 5, 7, 6, 2, 1, 3, 5, 4, 6], 5, [3, 7, 4, 1, 9, 10, 8, 2, 6, 5], 5, [10, 9, 8, 7, 6]),
+]
+
+
+@pytest.mark.parametrize("case", range(len(RESTORE_CASES)))
+def test_restore_particle_ordering_known_answers(orc, golden, case):
+    index, n_set, buffer, nbuffer, head = RESTORE_CASES[case]
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    slots = np.zeros((10, 7))
+    for i in range(1, n_set + 1):  # particles[i] = Particle(i, [i, 2i, 3i], [-i, -4i, -5i])
+        slots[index[i - 1] - 1] = [i, i, 2 * i, 3 * i, -i, -4 * i, -5 * i]
+    o = orc.Oracle(1, 1, [ar])
+    o.pv_set(0, slots, index=index, buffer=buffer, nbuffer=nbuffer)
+    o.restore_ordering(0)
+    pv = o.pv_get(0)
+    assert pv["index"].tolist() == list(range(1, 11))
+    assert pv["nbuffer"] == nbuffer
+    assert pv["buffer"][: len(head)].tolist() == head
+    for i in range(1, n_set + 1 if nbuffer < 10 else 11):
+        assert pv["particles"][i - 1].tolist() == [i, i, 2 * i, 3 * i, -i, -4 * i, -5 * i]
