@@ -682,3 +682,47 @@ def test_restore_particle_ordering_known_answers(orc, golden, case):
     assert pv["buffer"][: len(head)].tolist() == head
     for i in range(1, n_set + 1 if nbuffer < 10 else 11):
         assert pv["particles"][i - 1].tolist() == [i, i, 2 * i, 3 * i, -i, -4 * i, -5 * i]
+
+
+def _sampled_three_cells(orc, ar, nps, Ts, Fnum):
+    o = orc.Oracle(3, 1, [ar])
+    o.pv_create(0, 700)
+    xcells = [0.0, 0.5, 1.0, 1.5]
+    for c in range(3):
+        o.sample_equal_weight(0, c + 1, nps[c], Ts[c], Fnum, box=(xcells[c], xcells[c + 1], 0, 1, 0, 1), seed=1234,
+                              step=0)
+    return o
+
+
+def test_merge_and_squash_conserve_known_answers(orc, golden):
+    # test/test_pia_contiguous.jl:324-439: cells of 100, 200 and 300 sampled
+    # particles merged to 16 (N:2 octree, middle split, bounds from C), then
+    # squashed; the temperatures are checked to 4.5 standard errors of the
+    # sample (the reference's fixed bounds are met by its own stream)
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    nps, Ts, Fnum = [100, 200, 300], [1000.0, 750.0, 600.0], 1e10
+    for split_cell3 in (False, True):
+        o = _sampled_three_cells(orc, ar, nps, Ts, Fnum)
+        if split_cell3:
+            ind, nt, cg = o.pia_get()
+            ind[0, 2] = [300, 301, 304, 4, 305, 600, 296]
+            o.pia_set(ind, nt, cg)
+        pr = o.compute_props(mode=0)
+        assert pr["np"][0].tolist() == nps
+        for c in range(3):
+            assert abs(pr["T"][0, c] - Ts[c]) / Ts[c] < 4.5 * np.sqrt(2.0 / (3.0 * nps[c]))
+        T0 = pr["T"][0].copy()
+        oc = orc.Octree(orc.SPLIT_MID, orc.INIT_C)
+        order = (3, 2, 1) if split_cell3 else (1, 2, 3)
+        expect_contiguous = (True, False, False) if split_cell3 else (False, False, False)
+        for cell, contiguous in zip(order, expect_contiguous):
+            o.merge_octree(oc, 0, cell, 16, seed=1234, step=1)
+            assert bool(o.pia_get()[2][0]) == contiguous, (split_cell3, cell)
+        o.squash(0)
+        pr = o.compute_props(mode=0)
+        assert np.all(pr["np"][0] < 30)
+        for c in range(3):
+            assert abs(pr["n"][0, c] - Fnum * nps[c]) / (Fnum * nps[c]) < 1e-15
+            assert abs(pr["T"][0, c] - T0[c]) / T0[c] < 1e-14
+        if not split_cell3:
+            assert o.pv_get(0)["nbuffer"] == int(sum(nps) - pr["np"][0].sum()) + 700 - sum(nps)
