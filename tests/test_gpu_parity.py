@@ -387,6 +387,11 @@ SQUASH_CASES = [
      [[4, 1, 3, 3, 8, 8, 1], [2, 4, 5, 2, -1, -1, 0], [4, 6, 7, 2, 9, 10, 2]], [(1, 0), (1, 0), (1, 0), (3, 1)]),
     ([1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0],
      [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]], [(1, 0), (3, 0), (3, 0), (2, 1)]),
+    # test/test_pia_contiguous.jl:440-615: cells deleted to empty
+    ([1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0],
+     [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]], [(1, 0), (1, 0), (1, 0)]),
+    ([1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0],
+     [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]], [(1, 0), (3, 0), (3, 0), (3, 0)]),
 ]
 
 

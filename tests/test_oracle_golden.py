@@ -726,3 +726,35 @@ def test_merge_and_squash_conserve_known_answers(orc, golden):
             assert abs(pr["T"][0, c] - T0[c]) / T0[c] < 1e-14
         if not split_cell3:
             assert o.pv_get(0)["nbuffer"] == int(sum(nps) - pr["np"][0].sum()) + 700 - sum(nps)
+
+
+def test_squash_pia_emptied_cells_known_answers(orc, golden):
+    # test/test_pia_contiguous.jl:440-615: layout 111 2 333 222 with cell 1,
+    # then cell 3, deleted to empty
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    x = [1.0, 1.0, 1.0, 2.0, 3.0, 3.0, 3.0, 2.0, 2.0, 2.0]
+    rows = [[3, 1, 3, 3, -1, -1, 0], [4, 4, 4, 1, 8, 10, 3], [3, 5, 7, 3, -1, -1, 0]]
+    o = _pia_state(orc, ar, 3, x, rows)
+    for _ in range(3):
+        o.delete_particle_end(0, 1)
+    _mark_noncontiguous(o)
+    o.squash(0)
+    ind, _, _ = o.pia_get()
+    assert ind[0, 0].tolist()[:4] == [0, 0, -1, 0] and ind[0, 0, 6] == 0
+    assert ind[0, 1].tolist() == [4, 1, 1, 1, 5, 7, 3]
+    assert ind[0, 2].tolist()[:4] == [3, 2, 4, 3] and ind[0, 2, 6] == 0
+
+    o = _pia_state(orc, ar, 3, x, rows)
+    o.delete_particle_end(0, 1)
+    for _ in range(3):
+        o.delete_particle_end(0, 3)
+    _mark_noncontiguous(o)
+    pv = o.pv_get(0)
+    assert pv["nbuffer"] == 4 and pv["buffer"][:4].tolist() == [3, 7, 6, 5]
+    o.squash(0)
+    ind, nt, _ = o.pia_get()
+    assert ind[0, 0].tolist()[:4] == [2, 1, 2, 2] and ind[0, 0, 6] == 0
+    assert ind[0, 1].tolist() == [4, 3, 3, 1, 4, 6, 3]
+    assert ind[0, 2].tolist()[:4] == [0, 0, -1, 0] and ind[0, 2, 6] == 0
+    pv = o.pv_get(0)
+    assert not any(i in (3, 7, 6, 5) for i in pv["index"][: nt[0]])
