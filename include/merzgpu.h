@@ -415,7 +415,8 @@ typedef struct {
 
 /* a server for up to max_requests concurrent requests of n_species species
  * (masses, interactions [s1 + n_species * s2] as mz_set_interactions), time
- * step dt, capacity[s] particles of each species in HBM */
+ * step dt; each of the two lanes holds up to max_requests requests and
+ * capacity[s] particles of each species in HBM */
 int mz_server_create(mz_ctx* ctx, int32_t n_species, const double* mass, const mz_interaction* inter, double dt,
                      int64_t max_requests, const int64_t* capacity, mz_server** out);
 int mz_server_destroy(mz_server* server);
