@@ -1,0 +1,84 @@
+"""The oracle against the analytic and equilibrium answers the reference's
+statistical tests check (test/test_bkw.jl, test/test_2species.jl), on the
+CPU: this pins the oracle's collision operator itself, independently of the
+device.  Eight independent cells are averaged, so the reference's bounds
+(met by one run of its own random stream) hold with a wide margin for any
+stream: the BKW moments' worst deviations over eight cells are about a
+fifth of the bounds."""
+import math
+
+import numpy as np
+
+import merzgpu as mz
+
+NC = 8
+
+
+def _bkw_analytic(t, magic, N):
+    # test/test_bkw.jl:22-26
+    C = 1.0 - 0.4 * np.exp(-t * magic / 6.0)
+    kk = N / 2
+    return C ** (kk - 1) * (kk - (kk - 1) * C)
+
+
+def test_oracle_bkw_moments_follow_the_analytic_solution(orc):
+    """test/test_bkw.jl:31-128: pseudo-Maxwell Ar, 20,000 particles per cell
+    sampled from the BKW distribution, ntc! and total moments every step for
+    500 steps of 0.025 t_ref; M4, M6, M8 within 5 %, 5.5 %, 15 %."""
+    d, om, tr = mz.PSEUDO_MAXWELL["Ar,Ar"]
+    n_particles, n_t, T0, n_dens = 20000, 500, 273.0, 1e23
+    sigma_ref = math.pi * d * d
+    tref = 1.0 / (n_dens * sigma_ref) / math.sqrt(2 * mz.K_B * T0 / mz.AR_MASS)
+    kappa_mult = sigma_ref * (0.5 * mz.AR_MASS / (2 * mz.K_B * T0)) ** (-0.5) / math.gamma(1.5)
+    magic = tref / (1.0 / (4 * math.pi * n_dens * kappa_mult)) / (4 * math.pi)
+    Fnum = n_dens / n_particles
+    o = orc.Oracle(NC, 1, [mz.AR_MASS])
+    o.load_interactions(d, om, tr)
+    o.pv_create(0, NC * n_particles + 64)
+    for c in range(NC):
+        o.sample_equal_weight(0, c + 1, n_particles, T0, Fnum, seed=2024, step=0, distribution=1)
+    o.cf_set_smax(0, 0, o.estimate_single(0, 0, T0, T0, Fnum))
+    dt = 0.025 * tref
+
+    def moments():
+        r = o.compute_props(mode=1, powers=[4, 6, 8, 10], Tref=T0, nthreads=8)
+        assert np.all(r["np"][0] == n_particles)
+        return r["moments"][0].mean(axis=0)
+
+    moms = [moments()]
+    for ts in range(1, n_t + 1):
+        o.ntc_cells(0, 0, dt, None, 2024, ts, equal_weight=True, nthreads=8)
+        moms.append(moments())
+    moms = np.array(moms)
+    t = np.arange(n_t + 1) * 0.025
+    for k, (N, tol) in enumerate(((4, 0.05), (6, 0.055), (8, 0.15))):
+        a = _bkw_analytic(t, magic, N)
+        rel = np.abs(a - moms[:, k]) / a
+        assert np.max(rel) < tol, f"M{N}: worst relative deviation {np.max(rel):.4f}"
+
+
+def test_oracle_two_species_relax_to_the_equilibrium_temperature(orc):
+    """test/test_2species.jl: the README case (400 Ar at 3000 K, 4000 He at
+    360 K, Fnum 5e12, dt 2.5e-3, 800 steps of ntc! for every pair) ends
+    within 12 % of T_eq = 600 K for both species; number densities and
+    counts stay exact."""
+    t = mz.VHS
+    o = orc.Oracle(NC, 2, [mz.AR_MASS, mz.HE_MASS])
+    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    counts, T0, Fnum = (400, 4000), (3000.0, 360.0), 5e12
+    for s in range(2):
+        o.pv_create(s, counts[s] * NC + 64)
+        for c in range(NC):
+            o.sample_equal_weight(s, c + 1, counts[s], T0[s], Fnum, seed=77, step=0)
+    o.estimate_sigma_g_w_max(list(T0), Fnum)
+    for step in range(1, 801):
+        for s2 in range(2):
+            for s1 in range(s2, 2):
+                o.ntc_cells(s1, s2, 2.5e-3, None, 77, step, equal_weight=True, nthreads=8)
+    r = o.compute_props(mode=0)
+    T_eq = (counts[0] * T0[0] + counts[1] * T0[1]) / (counts[0] + counts[1])
+    for s in range(2):
+        assert np.all(r["np"][s] == counts[s])
+        assert np.all(np.abs(r["n"][s] - Fnum * counts[s]) / (Fnum * counts[s]) < np.finfo(float).eps)
+        assert abs(r["T"][s].mean() - T_eq) / T_eq < 0.12, (s, r["T"][s])
