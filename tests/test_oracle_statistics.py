@@ -82,3 +82,55 @@ def test_oracle_two_species_relax_to_the_equilibrium_temperature(orc):
         assert np.all(r["np"][s] == counts[s])
         assert np.all(np.abs(r["n"][s] - Fnum * counts[s]) / (Fnum * counts[s]) < np.finfo(float).eps)
         assert abs(r["T"][s].mean() - T_eq) / T_eq < 0.12, (s, r["T"][s])
+
+
+def test_oracle_variable_weight_bkw_with_octree_merging(orc):
+    """test/test_bkw_varweight_octree.jl: the BKW case run with ntc! (weights
+    split on unequal-weight collisions) and an N:2 octree merge (middle split,
+    bin bounds from the extreme velocities, 6,000 bins) down to 8,000
+    particles whenever a cell holds more than 10,000: number density and
+    temperature conserved to round-off (the reference: 1e-11 and 5e-4 K),
+    fewer than 10,000 particles at the end, M4, M6, M8 within 2.5 %, 7.8 %,
+    21 % of the analytic solution.  Eight one-cell runs, averaged (the
+    reference's case is one cell; with several cells in one particle vector
+    its drivers squash the index between sweeps, because a split appends to
+    the cell's group 2 at the end of the vector)."""
+    d, om, tr = mz.PSEUDO_MAXWELL["Ar,Ar"]
+    n0, n_t, T0, n_dens = 20000, 500, 273.0, 1e23
+    sigma_ref = math.pi * d * d
+    tref = 1.0 / (n_dens * sigma_ref) / math.sqrt(2 * mz.K_B * T0 / mz.AR_MASS)
+    kappa_mult = sigma_ref * (0.5 * mz.AR_MASS / (2 * mz.K_B * T0)) ** (-0.5) / math.gamma(1.5)
+    magic = tref / (1.0 / (4 * math.pi * n_dens * kappa_mult)) / (4 * math.pi)
+    Fnum = n_dens / n0
+    runs = []
+    for k in range(NC):
+        seed = 900 + k
+        o = orc.Oracle(1, 1, [mz.AR_MASS])
+        o.load_interactions(d, om, tr)
+        o.pv_create(0, 2 * n0)
+        o.sample_equal_weight(0, 1, n0, T0, Fnum, seed=seed, step=0, distribution=1)
+        o.cf_set_smax(0, 0, o.estimate_single(0, 0, T0, T0, Fnum))
+        octree = orc.Octree(orc.SPLIT_MID, orc.INIT_MINMAX, max_Nbins=6000)
+
+        def props():
+            return o.compute_props(mode=1, powers=[4, 6, 8, 10], Tref=T0)
+
+        r = props()
+        T_init, n_init = r["T"][0, 0], r["n"][0, 0]
+        moms = [r["moments"][0, 0].copy()]
+        for ts in range(1, n_t + 1):
+            o.ntc_cells(0, 0, 0.025 * tref, None, seed, ts)
+            if props()["np"][0, 0] > 10000:
+                o.merge_octree(octree, 0, 1, 8000, seed=seed, step=ts)
+            r = props()
+            moms.append(r["moments"][0, 0].copy())
+        assert r["np"][0, 0] < 10000
+        assert abs(r["n"][0, 0] / n_init - 1.0) < 1e-11
+        assert abs(r["T"][0, 0] - T_init) < 5e-4
+        runs.append(np.array(moms))
+    moms = np.mean(runs, axis=0)
+    t = np.arange(n_t + 1) * 0.025
+    for k, (N, tol) in enumerate(((4, 0.025), (6, 0.078), (8, 0.21))):
+        a = _bkw_analytic(t, magic, N)
+        rel = np.abs(a - moms[:, k]) / a
+        assert np.max(rel) < tol, f"M{N}: worst relative deviation {np.max(rel):.4f}"
