@@ -134,3 +134,52 @@ def test_oracle_variable_weight_bkw_with_octree_merging(orc):
         a = _bkw_analytic(t, magic, N)
         rel = np.abs(a - moms[:, k]) / a
         assert np.max(rel) < tol, f"M{N}: worst relative deviation {np.max(rel):.4f}"
+
+
+def test_oracle_swpm_bkw_with_octree_merging(orc):
+    """test/test_bkw_varweight_octree_swpm.jl: the BKW case run with swpm!
+    (G = 1: every collision transfers weight and adds two particles;
+    (sigma g)_max estimated with Fnum = 1) and the same octree merging down
+    to 8,000 above 10,000 particles: density and temperature conserved to
+    round-off, M4, M6, M8 within 2 %, 7 %, 15 % of the analytic solution.
+    Eight one-cell runs, averaged; the merged runs keep a systematic M4
+    deviation of about 1.4 % (sixteen runs give the same), inside the bound."""
+    d, om, tr = mz.PSEUDO_MAXWELL["Ar,Ar"]
+    n0, n_t, T0, n_dens = 20000, 500, 273.0, 1e23
+    sigma_ref = math.pi * d * d
+    tref = 1.0 / (n_dens * sigma_ref) / math.sqrt(2 * mz.K_B * T0 / mz.AR_MASS)
+    kappa_mult = sigma_ref * (0.5 * mz.AR_MASS / (2 * mz.K_B * T0)) ** (-0.5) / math.gamma(1.5)
+    magic = tref / (1.0 / (4 * math.pi * n_dens * kappa_mult)) / (4 * math.pi)
+    Fnum = n_dens / n0
+    runs = []
+    for k in range(NC):
+        seed = 100 + k
+        o = orc.Oracle(1, 1, [mz.AR_MASS])
+        o.load_interactions(d, om, tr)
+        o.pv_create(0, 2 * n0)
+        o.sample_equal_weight(0, 1, n0, T0, Fnum, seed=seed, step=0, distribution=1)
+        o.cf_set_smax(0, 0, o.estimate_single(0, 0, T0, T0, 1.0))
+        octree = orc.Octree(orc.SPLIT_MID, orc.INIT_MINMAX, max_Nbins=6000)
+
+        def props():
+            return o.compute_props(mode=1, powers=[4, 6, 8, 10], Tref=T0)
+
+        r = props()
+        T_init, n_init = r["T"][0, 0], r["n"][0, 0]
+        moms = [r["moments"][0, 0].copy()]
+        for ts in range(1, n_t + 1):
+            o.swpm(0, 1, 1.0, 0.025 * tref, 1.0, seed, ts)
+            if props()["np"][0, 0] > 10000:
+                o.merge_octree(octree, 0, 1, 8000, seed=seed, step=ts)
+            r = props()
+            moms.append(r["moments"][0, 0].copy())
+        assert r["np"][0, 0] < 10000
+        assert abs(r["n"][0, 0] / n_init - 1.0) < 1e-11
+        assert abs(r["T"][0, 0] - T_init) < 5e-4
+        runs.append(np.array(moms))
+    moms = np.mean(runs, axis=0)
+    t = np.arange(n_t + 1) * 0.025
+    for k, (N, tol) in enumerate(((4, 0.02), (6, 0.07), (8, 0.15))):
+        a = _bkw_analytic(t, magic, N)
+        rel = np.abs(a - moms[:, k]) / a
+        assert np.max(rel) < tol, f"M{N}: worst relative deviation {np.max(rel):.4f}"
