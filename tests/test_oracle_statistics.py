@@ -183,3 +183,45 @@ def test_oracle_swpm_bkw_with_octree_merging(orc):
         a = _bkw_analytic(t, magic, N)
         rel = np.abs(a - moms[:, k]) / a
         assert np.max(rel) < tol, f"M{N}: worst relative deviation {np.max(rel):.4f}"
+
+
+def test_oracle_two_species_variable_weight_with_merging(orc):
+    """test/test_2species_varweight_octree.jl: Ar (2e15, 3000 K, Fnum 5e11:
+    4,000 particles) and He (2e16, 360 K, Fnum 5e12: 4,000 particles) in one
+    cell of 1 m^3, ntc! for every pair (unequal weights split), each species
+    merged back to its initial count (octree, middle split, bounds from the
+    extreme velocities, 6,000 bins) when it exceeds 1.2x that count, 800
+    steps of 2.5e-3: number densities conserved to round-off, both species
+    within 5.5 % of T_eq = 600 K.  Eight one-cell runs, temperatures averaged."""
+    t = mz.VHS
+    n_Ar, n_He, T0 = 2e15, 2e16, (3000.0, 360.0)
+    F = (5e11, 5e12)
+    counts = (round(n_Ar / F[0]), round(n_He / F[1]))
+    T_eq = (n_Ar * T0[0] + n_He * T0[1]) / (n_Ar + n_He)
+    T_end, merges = [], 0
+    for k in range(NC):
+        seed = 300 + k
+        o = orc.Oracle(1, 2, [mz.AR_MASS, mz.HE_MASS])
+        o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                            [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+        for s in range(2):
+            o.pv_create(s, 4 * counts[s])
+            o.sample_equal_weight(s, 1, counts[s], T0[s], F[s], seed=seed, step=0)
+        o.estimate_sigma_g_w_max(list(T0), list(F))
+        octree = orc.Octree(orc.SPLIT_MID, orc.INIT_MINMAX, max_Nbins=6000)
+        for step in range(1, 801):
+            for s2 in range(2):
+                for s1 in range(s2, 2):
+                    o.ntc_cells(s1, s2, 2.5e-3, None, seed, step)
+            ind, _, _ = o.pia_get()
+            for s in range(2):
+                if ind[s, 0, 0] > round(1.2 * counts[s]):
+                    o.merge_octree(octree, s, 1, counts[s], seed=seed, step=step)
+                    merges += 1
+        r = o.compute_props(mode=0)
+        assert abs(r["n"][0, 0] - n_Ar) / n_Ar < 2e-15
+        assert abs(r["n"][1, 0] - n_He) / n_He < 6e-15
+        T_end.append(r["T"][:, 0].copy())
+    assert merges > 0
+    T_end = np.mean(T_end, axis=0)
+    assert np.all(np.abs(T_end - T_eq) / T_eq < 0.055), (T_end, T_eq)
