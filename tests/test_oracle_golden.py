@@ -227,6 +227,31 @@ def test_collide_vhs_split_semantics(orc, golden, w1, w2, dw_tol, expect_split):
     assert abs(_kinetic(logical, ar) - ke0) <= 1e-14
 
 
+@pytest.mark.parametrize("w1,w2", [(1.0, 1.0), (2.0, 1.0), (1.0, 2.0)])
+def test_collide_vhs_equal_weight_known_answers(orc, golden, w1, w2):
+    # test/test_collision_vhs_equal_weight.jl: the equal-weight collision
+    # never splits, whatever the weights, and conserves the weighted energy
+    ar = golden["species"]["Ar"]["mass"]
+    o = orc.Oracle(1, 1, [ar])
+    o.load_interactions(*golden["vhs"]["Ar,Ar"])
+    parts = np.array([[w1, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0], [w2, -1.0, 0.0, 0.0, 0.0, 0.0, 0.0]])
+    o.pv_set(0, parts, nbuffer=0)
+    ind, nt, cg = o.pia_get()
+    nt[0] = 2
+    ind[0, 0] = [2, 1, 2, 2, 0, -1, 0]
+    o.pia_set(ind, nt, cg)
+    o.cf_set_smax(0, 0, 0.0)
+    ke0 = _kinetic(parts, ar)
+    o.collide_vhs(0, 0, 1, 1, 2, seed=1234, equal_weight=True)
+    _, cnt = o.cf_get(0, 0)
+    assert cnt[0, 3] > 0 and cnt[0, 4] == cnt[0, 3]
+    _, nt, _ = o.pia_get()
+    assert nt[0] == 2
+    logical, _ = o.logical(0)
+    assert logical[:, 0].tolist() == [w1, w2]
+    assert abs(_kinetic(logical, ar) - ke0) <= 1e-14
+
+
 def _merge_state(orc, parts, ar, indexer=None):
     parts = np.array(parts)
     n = parts.shape[0]
