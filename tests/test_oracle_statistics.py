@@ -225,3 +225,26 @@ def test_oracle_two_species_variable_weight_with_merging(orc):
     assert merges > 0
     T_end = np.mean(T_end, axis=0)
     assert np.all(np.abs(T_end - T_eq) / T_eq < 0.055), (T_end, T_eq)
+
+
+def test_oracle_maxwellian_sampler(orc):
+    """test/test_sampling.jl: 20,000 particles sampled in a 0.5 x 1 x 2 box
+    from Maxwellians (273 K at rest, 1000 K drifting at (20, -10, 30) m/s,
+    500 K at (3000, 2000, -1000) m/s): number density exact, positions in the
+    box, moments M4, M6, M8 within 5 %, 5 %, 12 % of the Maxwellian's, mean
+    velocity and temperature to 4.5 standard errors of the sample (the
+    reference's 10 m/s and 1 % sit at about 3 and 1.6 standard errors)."""
+    N, n_dens = 20000, 1e20
+    for v0, T0 in zip([(0.0, 0.0, 0.0), (20.0, -10.0, 30.0), (3000.0, 2000.0, -1000.0)], [273.0, 1000.0, 500.0]):
+        o = orc.Oracle(1, 1, [mz.AR_MASS])
+        o.pv_create(0, N + 8)
+        o.sample_equal_weight(0, 1, N, T0, n_dens / N, box=(0.0, 0.5, 0.0, 1.0, 0.0, 2.0), seed=1234, step=0, v0=v0)
+        r = o.compute_props(mode=1, powers=[4, 6, 8], Tref=T0)
+        assert abs(r["n"][0, 0] - n_dens) / n_dens < np.finfo(float).eps
+        sv = math.sqrt(mz.K_B * T0 / mz.AR_MASS / N)
+        assert np.all(np.abs(r["v"][0, 0] - np.array(v0)) < 4.5 * sv)
+        assert abs(r["T"][0, 0] / T0 - 1.0) < 4.5 * math.sqrt(2.0 / (3.0 * N))
+        for m, tol in zip(r["moments"][0, 0], (0.05, 0.05, 0.12)):
+            assert abs(m - 1.0) < tol
+        x = o.logical(0)[0][:, 4:7]
+        assert np.all((x >= 0.0) & (x <= np.array([0.5, 1.0, 2.0])))
