@@ -96,3 +96,24 @@ def test_oracle_is_not_imported_by_the_product():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".jl")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in re.sub(r"#.*|//.*", "", txt).lower() or f == "build.py", f
+
+
+def test_collisional_props_known_answers():
+    """test/test_collisional_props_computes.jl: mean free path and collision
+    frequency of VHS argon at 1e23 m^-3 and 300 K (bit-exact values), their
+    monotonicity in T and linear scaling in n, and the temperature-independent
+    mean free path of a hard-sphere gas (omega = 0.5)."""
+    import merzgpu as mz
+
+    sp = [mz.Species("Ar", mz.AR_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    mfp1 = mz.mean_free_path(inter, 0, 1e23, 300.0)
+    cf1 = mz.mean_collision_frequency(inter, sp, 0, 1e23, 300.0)
+    assert abs(mfp1 - 1.371982759796177e-5) <= 2 * np.finfo(float).eps
+    assert abs(cf1 - 2.907146431686186e7) <= 2 * np.finfo(float).eps
+    assert mz.mean_free_path(inter, 0, 1e23, 500.0) > mfp1
+    assert mz.mean_collision_frequency(inter, sp, 0, 1e23, 500.0) > cf1
+    assert abs(mz.mean_free_path(inter, 0, 2e23, 300.0) / mfp1 - 0.5) <= 2 * np.finfo(float).eps
+    assert abs(mz.mean_collision_frequency(inter, sp, 0, 2e23, 300.0) / cf1 - 2.0) <= 2 * np.finfo(float).eps
+    hs = mz.interactions_from_vhs(sp, {"Ar,Ar": (4.11e-10, 0.5, 300.0)})
+    assert abs(mz.mean_free_path(hs, 0, 1e23, 300.0) - mz.mean_free_path(hs, 0, 1e23, 5000.0)) <= 2 * np.finfo(float).eps
