@@ -1630,6 +1630,11 @@ void orc_sort(void* h, int32_t s, double L, int64_t nx, double wall_offset)
 void orc_squash(void* h, int32_t s) { squash_pia(*(Orc*)h, s); }
 void orc_restore_ordering(void* h, int32_t s) { restore_particle_ordering(((Orc*)h)->pv[s]); }
 void orc_delete_particle_end(void* h, int32_t s, int64_t cell) { delete_particle_end(*(Orc*)h, cell, s); }
+// map_cont_index (particles.jl:364-366): 0-based position within the cell's
+// particles -> position in the index array (1-based)
+int64_t orc_map_cont_index(void* h, int32_t s, int64_t cell, int64_t i) { return map_cont_index(((Orc*)h)->pi(cell, s), i); }
+// update_particle_indexer_new_particle! (particles.jl:426-433)
+void orc_indexer_new_particle(void* h, int32_t s, int64_t cell) { update_particle_indexer_new_particle(*(Orc*)h, cell, s); }
 void orc_delete_particle_end_group(void* h, int32_t s, int64_t cell, int32_t group)
 {
     if (group == 1)

@@ -81,6 +81,8 @@ def lib():
             "orc_restore_ordering": (None, [vp, i32]),
             "orc_delete_particle_end": (None, [vp, i32, i64]),
             "orc_delete_particle_end_group": (None, [vp, i32, i64, i32]),
+            "orc_map_cont_index": (i64, [vp, i32, i64, i64]),
+            "orc_indexer_new_particle": (None, [vp, i32, i64]),
             "orc_octree_create": (vp, [i32, i32, i32, i64, i64]),
             "orc_octree_destroy": (None, [vp]),
             "orc_octree_init": (None, [vp, vp, i32, i64]),
@@ -340,6 +342,14 @@ class Oracle:
 
     def delete_particle_end(self, s, cell):
         self.L.orc_delete_particle_end(self.h, s, cell)
+
+    def map_cont_index(self, s, cell, i):
+        """map_cont_index (particles.jl:364-366), cell 1-based, i 0-based"""
+        return self.L.orc_map_cont_index(self.h, s, cell, i)
+
+    def indexer_new_particle(self, s, cell):
+        """update_particle_indexer_new_particle! (particles.jl:426-433)"""
+        self.L.orc_indexer_new_particle(self.h, s, cell)
 
     def delete_particle_end_group(self, s, cell, group):
         """delete_particle_end_group1! / _group2! (particles.jl:501-566)"""

@@ -783,3 +783,30 @@ def test_squash_pia_emptied_cells_known_answers(orc, golden):
     assert ind[0, 2].tolist()[:4] == [0, 0, -1, 0] and ind[0, 2, 6] == 0
     pv = o.pv_get(0)
     assert not any(i in (3, 7, 6, 5) for i in pv["index"][: nt[0]])
+
+
+def test_indexer_known_answers(orc, golden):
+    # test/test_indexing.jl:1-63: appends go to group 2; map_cont_index walks
+    # group 1, then group 2
+    ar = scenario(golden, "octree_merge_24")["mass"]
+    o = orc.Oracle(1, 1, [ar])
+    o.pv_create(0, 64)
+    ind, nt, cg = o.pia_get()
+    ind[0, 0] = [20, 1, 20, 20, 0, -1, 0]
+    nt[0] = 20
+    o.pia_set(ind, nt, cg)
+    o.indexer_new_particle(0, 1)
+    o.indexer_new_particle(0, 1)
+    ind, nt, _ = o.pia_get()
+    assert nt[0] == 22 and ind[0, 0].tolist() == [22, 1, 20, 20, 21, 22, 2]
+
+    ind[0, 0] = [15, 1, 10, 10, 31, 35, 5]
+    nt[0] = 15
+    o.pia_set(ind, nt, cg)
+    assert [o.map_cont_index(0, 1, i0 - 1) for i0 in (1, 4, 10)] == [1, 4, 10]
+    assert [o.map_cont_index(0, 1, i0 - 1) for i0 in (11, 12, 15)] == [31 + i0 - 10 - 1 for i0 in (11, 12, 15)]
+    ind[0, 0] = [10, 24, 28, 5, 31, 35, 5]
+    nt[0] = 10
+    o.pia_set(ind, nt, cg)
+    assert [o.map_cont_index(0, 1, i0 - 1) for i0 in (1, 4, 5)] == [24 + i0 - 1 for i0 in (1, 4, 5)]
+    assert [o.map_cont_index(0, 1, i0 - 1) for i0 in (6, 8, 10)] == [31 + i0 - 5 - 1 for i0 in (6, 8, 10)]
