@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MZ_ABI_VERSION 1
+#define MZ_ABI_VERSION 2
 #define MZ_MAX_SPECIES 4
 
 enum {
@@ -109,7 +109,9 @@ typedef struct {
 typedef struct {
     int32_t dims;         /* 0: 0D cells (no convection, no sort); 1: 1D grid */
     int32_t collide;      /* 1: run NTC each step */
-    int32_t equal_weight; /* 1: ntc_equal_weight!; 0: ntc! (requires 0D or no splits in flight) */
+    int32_t equal_weight; /* 1: ntc_equal_weight!; 0: ntc! with weight splitting and octree merging
+                             (merge_* below); one species runs device-resident and graph-replayed,
+                             a mixture runs the standalone entry points step by step */
     int32_t props;        /* 1: compute props at the end of every step */
     int64_t avg_start;    /* 1-based step of this call from which props are averaged; <= 0: never */
     int64_t n_avg;        /* avg_props! denominator */
@@ -123,6 +125,21 @@ typedef struct {
     mz_walls1d walls;
     int32_t launches;     /* 1-D: launches per step, 1 (fused) or 2 (sort + gather + props, then NTC +
                              convection); 0: the autotuner's choice, else 1.  Results do not depend on it */
+    int64_t hit_queue_capacity; /* 1-D: entries of the queue of particles that reach a wall (0: a
+                                   sixteenth of the particles, at least 4,096); particles beyond it are
+                                   reflected inside the step kernel.  Results do not depend on it */
+    /* equal_weight = 0: the variable-weight loop of
+     * simulations/1D/couette_varweight_octree.jl:85-135 (dims = 1) and of the
+     * 0-D variable-weight tests -- per cell ntc! with splitting, then
+     * merge_octree_N2_based! of the cells holding more than merge_threshold
+     * particles down to merge_target (1-D: positions clamped to the grid) --
+     * before convection (1-D), sort and props.  merge_threshold <= 0: no
+     * merging.  A step that would overflow the storage is abandoned before it
+     * changes a particle; the call grows the storage (mz_domain_reserve) and
+     * resumes, so results equal an uninterrupted run. */
+    int64_t merge_threshold;
+    int64_t merge_target;
+    mz_octree_params octree;
 } mz_step_plan;
 
 /* ---------------------------------------------------------------- context */
@@ -416,7 +433,13 @@ typedef struct {
 /* a server for up to max_requests concurrent requests of n_species species
  * (masses, interactions [s1 + n_species * s2] as mz_set_interactions), time
  * step dt; each of the two lanes holds up to max_requests requests and
- * capacity[s] particles of each species in HBM */
+ * capacity[s] particles of each species in HBM.  capacity[s] = 0 (any
+ * species) admits by free device memory instead: a lane's storage grows when
+ * an admission needs it and cudaMemGetInfo's free bytes, less the headroom
+ * (mz_server_set_hbm_headroom, 2 GiB by default), hold the larger storage
+ * (144 bytes per particle); a request that does not fit waits in its lane's
+ * queue, and only a request larger than the whole device memory less the
+ * headroom is refused at submission. */
 int mz_server_create(mz_ctx* ctx, int32_t n_species, const double* mass, const mz_interaction* inter, double dt,
                      int64_t max_requests, const int64_t* capacity, mz_server** out);
 int mz_server_destroy(mz_server* server);
@@ -444,6 +467,8 @@ int mz_server_info(mz_server* server, int64_t* steps_run, int64_t* particle_step
  * the lane of large requests; 0 puts all requests in one lane.  Applies to
  * requests submitted afterwards.  Results do not depend on the lane. */
 int mz_server_set_lane_split(mz_server* server, int64_t particles);
+/* device memory admission by free memory keeps free (capacity 0 at creation) */
+int mz_server_set_hbm_headroom(mz_server* server, int64_t bytes);
 
 /* Choose the fused step's mapping by timing it: every combination of lanes
  * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the
@@ -469,6 +494,25 @@ int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
  * uniform draw's mantissa).  Host arrays of n elements; for accuracy tests. */
 int mz_sincos_2pi(mz_ctx* ctx, int64_t n, const uint64_t* m, double* s, double* c);
 
+/* ---------------------------------------------------------------- validators */
+/* The reference's indexing checks (particles.jl:805-1025) on the device
+ * layout of one species.  mode 0: check_pia_is_correct -- every cell's groups
+ * have non-negative sizes and lie inside the slots in use, and the cells'
+ * counts add up to n_total; *ok = 0 with *detail = the first bad cell
+ * (1-based) or 0 for a wrong total.  mode 1: check_unique_index -- *ok = 0
+ * when a slot is listed by more than one group (*detail = the largest count,
+ * negated when free slots are listed as well) or a group lists a free slot
+ * (*detail = -1).  mode 2: check_unique_buffer -- free slots are marked slot by
+ * slot, so this always holds.  modes 3 and 4: count_disordered_particles with
+ * and without per-cell offsets (use_offset), the count in *detail. */
+int mz_check_indexing(mz_domain* dom, int32_t species, int32_t mode, int32_t* ok, int64_t* detail);
+/* Write a species' indexer as given (a ParticleIndexerArray edited by hand,
+ * as the reference's tests do): groups must lie inside the slots in use and
+ * list no more particles than the storage holds; overlaps, free slots in
+ * groups and an n_total that disagrees are accepted and left to the checks
+ * above. */
+int mz_set_indexer(mz_domain* dom, int32_t species, const mz_particle_indexer* indexer, int64_t n_total);
+
 /* ---------------------------------------------------------------- no-allocation sort */
 /* Largest n_cells mz_sort_keys_noalloc accepts.  Its scratch (per-cell counts
  * and cursors, 2 * 4 B per cell, 2 MiB) is a static device array that every
@@ -484,12 +528,14 @@ int mz_sincos_2pi(mz_ctx* ctx, int64_t n, const uint64_t* m, double* s, double* 
  * reported as MZ_E_STATE), d_perm[n] receives for every sorted position the
  * index of the key that lands there (stable: equal keys keep their order),
  * d_cell_start[n_cells + 1] the exclusive prefix of the per-cell counts.
- * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it
- * before returning.  Allocates nothing: the per-cell counters live in a
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and, before
+ * returning, waits for that stream (not for the whole device) to read the
+ * out-of-range-key word.  Allocates nothing: the per-cell counters live in a
  * static device array shared by every call, cleared at the start of each
  * call; calls that overlap on the GPU race on it, so serialise them.  The
- * first call on a device looks up that array's device address (with the
- * device current); make that first call before any stream capture. */
+ * first call on a device -- and the first after that device's context was
+ * reset -- looks up that array's device address (with the device current);
+ * make that first call before any stream capture. */
 int mz_sort_keys_noalloc(void* stream, const int32_t* d_keys, int64_t n, int32_t n_cells, int32_t* d_perm,
                          int32_t* d_cell_start);
 

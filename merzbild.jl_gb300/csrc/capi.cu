@@ -420,6 +420,8 @@ int mz_domain_destroy(mz_domain* d)
     cudaFree(d->d_step);
     cudaFree(d->d_done);
     cudaFree(d->d_hitq);
+    cudaFree(d->d_vw);
+    cudaFreeHost(d->h_vw);
     cudaFreeHost(d->h_scalar);
     delete d;
     return MZ_OK;

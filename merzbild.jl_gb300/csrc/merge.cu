@@ -61,6 +61,12 @@ struct MergeArgs {
     int64_t* deleted;  // total particles deleted
     int64_t* merged;   // cells merged
     unsigned int* next;  // cell counter of the warps
+    // fused step: the RNG step index in device memory (nullptr: `step`), an
+    // abort word (nonzero: the step was abandoned before it changed any
+    // particle, do nothing) and the particle count the scratch slices hold
+    const uint32_t* step_ptr;
+    const int* abort;
+    int32_t nmax;
 };
 
 __device__ __forceinline__ double warp_min(double v)
@@ -508,6 +514,8 @@ __device__ void merge_cell(const DomainView& d, const MergeArgs& a, int c, char*
 // the range, and each merge a long chain) spread evenly over the warps.
 __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
 {
+    if (a.abort && *a.abort) return;
+    if (a.step_ptr) a.step = *a.step_ptr;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     char* base = a.scratch + (size_t)warp * a.stride;
@@ -521,6 +529,10 @@ __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
                 const Indexer p = d.sp[a.s].ind[q];
                 const int n = p.n1 + p.n2;
                 if (n > 0 && (a.threshold < 0 || n > a.threshold)) {
+                    if (n > a.nmax) {  // larger than the scratch slices: leave the cell
+                        set_status(d, ST_CAPACITY);
+                        continue;
+                    }
                     c = q;
                     break;
                 }
@@ -554,18 +566,103 @@ __global__ void k_merge_sizes(DomainView d, int s, int cb, int ce, int64_t thres
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-}  // namespace
-
-void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
-                  const mz_octree_params* prm, const mz_grid1d* g, uint64_t step, int64_t* n_merged)
+// per-warp scratch layout for cells of up to nmax particles
+void merge_layout(MergeArgs& a, int64_t nmax, int64_t target, int32_t max_Nbins)
 {
-    mz_ctx* c = d->ctx;
+    const int64_t outmax = std::max<int64_t>(target, 2);
+    size_t off = align256((size_t)max_Nbins * sizeof(MergeBin));
+    a.off_pis = off;
+    off += align256(nmax * sizeof(int32_t));
+    a.off_tmp = off;
+    off += align256(nmax * sizeof(int32_t));
+    a.off_w = off;
+    off += align256(nmax * sizeof(double));
+    a.off_tw = off;
+    off += align256(nmax * sizeof(double));
+    a.off_lv = off;
+    off += align256(nmax * sizeof(PV));
+    a.off_lx = off;
+    off += align256(nmax * sizeof(PX));
+    a.off_oct = off;
+    off += align256(nmax);
+    a.off_ov = off;
+    off += align256(outmax * sizeof(PV));
+    a.off_ox = off;
+    off += align256(outmax * sizeof(PX));
+    a.stride = off;
+    a.nmax = (int32_t)nmax;
+}
+
+void check_octree(const mz_octree_params* prm, int64_t target)
+{
     MZ_REQUIRE(prm->split == 1, "mz_merge_octree_n2: only OctreeBinMidSplit (split = 1) is implemented");
     MZ_REQUIRE(prm->init_bin_bounds >= 1 && prm->init_bin_bounds <= 3, "mz_merge_octree_n2: bad init_bin_bounds");
     MZ_REQUIRE(prm->bin_bounds_compute == 1 || prm->bin_bounds_compute == 2,
                "mz_merge_octree_n2: bad bin_bounds_compute");
     MZ_REQUIRE(prm->max_Nbins >= 8, "mz_merge_octree_n2: max_Nbins must be at least 8 (one split)");
     MZ_REQUIRE(target <= (1 << 30), "mz_merge_octree_n2: target_np too large");
+}
+
+void ensure_merge_scratch(mz_domain* d, size_t need)
+{
+    if (need <= d->merge_scratch_bytes) return;
+    cudaFree(d->d_merge_scratch);
+    d->d_merge_scratch = nullptr;
+    d->merge_scratch_bytes = 0;
+    MZ_CK(cudaMalloc(&d->d_merge_scratch, need));
+    d->merge_scratch_bytes = need;
+}
+
+}  // namespace
+
+int merge_fused_warps(mz_domain* d) { return d->ctx->num_sms * 2; }
+
+void merge_fused_reserve(mz_domain* d, int64_t nmax, int64_t target, const mz_octree_params* prm)
+{
+    check_octree(prm, target);
+    MergeArgs a;
+    memset(&a, 0, sizeof a);
+    merge_layout(a, nmax, target, prm->max_Nbins);
+    ensure_merge_scratch(d, (size_t)merge_fused_warps(d) * a.stride);
+}
+
+void launch_merge_fused(mz_domain* d, int s, int64_t threshold, int64_t target, const mz_octree_params* prm,
+                        const mz_grid1d* g, const uint32_t* step_ptr, const int* abort, int64_t nmax,
+                        long long* words3)
+{
+    mz_ctx* c = d->ctx;
+    MergeArgs a;
+    memset(&a, 0, sizeof a);
+    a.s = s;
+    a.cb = 0;
+    a.ce = (int)d->n_cells;
+    a.threshold = threshold;
+    a.target = (int32_t)target;
+    a.prm = *prm;
+    a.clamp = g != nullptr;
+    if (g) {
+        a.min_x = g->min_x;
+        a.max_x = g->max_x;
+    }
+    merge_layout(a, nmax, target, prm->max_Nbins);
+    const int warps = merge_fused_warps(d);
+    MZ_REQUIRE((size_t)warps * a.stride <= d->merge_scratch_bytes, "merge: scratch not reserved");
+    a.scratch = static_cast<char*>(d->d_merge_scratch);
+    a.deleted = reinterpret_cast<int64_t*>(words3);
+    a.merged = reinterpret_cast<int64_t*>(words3 + 1);
+    a.next = reinterpret_cast<unsigned int*>(words3 + 2);
+    a.step_ptr = step_ptr;
+    a.abort = abort;
+    DomainView v = make_view(d);
+    MZ_CK(cudaMemsetAsync(a.next, 0, sizeof(unsigned int), c->stream));
+    MZ_LAUNCH(c, "merge", k_merge, warps, 32, 0, v, a);
+}
+
+void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
+                  const mz_octree_params* prm, const mz_grid1d* g, uint64_t step, int64_t* n_merged)
+{
+    mz_ctx* c = d->ctx;
+    check_octree(prm, target);
     if (n_merged) *n_merged = 0;
     if (ce <= cb) return;
     DomainView v = make_view(d);
@@ -592,39 +689,12 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
         a.max_x = g->max_x;
     }
     a.step = (uint32_t)step;
-    const int64_t outmax = std::max<int64_t>(target, 2);
-    size_t off = align256((size_t)prm->max_Nbins * sizeof(MergeBin));
-    a.off_pis = off;
-    off += align256(nmax * sizeof(int32_t));
-    a.off_tmp = off;
-    off += align256(nmax * sizeof(int32_t));
-    a.off_w = off;
-    off += align256(nmax * sizeof(double));
-    a.off_tw = off;
-    off += align256(nmax * sizeof(double));
-    a.off_lv = off;
-    off += align256(nmax * sizeof(PV));
-    a.off_lx = off;
-    off += align256(nmax * sizeof(PX));
-    a.off_oct = off;
-    off += align256(nmax);
-    a.off_ov = off;
-    off += align256(outmax * sizeof(PV));
-    a.off_ox = off;
-    off += align256(outmax * sizeof(PX));
-    a.stride = off;
+    merge_layout(a, nmax, target, prm->max_Nbins);
     // one warp per block: the merging warps spread over all SMs (a merge is a
     // long sequential chain; SMs shared by several merging warps slow each)
     const int warps_wanted = (int)std::min<int64_t>(ncells, (int64_t)c->num_sms * 16);
     const int blocks = std::max(1, warps_wanted);
-    const size_t need = (size_t)blocks * a.stride;
-    if (need > d->merge_scratch_bytes) {
-        cudaFree(d->d_merge_scratch);
-        d->d_merge_scratch = nullptr;
-        d->merge_scratch_bytes = 0;
-        MZ_CK(cudaMalloc(&d->d_merge_scratch, need));
-        d->merge_scratch_bytes = need;
-    }
+    ensure_merge_scratch(d, (size_t)blocks * a.stride);
     a.scratch = static_cast<char*>(d->d_merge_scratch);
     a.deleted = d->d_scalar + 2;
     a.merged = d->d_scalar + 3;

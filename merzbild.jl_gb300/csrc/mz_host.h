@@ -78,6 +78,25 @@ struct SpeciesHost {
     mz::Indexer* ind = nullptr;
 };
 
+// Device words of the fused variable-weight step.  Slot counts live on the
+// device there (the host learns them at the end of the call); a step that
+// would overflow the particle storage or the merge scratch is abandoned
+// before it changes any particle: `abort` is set, every later kernel of the
+// call returns at once, and the host grows the storage and resumes.
+enum : int { VW_CAPACITY = 1, VW_SCRATCH = 2 };
+struct VwSpecies {
+    long long hw;        // slots in use at the start of a step (the live count after the last sort)
+    long long hw_split;  // slots in use after this step's split reservations
+    long long need;      // slots the abandoned step needed (VW_CAPACITY)
+    long long merge[3];  // merge kernel: particles deleted, cells merged, cell counter
+};
+struct VwDev {
+    VwSpecies sp[MZ_MAX_SPECIES];
+    int abort;             // VW_* reasons
+    int pad;
+    long long need_cell;   // particles of the largest cell the merge scratch must hold (VW_SCRATCH)
+};
+
 struct mz_domain_s {
     mz_ctx* ctx = nullptr;
     int64_t n_cells = 0;
@@ -114,6 +133,10 @@ struct mz_domain_s {
     int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
     int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
     int32_t tuned_split = 0;    // 1-D: 1 = gather + props and NTC + convection in two launches
+    // fused variable-weight step
+    VwDev* d_vw = nullptr;
+    VwDev* h_vw = nullptr;      // pinned mirror
+    int64_t vw_nmax = 0;        // particles per cell the merge scratch holds
 };
 
 // SurfProps of a domain's 1-D walls (surface_props.jl:22-67): device sums
@@ -174,7 +197,8 @@ void launch_compact(mz_domain* d, int s);
 // also zeroes fill and counts), the total into total_out
 void launch_scan_cells(mz_domain* d, int32_t* counts, mz::Indexer* ind, int32_t* fill, int64_t* total_out,
                        bool write_indexer, int32_t* base_out, int64_t base_offset,
-                       const mz::Indexer* nlocal_from = nullptr);
+                       const mz::Indexer* nlocal_from = nullptr, const long long* base_offset_dev = nullptr,
+                       const int* abort = nullptr);
 void launch_ntc(mz_domain* d, int s1, int s2, double dt, int64_t cb, int64_t ce, uint64_t step, int32_t flags,
                 double dw_tol);
 void launch_props(mz_domain* d, mz_props* p, int32_t mode);
@@ -187,6 +211,19 @@ void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const 
 void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step);
 void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
                   const mz_octree_params* prm, const mz_grid1d* grid, uint64_t step, int64_t* n_merged);
+// merging inside the fused step: no host synchronisation; the step index and
+// an abort word come from device memory, scratch is reserved beforehand for
+// cells of up to nmax particles; words3 = {deleted, merged, cell counter}
+int merge_fused_warps(mz_domain* d);
+void merge_fused_reserve(mz_domain* d, int64_t nmax, int64_t target, const mz_octree_params* prm);
+void launch_merge_fused(mz_domain* d, int s, int64_t threshold, int64_t target, const mz_octree_params* prm,
+                        const mz_grid1d* g, const uint32_t* step_ptr, const int* abort, int64_t nmax,
+                        long long* words3);
+// convect_particles! + get_cell for the fused variable-weight step: slots
+// [0, *hw_dev), dead slots skipped, destination counts into the species'
+// counts for the next sort
+void launch_convect_count(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w, double dt,
+                          const uint32_t* step_ptr, const long long* hw_dev, const int* abort, double* surf);
 void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
 void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes_out, int32_t* big_out);
 void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v);

@@ -81,6 +81,8 @@ struct ScanArgs {
     int write_indexer;
     const Indexer* nlocal_from;  // counts from n1 + n2 of an indexer instead
     int64_t* tile_sums;
+    const long long* base_offset_dev;  // added to base_offset when not null (a count the host does not hold)
+    const int* abort;                  // nonzero: the fused step was abandoned, write nothing
 };
 
 __device__ __forceinline__ int32_t scan_count(const ScanArgs& a, int c)
@@ -114,6 +116,7 @@ __device__ __forceinline__ long long block_exclusive_scan(long long v, long long
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(ScanArgs a)
 {
+    if (a.abort && *a.abort) return;
     const int c0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
     long long local = 0;
 #pragma unroll
@@ -127,6 +130,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(ScanArgs a)
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(ScanArgs a)
 {
     __shared__ long long prefix_sh;
+    if (a.abort && *a.abort) return;
     // sum of the tiles before this one
     long long pre = 0;
     for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) pre += a.tile_sums[t];
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(ScanArgs a)
     __syncthreads();
     if ((threadIdx.x & 31) == 0 && pre) atomicAdd((unsigned long long*)&prefix_sh, (unsigned long long)pre);
     __syncthreads();
-    const long long tile_base = a.base_offset + prefix_sh;
+    const long long tile_base = a.base_offset + (a.base_offset_dev ? *a.base_offset_dev : 0ll) + prefix_sh;
 
     const int c0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
     int32_t cnt[SCAN_PER_THREAD];
@@ -166,7 +170,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(ScanArgs a)
         if (a.base_out) a.base_out[c] = (int32_t)run;
         run += cnt[k];
     }
-    if (a.total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *a.total_out = tile_base - a.base_offset + total;
+    if (a.total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *a.total_out = prefix_sh + total;
 }
 
 __global__ void k_scatter(DomainView d, int s, int64_t hw)
@@ -240,7 +244,8 @@ void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v)
 }
 
 void launch_scan_cells(mz_domain* d, int32_t* counts, Indexer* ind, int32_t* fill, int64_t* total_out,
-                       bool write_indexer, int32_t* base_out, int64_t base_offset, const Indexer* nlocal_from)
+                       bool write_indexer, int32_t* base_out, int64_t base_offset, const Indexer* nlocal_from,
+                       const long long* base_offset_dev, const int* abort)
 {
     ScanArgs a;
     a.counts = counts;
@@ -253,6 +258,8 @@ void launch_scan_cells(mz_domain* d, int32_t* counts, Indexer* ind, int32_t* fil
     a.write_indexer = write_indexer ? 1 : 0;
     a.nlocal_from = nlocal_from;
     a.tile_sums = d->d_tile_sums;
+    a.base_offset_dev = base_offset_dev;
+    a.abort = abort;
     const int tiles = (int)std::max<int64_t>(1, scan_tiles(d->n_cells));
     MZ_LAUNCH(d->ctx, "scan_tiles", k_scan_tiles, tiles, SCAN_THREADS, 0, a);
     MZ_LAUNCH(d->ctx, "scan", k_scan_apply, tiles, SCAN_THREADS, 0, a);

@@ -60,6 +60,7 @@ struct StepArgs {
     double* surf;         // wall sums of this step [species][2][11], or nullptr
     double* surf_avg;     // their average, or nullptr
     double surf_factor[MZ_MAX_SPECIES];  // mass / dt per species (surface_props_scale!)
+    const int* abort;     // variable-weight step: nonzero = the step was abandoned (do nothing), or nullptr
 };
 
 // cells of the per-warp destination histogram of k_cell (48 KB per block)
@@ -114,8 +115,10 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
     const int ns = d.n_species;
     unsigned long long cand = 0, accd = 0, hits = 0;
     bool cap = false;
+    const bool abandoned = a.abort && *a.abort;
     // a resident grid; warps take the next CPW cells until none are left
     for (;;) {
+        if (abandoned) break;
         unsigned int t = 0;
         if (lane == 0) t = atomicAdd(a.next, (unsigned)CPW);
         const int c0 = (int)__shfl_sync(0xFFFFFFFFu, t, 0);
@@ -506,6 +509,7 @@ constexpr int SCATTER_TILE = 4096, SCATTER_WINDOW = 2048;
 // average from avg_start on (the convection of RNG step `step`)
 __global__ void k_surf_finish(StepArgs a, int ns)
 {
+    if (a.abort && *a.abort) return;
     const uint32_t step = *a.step_ptr - 1;  // k_cell advanced it
     const bool averaging = a.surf_avg && (int64_t)step - (int64_t)a.step0 >= a.avg_start;
     for (int i = threadIdx.x; i < ns * 2 * SURF_Q; i += blockDim.x) {
@@ -517,11 +521,16 @@ __global__ void k_surf_finish(StepArgs a, int ns)
     }
 }
 
-__global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, int64_t n)
+// n_dev (variable-weight step): the slot count from device memory, and slots
+// whose cell is -1 (dead) take no ticket
+__global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, int64_t n, const long long* n_dev,
+                                                         const int* abort)
 {
     __shared__ int32_t hist[SCATTER_WINDOW];
     constexpr int PER = SCATTER_TILE / 256;
     const SpeciesView& S = d.sp[s];
+    if (abort && *abort) return;
+    if (n_dev) n = *n_dev;
     for (int64_t t0 = (int64_t)blockIdx.x * SCATTER_TILE; t0 < n; t0 += (int64_t)gridDim.x * SCATTER_TILE) {
         const int64_t t1 = min(n, t0 + (int64_t)SCATTER_TILE);
         const int32_t cmid = S.cell[(t0 + t1 - 1) / 2];
@@ -534,7 +543,7 @@ __global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, in
             const int64_t slot = t0 + threadIdx.x + 256 * r;
             rank[r] = -1;
             key[r] = 0;
-            if (slot < t1) {
+            if (slot < t1 && (!n_dev || S.cell[slot] >= 0)) {
                 const int32_t k = S.key[slot];
                 key[r] = k;
                 const int b = k - kb;
@@ -559,29 +568,145 @@ __global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, in
     }
 }
 
+// ------------------------------------------------ variable-weight step
+// The loop body of simulations/1D/couette_varweight_octree.jl:85-135 (and of
+// the 0-D variable-weight drivers, test_bkw_varweight_octree.jl): per cell
+// ntc! with splitting (collision_ntc.jl:338-380), then
+// merge_octree_N2_based! of the cells above a threshold, then convection
+// and the sort with compute_props_sorted!.  Every kernel reads the RNG step
+// and the slot counts from device memory, so a step is captured once in a
+// CUDA graph with no host synchronisation.  The first kernel computes every
+// cell's candidate count (compute_n_coll_single_species,
+// collision_ntc.jl:173-184), which bounds its splits; the scan of those
+// counts reserves each cell's split region after the used slots, and the
+// step is abandoned right there -- before any particle changes -- when the
+// reservation would pass the storage capacity or a cell could outgrow the
+// merge scratch (the host grows both and resumes the step).
+
+// n_coll of every cell and the split reservation res[c] = n_coll; cells that
+// may be merged must fit the merge scratch (nmax particles)
+__global__ void k_vw_prepare(DomainView d, int s, double dt, const uint32_t* step_ptr, VwDev* vw, int32_t* res,
+                             int merging, int64_t threshold, int64_t nmax)
+{
+    if (vw->abort) return;
+    const uint32_t step = *step_ptr;
+    const SpeciesView& S = d.sp[s];
+    const int ns = d.n_species;
+    const int cfi = s + ns * s;
+    const uint32_t pc = (uint32_t)(s * ns + s);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d.n_cells; c += gridDim.x * blockDim.x) {
+        const Indexer p = S.ind[c];
+        const int64_t n = (int64_t)p.n1 + p.n2;
+        CollisionFactors& cf = d.cf[(size_t)cfi * d.n_cells + c];
+        const int32_t nc = ntc_ncoll(d, cf, true, n, n, dt, d.cell_V[c], cell_seed(d, c), pc,
+                                     cell_step(d, c, step), cell_rid(d, c));
+        res[c] = nc;
+        if (merging && n + nc > threshold && n + nc > nmax) {
+            atomicMax(&vw->need_cell, (long long)(n + nc));
+            atomicOr(&vw->abort, VW_SCRATCH);
+        }
+    }
+}
+
+// after the scan of the reservations (total in sp.need): the slots in use
+// after the splits, or the step is abandoned for capacity
+__global__ void k_vw_check(VwDev* vw, int s, long long capacity)
+{
+    if (vw->abort) return;
+    VwSpecies& q = vw->sp[s];
+    const long long need = q.hw + q.need;
+    q.need = need;
+    if (need > capacity)
+        vw->abort |= VW_CAPACITY;
+    else
+        q.hw_split = need;
+}
+
+// ntc! of every cell, one group of G lanes per cell; split particles go to
+// the cell's reserved region [base[c], base[c] + res[c]), whose unused slots
+// become dead (as k_ntc does for the standalone entry point)
+template <int G>
+__global__ void __launch_bounds__(256) k_vw_ntc(DomainView d, int s, double dw_tol, const uint32_t* step_ptr,
+                                                const int* abort, const int32_t* base, const int32_t* res)
+{
+    if (*abort) return;
+    const uint32_t step = *step_ptr;
+    const SpeciesView& S = d.sp[s];
+    const int ns = d.n_species;
+    const int cfi = s + ns * s;
+    const uint32_t pc = (uint32_t)(s * ns + s);
+    const Interaction I = d.inter[cfi];
+    const WarpGroup<G> grp;
+    const int ngroups = (gridDim.x * blockDim.x) / G;
+    unsigned long long cand = 0, accd = 0, spl = 0;
+    for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); c < d.n_cells; c += ngroups) {
+        CollisionFactors* cfp = &d.cf[(size_t)cfi * d.n_cells + c];
+        const int32_t ncoll = cfp->n_coll;
+        if (ncoll <= 0) continue;
+        Indexer p1 = S.ind[c];
+        Indexer p2 = p1;
+        const int32_t b1 = base[c];
+        const NtcResult R = ntc_cell<false, G>(d, I, true, c, ncoll, cfp->smax, S.A, S.A, p1, p2, S.cell, S.key,
+                                               S.cell, S.key, b1, 0, dw_tol, cell_seed(d, c), pc,
+                                               cell_step(d, c, step), cell_rid(d, c));
+        if (grp.rank == 0) {
+            cfp->smax = R.smax;
+            cfp->n_coll_performed = R.perf;
+            cfp->n_eq_w_coll_performed = R.eqw;
+            cfp->n_split = R.nsp1;
+            S.ind[c] = p1;
+            cand += ncoll;
+            accd += R.perf;
+            spl += R.nsp1;
+        }
+        const int32_t r1 = res[c];
+        for (int32_t q = R.nsp1 + grp.rank; q < r1; q += G) S.cell[b1 + q] = -1;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand += __shfl_xor_sync(0xFFFFFFFFu, cand, o);
+        accd += __shfl_xor_sync(0xFFFFFFFFu, accd, o);
+        spl += __shfl_xor_sync(0xFFFFFFFFu, spl, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cand) {
+        atomicAdd(&d.counters->candidates, cand);
+        atomicAdd(&d.counters->accepted, accd);
+        atomicAdd(&d.counters->splits, spl);
+    }
+}
+
+// 0-D: every live slot stays in its cell; counting it there lets the sort
+// machinery compact the cells (squash_pia!) for the props
+__global__ void k_vw_keep(DomainView d, int s, const long long* hw_dev, const int* abort)
+{
+    if (*abort) return;
+    const SpeciesView& S = d.sp[s];
+    const int64_t hw = *hw_dev;
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < hw;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t slot = base + lane;
+        const int32_t c = slot < hw ? S.cell[slot] : -1;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, c >= 0);
+        if (c >= 0) {
+            S.key[slot] = c;
+            warp_agg_add(S.counts, c, m);
+        }
+    }
+}
+
+__global__ void k_vw_advance(uint32_t* step, const int* abort)
+{
+    if (!*abort) *step += 1u;
+}
+
 }  // namespace
 
-void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg)
+// launch arguments every fused step shares: walls, props and averaging,
+// surface sampling, the device step index and cell counters
+static StepArgs step_args(mz_domain* d, const mz_step_plan* plan, mz_props* inst, mz_props* avg)
 {
     mz_ctx* c = d->ctx;
-    if (n_steps <= 0) return;
-    MZ_REQUIRE(plan->equal_weight, "mz_step: the fused step runs ntc_equal_weight!; use mz_ntc for splitting");
-    // the 1-D step's sort runs over slots [0, n_total): close gaps first; the
-    // 0-D step works on each cell's group-1 list in place, so only split
-    // particles in group 2 need a compaction
-    for (int s = 0; s < d->ns; ++s)
-        if (plan->dims == 1 || d->sp[s].group2) launch_compact(d, s);
-    if (!d->d_step) {
-        MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
-        MZ_CK(cudaMalloc(&d->d_done, 8 * sizeof(unsigned int)));
-        MZ_CK(cudaMemsetAsync(d->d_done, 0, 8 * sizeof(unsigned int), c->stream));
-    }
-    const uint32_t first = (uint32_t)(plan->step0 + 1);
-    // a one-thread kernel, not a copy from pageable host memory: such a copy
-    // waits for the stream to drain, and the host would then launch the next
-    // step's kernels on an idle GPU
-    MZ_LAUNCH(c, "step_set_index", k_set_step, 1, 1, 0, d->d_step, first);
-
     StepArgs a;
     memset(&a, 0, sizeof a);
     a.W.L = plan->grid.L;
@@ -623,11 +748,47 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     a.hit_done = d->d_done + 3;
     a.big_next = d->d_done + 4;
     a.big_done = d->d_done + 5;
+    return a;
+}
+
+static void ensure_step_words(mz_domain* d)
+{
+    if (!d->d_step) {
+        MZ_CK(cudaMalloc(&d->d_step, sizeof(uint32_t)));
+        MZ_CK(cudaMalloc(&d->d_done, 8 * sizeof(unsigned int)));
+        MZ_CK(cudaMemsetAsync(d->d_done, 0, 8 * sizeof(unsigned int), d->ctx->stream));
+    }
+}
+
+static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg);
+
+void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg)
+{
+    mz_ctx* c = d->ctx;
+    if (n_steps <= 0) return;
+    if (!plan->equal_weight) {
+        launch_step_vw(d, plan, n_steps, inst, avg);
+        return;
+    }
+    // the 1-D step's sort runs over slots [0, n_total): close gaps first; the
+    // 0-D step works on each cell's group-1 list in place, so only split
+    // particles in group 2 need a compaction
+    for (int s = 0; s < d->ns; ++s)
+        if (plan->dims == 1 || d->sp[s].group2) launch_compact(d, s);
+    ensure_step_words(d);
+    const uint32_t first = (uint32_t)(plan->step0 + 1);
+    // a one-thread kernel, not a copy from pageable host memory: such a copy
+    // waits for the stream to drain, and the host would then launch the next
+    // step's kernels on an idle GPU
+    MZ_LAUNCH(c, "step_set_index", k_set_step, 1, 1, 0, d->d_step, first);
+    StepArgs a = step_args(d, plan, inst, avg);
     if (plan->dims == 1) {
-        // wall-hit queue: a fraction of the particles; overflow is handled inline
+        // wall-hit queue: a fraction of the particles (or the plan's size);
+        // overflow is handled inline
         int64_t n_all = 0;
         for (int s = 0; s < d->ns; ++s) n_all += d->sp[s].n_total;
-        const int64_t want = std::max<int64_t>(4096, n_all / 16);
+        const int64_t want =
+            plan->hit_queue_capacity > 0 ? plan->hit_queue_capacity : std::max<int64_t>(4096, n_all / 16);
         if (want > d->hitq_cap) {
             cudaFree(d->d_hitq);
             d->d_hitq = nullptr;
@@ -636,7 +797,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             d->hitq_cap = want;
         }
         a.hitq = static_cast<int4*>(d->d_hitq);
-        a.hitq_cap = (unsigned)std::min<int64_t>(d->hitq_cap, 0x7FFFFFFF);
+        a.hitq_cap = (unsigned)std::min<int64_t>(std::min(want, d->hitq_cap), 0x7FFFFFFF);
     }
     const bool want_props = plan->props && (inst || a.has_avg);
     const bool split = plan->dims == 1 && (plan->launches == 2 || (plan->launches == 0 && d->tuned_split > 0));
@@ -709,7 +870,8 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             SpeciesHost& S = d->sp[s];
             launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar + s, true, nullptr, 0);
             const int sb = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(S.n_total, SCATTER_TILE), (int64_t)c->num_sms * 8));
-            MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total);
+            MZ_LAUNCH(c, "step_scatter", k_step_scatter, sb, 256, 0, v, s, S.n_total, (const long long*)nullptr,
+                      (const int*)nullptr);
         }
         if (split && physics) {
             // gather + props, then NTC + convection in place on the sorted
@@ -763,6 +925,200 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             d->sp[s].hw = d->sp[s].n_total;
             d->sp[s].compact = true;
         }
+}
+
+// The variable-weight loop with the standalone kernels, step by step (a
+// mixture: each pair's splits change the cells the next pair draws from, so
+// no reservation can be made for the whole step before it starts).
+static void launch_step_vw_sequence(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst,
+                                    mz_props* avg)
+{
+    mz_ctx* c = d->ctx;
+    const bool want_props = plan->props && (inst || (avg && plan->avg_start > 0));
+    mz_props* p = inst;
+    mz_props* own = nullptr;
+    if (want_props && !p) {
+        MZ_REQUIRE(mz_props_create(d, 0, nullptr, 300.0, avg->ndens, &own) == MZ_OK, "mz_step: props");
+        p = own;
+    }
+    const int64_t m = d->n_cells * d->ns;
+    for (int64_t k = 1; k <= n_steps; ++k) {
+        const uint64_t step = plan->step0 + (uint64_t)k;
+        if (plan->collide)
+            for (int s2 = 0; s2 < d->ns; ++s2)
+                for (int s1 = s2; s1 < d->ns; ++s1)
+                    launch_ntc(d, s1, s2, plan->dt, 0, d->n_cells, step, 0, plan->dw_tol);
+        for (int s = 0; s < d->ns; ++s) {
+            if (plan->merge_threshold > 0)
+                launch_merge(d, s, 0, d->n_cells, plan->merge_threshold, plan->merge_target, &plan->octree,
+                             plan->dims == 1 ? &plan->grid : nullptr, step, nullptr);
+            if (plan->dims == 1) {
+                launch_convect(d, s, &plan->grid, &plan->walls, plan->dt, step, 0);
+                launch_sort(d, s, &plan->grid, nullptr);
+            } else {
+                launch_compact(d, s);
+            }
+        }
+        if (want_props) {
+            launch_props(d, p, plan->dims == 1 ? MZ_PROPS_SORTED : MZ_PROPS_ALL);
+            if (avg && plan->avg_start > 0 && k >= plan->avg_start) {
+                const double inv = 1.0 / (double)plan->n_avg;
+                launch_avg(c, avg->np, p->np, m, inv);
+                launch_avg(c, avg->n, p->n, m, inv);
+                launch_avg(c, avg->v, p->v, 3 * m, inv);
+                launch_avg(c, avg->T, p->T, m, inv);
+            }
+        }
+    }
+    if (own) mz_props_destroy(own);
+}
+
+// Variable-weight steps of one species, device-resident and graph-replayed
+// (the kernels k_vw_prepare .. k_cell_gather above).  A step abandoned for
+// capacity or merge scratch leaves the state of the step before; the host
+// reads how many steps finished, grows what was short and runs the rest, so
+// the result equals an uninterrupted run.
+static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_props* inst, mz_props* avg)
+{
+    mz_ctx* c = d->ctx;
+    MZ_REQUIRE(plan->dims == 0 || plan->dims == 1, "mz_step: dims must be 0 or 1");
+    const bool merging = plan->merge_threshold > 0;
+    if (merging) MZ_REQUIRE(plan->merge_target >= 1, "mz_step: merge_target must be at least 1");
+    if (d->ns != 1) {
+        launch_step_vw_sequence(d, plan, n_steps, inst, avg);
+        return;
+    }
+    const int s = 0;
+    SpeciesHost& S = d->sp[s];
+    launch_compact(d, s);
+    ensure_step_words(d);
+    if (!d->d_vw) {
+        MZ_CK(cudaMalloc(&d->d_vw, sizeof(VwDev)));
+        MZ_CK(cudaMallocHost(&d->h_vw, sizeof(VwDev)));
+    }
+    if (merging) {
+        d->vw_nmax = std::max<int64_t>(d->vw_nmax, std::max<int64_t>(2 * plan->merge_threshold,
+                                                                     plan->merge_threshold + 2048));
+        merge_fused_reserve(d, d->vw_nmax, plan->merge_target, &plan->octree);
+    }
+    MZ_CK(cudaMemsetAsync(S.counts, 0, (d->n_cells + 1) * sizeof(int32_t), c->stream));
+    const bool want_props = plan->props && (inst || (avg && plan->avg_start > 0));
+    const int G = ntc_group_width(d->n_cells);
+    using KNtc = void (*)(DomainView, int, double, const uint32_t*, const int*, const int32_t*, const int32_t*);
+    const KNtc kntc = G == 8 ? k_vw_ntc<8> : (G == 16 ? k_vw_ntc<16> : k_vw_ntc<32>);
+    const int cblocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells, 256), (int64_t)c->num_sms * 8));
+    const int nblocks =
+        (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells * G, 256), (int64_t)c->num_sms * 16));
+    int per_sm = 0;
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_gather, 256, 0));
+    const int gblocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>(div_up(d->n_cells, 8), (int64_t)c->num_sms * std::max(per_sm, 1)));
+    VwDev* V = d->d_vw;
+    const int* abort = &V->abort;
+
+    int64_t done = 0;
+    while (done < n_steps) {
+        memset(d->h_vw, 0, sizeof(VwDev));
+        d->h_vw->sp[s].hw = S.n_total;
+        MZ_CK(cudaMemcpyAsync(d->d_vw, d->h_vw, sizeof(VwDev), cudaMemcpyHostToDevice, c->stream));
+        const uint32_t first = (uint32_t)(plan->step0 + 1 + (uint64_t)done);
+        MZ_LAUNCH(c, "step_set_index", k_set_step, 1, 1, 0, d->d_step, first);
+        StepArgs a = step_args(d, plan, inst, avg);
+        a.abort = abort;
+        a.props_lag = 1;  // the gather runs after the step index advanced
+        const int cur0 = S.cur;
+        const int64_t sblocks = std::max<int64_t>(
+            1, std::min<int64_t>(div_up(S.capacity, SCATTER_TILE), (int64_t)c->num_sms * 8));
+        auto one_step = [&]() {
+            DomainView v = make_view(d);
+            if (plan->collide) {
+                // n_coll and split reservations, then the reservations' bases
+                // after the used slots and the capacity check
+                MZ_LAUNCH(c, "vw_prepare", k_vw_prepare, cblocks, 256, 0, v, s, plan->dt, d->d_step, V, S.fill,
+                          merging ? 1 : 0, plan->merge_threshold, d->vw_nmax);
+                launch_scan_cells(d, S.fill, S.ind, S.fill, reinterpret_cast<int64_t*>(&V->sp[s].need), false,
+                                  S.work, 0, nullptr, &V->sp[s].hw, abort);
+            } else {
+                MZ_CK(cudaMemsetAsync(&V->sp[s].need, 0, sizeof(long long), c->stream));
+            }
+            MZ_LAUNCH(c, "vw_check", k_vw_check, 1, 1, 0, V, s, (long long)S.capacity);
+            if (plan->collide)
+                MZ_LAUNCH(c, "vw_ntc", kntc, nblocks, 256, 0, v, s, plan->dw_tol, d->d_step, abort, S.work, S.fill);
+            if (merging)
+                launch_merge_fused(d, s, plan->merge_threshold, plan->merge_target, &plan->octree,
+                                   plan->dims == 1 ? &plan->grid : nullptr, d->d_step, abort, d->vw_nmax,
+                                   V->sp[s].merge);
+            if (plan->dims == 1) {
+                if (a.surf)
+                    MZ_CK(cudaMemsetAsync(a.surf, 0, (size_t)d->ns * 2 * SURF_Q * sizeof(double), c->stream));
+                launch_convect_count(d, s, &plan->grid, &plan->walls, plan->dt, d->d_step, &V->sp[s].hw_split,
+                                     abort, a.surf);
+            } else {
+                MZ_LAUNCH(c, "vw_keep", k_vw_keep, (int)sblocks, 256, 0, v, s, &V->sp[s].hw_split, abort);
+            }
+            MZ_LAUNCH(c, "vw_advance", k_vw_advance, 1, 1, 0, d->d_step, abort);
+            if (a.surf) MZ_LAUNCH(c, "step_surf", k_surf_finish, 1, 128, 0, a, d->ns);
+            // sort_particles! over the used slots (dead ones skipped) and
+            // compute_props_sorted! of the sorted state
+            launch_scan_cells(d, S.counts, S.ind, S.fill, reinterpret_cast<int64_t*>(&V->sp[s].hw), true, nullptr, 0,
+                              nullptr, nullptr, abort);
+            MZ_LAUNCH(c, "step_scatter", k_step_scatter, (int)sblocks, 256, 0, v, s, (int64_t)0, &V->sp[s].hw_split,
+                      abort);
+            StepArgs b = a;
+            b.gather = 1;
+            b.props = want_props ? 1 : 0;
+            b.physics = 0;
+            b.advance = 0;
+            MZ_LAUNCH(c, "step_cell_final", k_cell_gather, gblocks, 256, 0, v, b);
+            S.cur ^= 1;
+        };
+        const int64_t todo = n_steps - done;
+        if (plan->use_graph && todo > 2) {
+            // two steps per graph: the buffers alternate
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            const int64_t launches0 = c->launches;
+            MZ_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            one_step();
+            one_step();
+            MZ_CK(cudaStreamEndCapture(c->stream, &g));
+            const int64_t per_graph = c->launches - launches0;
+            MZ_CK(cudaGraphInstantiate(&ge, g, 0));
+            const int64_t pairs = todo / 2;
+            for (int64_t i = 0; i < pairs; ++i) MZ_CK(cudaGraphLaunch(ge, c->stream));
+            c->launches += per_graph * (pairs - 1);
+            if (todo % 2) one_step();
+            MZ_CK(cudaGraphExecDestroy(ge));
+            MZ_CK(cudaGraphDestroy(g));
+        } else {
+            for (int64_t t = 0; t < todo; ++t) one_step();
+        }
+        MZ_CK(cudaMemcpyAsync(d->h_vw, d->d_vw, sizeof(VwDev), cudaMemcpyDeviceToHost, c->stream));
+        MZ_CK(cudaMemcpyAsync(d->h_scalar + 7, d->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+        MZ_CK(cudaStreamSynchronize(c->stream));
+        uint32_t now = 0;
+        memcpy(&now, d->h_scalar + 7, sizeof now);
+        const int64_t completed = (int64_t)(now - first);
+        MZ_REQUIRE(completed >= 0 && completed <= todo, "mz_step: step index out of range");
+        S.cur = cur0 ^ (int)(completed & 1);
+        S.n_total = S.hw = d->h_vw->sp[s].hw;
+        S.compact = true;
+        S.group2 = false;
+        done += completed;
+        const int why = d->h_vw->abort;
+        if (!why) {
+            MZ_REQUIRE(completed == todo, "mz_step: steps missing");
+            break;
+        }
+        if (why & VW_CAPACITY) {
+            const int64_t need = d->h_vw->sp[s].need;
+            reserve_species(d, s, need + need / 8 + 1024);
+        }
+        if (why & VW_SCRATCH) {
+            d->vw_nmax = d->h_vw->need_cell + d->h_vw->need_cell / 4 + 256;
+            merge_fused_reserve(d, d->vw_nmax, plan->merge_target, &plan->octree);
+        }
+    }
 }
 
 // Time every mapping of the fused step on real steps of the simulation (the

@@ -74,7 +74,8 @@ MZ_REQ_QUEUED, MZ_REQ_RUNNING, MZ_REQ_DONE = 0, 1, 2
 class StepPlan(C.Structure):
     _fields_ = [("dims", i32), ("collide", i32), ("equal_weight", i32), ("props", i32), ("avg_start", i64),
                 ("n_avg", i64), ("dt", d), ("dw_tol", d), ("step0", u64), ("use_graph", i32), ("big_cell", i32),
-                ("grid", Grid1D), ("walls", Walls1D), ("launches", i32)]
+                ("grid", Grid1D), ("walls", Walls1D), ("launches", i32), ("hit_queue_capacity", i64),
+                ("merge_threshold", i64), ("merge_target", i64), ("octree", OctreeParams)]
 
 
 _SIGS = {
@@ -139,6 +140,9 @@ _SIGS = {
     "mz_server_retired": (i32, [vp, i64, P(i64), P(i64)]),
     "mz_server_info": (i32, [vp, P(i64), P(i64)]),
     "mz_server_set_lane_split": (i32, [vp, i64]),
+    "mz_server_set_hbm_headroom": (i32, [vp, i64]),
+    "mz_check_indexing": (i32, [vp, i32, i32, P(i32), P(i64)]),
+    "mz_set_indexer": (i32, [vp, i32, P(ParticleIndexer), i64]),
     "mz_swpm": (i32, [vp, i32, d, d, i64, i64, u64]),
     "mz_props_snapshot": (i32, [vp, i32, P(d)]),
     "mz_props_snapshot_wait": (i32, [vp, i32]),

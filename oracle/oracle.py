@@ -237,13 +237,14 @@ class Oracle:
         n = particles.shape[0]
         self.pv_set(s, particles, cell=cells, nbuffer=0)
         ind, nt, cg = self.pia_get()
+        cnt = np.bincount(cells - 1, minlength=self.n_cells)[: self.n_cells].astype(np.int64)
+        pos = 1 + np.concatenate(([0], np.cumsum(cnt)[:-1]))
         ind[s] = np.array([0, 0, -1, 0, 0, -1, 0])
-        pos = 1
-        for c in range(1, self.n_cells + 1):
-            cnt = int(np.sum(cells == c))
-            if cnt:
-                ind[s, c - 1] = [cnt, pos, pos + cnt - 1, cnt, 0, -1, 0]
-            pos += cnt
+        nz = cnt > 0
+        ind[s, nz, 0] = cnt[nz]
+        ind[s, nz, 1] = pos[nz]
+        ind[s, nz, 2] = pos[nz] + cnt[nz] - 1
+        ind[s, nz, 3] = cnt[nz]
         nt[s] = n
         cg[s] = 1
         self.pia_set(ind, nt, cg)
@@ -254,18 +255,22 @@ class Oracle:
         then group2 (what pv[i] returns for i over the indexer)."""
         pv = self.pv_get(s)
         ind, _, _ = self.pia_get()
-        rows, cells = [], []
-        for c in range(self.n_cells):
-            p = ind[s, c]
-            for i in range(p[1], p[2] + 1):
-                if i >= 1:
-                    rows.append(pv["particles"][pv["index"][i - 1] - 1])
-                    cells.append(c + 1)
-            if p[6] > 0:
-                for i in range(p[4], p[5] + 1):
-                    rows.append(pv["particles"][pv["index"][i - 1] - 1])
-                    cells.append(c + 1)
-        return np.array(rows).reshape(-1, 7), np.array(cells, np.int64)
+        p = ind[s]
+        # per cell: positions start1..end1 (those >= 1), then start2..end2 when
+        # n_group2 > 0, cells in order
+        len1 = np.maximum(p[:, 2] - p[:, 1] + 1, 0)
+        len2 = np.where(p[:, 6] > 0, np.maximum(p[:, 5] - p[:, 4] + 1, 0), 0)
+        lens = np.column_stack([len1, len2]).reshape(-1)
+        starts = np.column_stack([p[:, 1], p[:, 4]]).reshape(-1)
+        total = int(lens.sum())
+        seg = np.repeat(np.arange(lens.size), lens)
+        first = np.concatenate(([0], np.cumsum(lens)[:-1]))
+        pos = starts[seg] + (np.arange(total) - first[seg])
+        cells = seg // 2 + 1
+        keep = pos >= 1
+        pos, cells = pos[keep], cells[keep]
+        rows = pv["particles"][pv["index"][pos - 1] - 1]
+        return rows.reshape(-1, 7), cells.astype(np.int64)
 
     def cf_get(self, s1, s2):
         smax = np.zeros(self.n_cells)

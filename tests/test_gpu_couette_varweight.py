@@ -118,3 +118,254 @@ def test_splitting_and_merging_conserve_per_cell(ctx):
         dom.convect(0, grid, walls, dt, step)
         dom.sort(0, grid)
     assert merged > 0 and dom.counters()["splits"] > 0
+
+
+def _vw_plan(grid, walls, dt, octree, threshold, target, dims=1, step0=0, graph=True, avg_start=0, n_avg=1):
+    """mz_step with equal_weight = 0: ntc! with splitting, merging of the cells
+    above `threshold` down to `target`, (1-D) convection, sort, props."""
+    p = mz._lib.StepPlan()
+    p.dims, p.collide, p.equal_weight, p.props = dims, 1, 0, 1
+    p.avg_start, p.n_avg, p.dt, p.dw_tol, p.step0 = avg_start, n_avg, dt, 1e-16, step0
+    p.use_graph = 1 if graph else 0
+    if grid is not None:
+        p.grid = grid.c_struct()
+    if walls is not None:
+        p.walls = walls.c_struct()
+    p.merge_threshold, p.merge_target, p.octree = threshold, target, octree.params
+    return p
+
+
+def _oracle_varweight_loop(o, oc, grid, walls, dt, seed, steps, threshold, target, step0=0, threads=8):
+    """The reference loop of couette_varweight_octree.jl:85-135 on the oracle:
+    ntc! per cell, merge of the cells above the threshold, squash_pia!,
+    convect, sort."""
+    nx = o.n_cells
+    merged = 0
+    for step in range(step0 + 1, step0 + steps + 1):
+        o.ntc_cells(0, 0, dt, None if grid is None else grid.V, seed, step, equal_weight=False, nthreads=threads)
+        ind, _, _ = o.pia_get()
+        for c in np.nonzero(ind[0, :, 0] > threshold)[0]:
+            if grid is None:
+                o.merge_octree(oc, 0, int(c) + 1, target, seed=seed, step=step)
+            else:
+                o.merge_octree(oc, 0, int(c) + 1, target, L=grid.L, nx=nx, seed=seed, step=step)
+            merged += 1
+        o.squash(0)
+        if grid is not None:
+            o.convect(0, grid.L, nx, walls.as_flat_array(), dt, seed, step, nthreads=threads)
+            o.sort(0, L=grid.L, nx=nx)
+    return merged
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_fused_varweight_step_equals_standalone_loop(ctx, orc, graph):
+    """mz_step with splitting and merging (one graph-replayed step, no host
+    synchronisation inside) gives the particles of the standalone calls
+    ntc! -> merge -> convect -> sort bit for bit, and both follow the oracle."""
+    nx, ppc, steps, threshold, target, seed = 24, 150, 5, 160, 80, 93
+    sp, inter, grid, walls, dt, smax, arrays = _varweight_state(nx, ppc, seed)
+    cap = 8 * nx * ppc
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    doms = []
+    for fused in (True, False):
+        dom = mz.Domain(ctx, nx, sp, cap, interactions=inter, seed=seed)
+        dom.upload(0, *arrays)
+        dom.set_cell_volumes(grid.V)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        if fused:
+            inst = mz.PhysProps(dom)
+            dom.step(_vw_plan(grid, walls, dt, octree, threshold, target, graph=graph), steps, inst)
+        else:
+            for step in range(1, steps + 1):
+                dom.ntc(0, 0, dt, step, equal_weight=False)
+                dom.merge_octree(0, octree, target, threshold=threshold, grid=grid, step=step)
+                dom.convect(0, grid, walls, dt, step)
+                dom.sort(0, grid)
+        doms.append(dom)
+    a, ca = device_logical(doms[0], 0)
+    b, cb = device_logical(doms[1], 0)
+    assert np.array_equal(ca, cb) and np.array_equal(a, b)
+    cnt = doms[0].counters()
+    assert cnt["merges"] >= nx and cnt["splits"] > 0
+    assert doms[0].info(0)["n_total"] == a.shape[0]
+    o = oracle_state(orc, nx, sp, mz.VHS, [arrays], capacity=cap)
+    o.cf_set_smax(0, 0, smax)
+    oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
+    _oracle_varweight_loop(o, oc, grid, walls, dt, seed, steps, threshold, target)
+    orows, oc_cells = oracle_logical(o, 0)
+    assert np.array_equal(oc_cells, ca)
+    assert_close_rows(orows, a, 1e-11, "fused variable-weight step")
+    r = inst.fetch()
+    ref = o.compute_props(mode=2)
+    assert np.array_equal(r["np"][:, 0], ref["np"][0])
+    assert_close_rows(r["T"][:, 0:1], ref["T"][0].reshape(-1, 1), 1e-11, "T after the fused steps")
+    for dom in doms:
+        dom.close()
+
+
+def test_fused_varweight_couette_at_the_benchmark_size_matches_oracle(ctx, orc):
+    """The variable-weight Couette configuration: 1,000 cells, 1,000 initial
+    particles per cell with weights log-uniform over two decades, merging of
+    cells above 1,200 particles down to 300; four fused steps against the
+    oracle's reference loop: candidate and collision counts per cell, cells
+    and indexers equal, particles within 1e-11."""
+    nx, ppc, steps, threshold, target, seed = 1000, 1000, 4, 1200, 300, 1234
+    sp, inter, grid, walls, dt, smax, arrays = _varweight_state(nx, ppc, seed)
+    cap = 5_000_000
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    dom = mz.Domain(ctx, nx, sp, cap, interactions=inter, seed=seed)
+    dom.upload(0, *arrays)
+    dom.set_cell_volumes(grid.V)
+    dom.set_sigma_g_w_max(0, 0, smax)
+    inst = mz.PhysProps(dom)
+    dom.step(_vw_plan(grid, walls, dt, octree, threshold, target), steps, inst)
+    o = oracle_state(orc, nx, sp, mz.VHS, [arrays], capacity=cap)
+    o.cf_set_smax(0, 0, smax)
+    oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
+    merged = _oracle_varweight_loop(o, oc, grid, walls, dt, seed, steps, threshold, target, threads=16)
+    cnt = dom.counters()
+    assert cnt["merges"] == merged and merged > 100
+    smax_o, ccnt = o.cf_get(0, 0)
+    cf = dom.collision_factors(0, 0)
+    assert np.array_equal(cf["n_coll"], ccnt[:, 2]) and np.array_equal(cf["n_coll_performed"], ccnt[:, 3])
+    orows, oc_cells = oracle_logical(o, 0)
+    drows, dc_cells = device_logical(dom, 0)
+    assert np.array_equal(oc_cells, dc_cells)
+    assert_close_rows(orows, drows, 1e-11, "variable-weight Couette, 1,000 cells")
+    oind, _, _ = o.pia_get()
+    dind, _ = dom.indexer(0)
+    assert np.array_equal(dind[:, 3], oind[0, :, 3])
+    r = inst.fetch()
+    ref = o.compute_props(mode=2)
+    assert np.array_equal(r["np"][:, 0], ref["np"][0])
+    assert_close_rows(r["T"][:, 0:1], ref["T"][0].reshape(-1, 1), 1e-11, "T")
+    dom.close()
+
+
+def test_fused_varweight_step_grows_storage_and_resumes(ctx):
+    """Storage too small for a step's split reservations, and a 0-D cell larger
+    than the merge scratch: the step is abandoned before it changes a
+    particle, the host grows the storage (MZ_E_CAPACITY's remedy,
+    collision_ntc.jl:241-243 resizes the ParticleVector) or the scratch and
+    resumes; the result equals a run that never ran short."""
+    sp = species(["Ar"])
+    inter = interactions(sp)
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    # 1-D: capacity just above the initial particles
+    nx, ppc, threshold, target, seed = 16, 150, 160, 80, 71
+    _, _, grid, walls, dt, smax, arrays = _varweight_state(nx, ppc, seed)
+    runs = []
+    for cap in (nx * ppc + 10, 8 * nx * ppc):
+        dom = mz.Domain(ctx, nx, sp, cap, interactions=inter, seed=seed)
+        dom.upload(0, *arrays)
+        dom.set_cell_volumes(grid.V)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        dom.step(_vw_plan(grid, walls, 3 * dt, octree, threshold, target), 6)
+        runs.append((device_logical(dom, 0), dom.info(0)["capacity"]))
+        dom.close()
+    (a, ca), cap_small = runs[0]
+    (b, cb), _ = runs[1]
+    assert cap_small > nx * ppc + 10  # the storage grew
+    assert np.array_equal(ca, cb) and np.array_equal(a, b)
+    # 0-D: a cell of 5,000 particles is beyond the default merge scratch
+    # (2 x threshold or threshold + 2,048)
+    counts = np.array([300, 5000, 800, 120])
+    states = []
+    for mode in ("graph", "direct", "standalone"):
+        dom = mz.Domain(ctx, len(counts), sp, 4 * int(counts.sum()), interactions=inter, seed=seed)
+        dom.sample_cells(0, counts, 300.0, 1e12, step=0, log10_weight_span=2.0)
+        dom.set_sigma_g_w_max(0, 0, mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], 300.0, 300.0, 1e12))
+        if mode == "standalone":
+            for step in range(1, 4):
+                dom.ntc(0, 0, 1e-3, step, equal_weight=False)
+                dom.merge_octree(0, octree, 100, threshold=200, step=step)
+                dom.squash(0)
+        else:
+            dom.step(_vw_plan(None, None, 1e-3, octree, 200, 100, dims=0, graph=mode == "graph"), 3)
+        states.append(device_logical(dom, 0))
+        # three cells above the threshold, merged to a target below it
+        assert dom.counters()["merges"] >= 3
+        dom.close()
+    for a, ca in states[1:]:
+        assert np.array_equal(states[0][1], ca) and np.array_equal(states[0][0], a)
+
+
+def test_fused_varweight_0d_and_mixture_match_oracle(ctx, orc):
+    """0-D variable-weight steps (test_bkw_varweight_octree.jl's loop: ntc!,
+    merge, compute_props!) on the device-resident path, and a two-species
+    mixture with unequal weights (test_2species_varweight_octree.jl), which
+    mz_step runs with the standalone kernels step by step: both against the
+    oracle."""
+    sp = species(["Ar"])
+    inter = interactions(sp)
+    counts = np.array([300, 1800, 800, 120, 2600, 40])
+    seed, steps, threshold, target, dt, Fnum = 19, 4, 1000, 400, 2e-3, 1e12
+    dom = mz.Domain(ctx, len(counts), sp, 6 * int(counts.sum()), interactions=inter, seed=seed)
+    dom.sample_cells(0, counts, 500.0, Fnum, step=0, log10_weight_span=2.0)
+    smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], 500.0, 500.0, Fnum)
+    dom.set_sigma_g_w_max(0, 0, smax)
+    w, v, x, cell = dom.download(0)
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    inst = mz.PhysProps(dom)
+    dom.step(_vw_plan(None, None, dt, octree, threshold, target, dims=0), steps, inst)
+    o = oracle_state(orc, len(counts), sp, mz.VHS, [(w, v, x, cell)], capacity=6 * int(counts.sum()))
+    o.cf_set_smax(0, 0, smax)
+    oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
+    merged = _oracle_varweight_loop(o, oc, None, None, dt, seed, steps, threshold, target)
+    assert dom.counters()["merges"] == merged and merged >= 2
+    orows, oc_cells = oracle_logical(o, 0)
+    drows, dc_cells = device_logical(dom, 0)
+    assert np.array_equal(oc_cells, dc_cells)
+    assert_close_rows(orows, drows, 1e-11, "0-D variable-weight cells")
+    r = inst.fetch()
+    ref = o.compute_props(mode=0)
+    assert_close_rows(r["T"][:, 0:1], ref["T"][0].reshape(-1, 1), 1e-11, "0-D T")
+    dom.close()
+
+    # two species, unequal weights: ntc! for (Ar,Ar), (He,Ar), (He,He), then
+    # merging of each species
+    sp2 = species(["Ar", "He"])
+    inter2 = interactions(sp2)
+    n_cells, seed = 4, 23
+    cnt2 = [np.array([400, 900, 150, 600]), np.array([1200, 300, 800, 500])]
+    Fn = (2e12, 5e11)
+    dom = mz.Domain(ctx, n_cells, sp2, 20000, interactions=inter2, seed=seed)
+    for s, T0 in enumerate((3000.0, 360.0)):
+        dom.sample_cells(s, cnt2[s], T0, Fn[s], step=0, log10_weight_span=1.0)
+    arrays = [dom.download(s) for s in range(2)]
+    smax2 = {}
+    for s1 in range(2):
+        for s2 in range(2):
+            T1, T2 = (3000.0, 360.0)[s1], (3000.0, 360.0)[s2]
+            smax2[s1, s2] = mz.estimate_sigma_g_w_max(inter2[s1][s2], sp2[s1], sp2[s2], T1, T2, max(Fn))
+            dom.set_sigma_g_w_max(s1, s2, smax2[s1, s2])
+    dom.step(_vw_plan(None, None, 1e-3, octree, 1000, 500, dims=0), 3)
+    t = mz.VHS
+    o = orc.Oracle(n_cells, 2, [s.mass for s in sp2])
+    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    for s in range(2):
+        w, v, x, cell = arrays[s]
+        o.set_particles_simple(s, cell.astype(np.int64) + 1, np.column_stack([w, v, x]))
+        o.pv_resize(s, 20000)
+    for (s1, s2), val in smax2.items():
+        o.cf_set_smax(s1, s2, val)
+    for step in range(1, 4):
+        # cell by cell, every pair on the cell (the reference's mixture loop):
+        # a cell's split particles then stay one contiguous group 2
+        for c in range(1, n_cells + 1):
+            for s2 in range(2):
+                for s1 in range(s2, 2):
+                    o.ntc(s1, s2, c, 1e-3, 1.0, seed, step, equal_weight=False)
+        ind, _, _ = o.pia_get()
+        for s in range(2):
+            for c in np.nonzero(ind[s, :, 0] > 1000)[0]:
+                o.merge_octree(oc, s, int(c) + 1, 500, seed=seed, step=step)
+            o.squash(s)
+    for s in range(2):
+        orows, oc_cells = oracle_logical(o, s)
+        drows, dc_cells = device_logical(dom, s)
+        assert np.array_equal(oc_cells, dc_cells), s
+        assert_close_rows(orows, drows, 1e-11, f"mixture species {s}")
+    assert dom.counters()["splits"] > 0
+    dom.close()
