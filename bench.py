@@ -19,7 +19,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -31,6 +30,14 @@ sys.path.insert(0, os.path.join(ROOT, "merzbild.jl_gb300"))
 
 L_DOMAIN, NDENS, T_WALL, V_WALL = 5e-4, 1e23, 273.0, 500.0
 ALG_BYTES = 112  # per particle-step: every particle read once and written once (7 FP64)
+# ncu figures of the Couette step's particle kernels at 10,000 cells x 400
+# particles (the capture-size rule keeps full-size launches out of ncu):
+# DRAM bytes moved per particle by the two-launch step (gather + props, then
+# NTC + convection) and by the one-launch step, and the FP64 warp
+# instructions per particle of a whole step
+DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH = 256.7
+DRAM_BYTES_PER_PARTICLE_FUSED = 386.6
+FP64_WARP_INST_PER_PARTICLE = 0.814
 
 
 def parse():
@@ -41,13 +48,14 @@ def parse():
     p.add_argument("--impl", default="merzgpu", choices=["merzgpu", "reference"])
     p.add_argument("--cells", type=int, default=50000)
     p.add_argument("--ppc", type=int, default=400)
-    p.add_argument("--plain-steps", type=int, default=1)
+    p.add_argument("--plain-steps", type=int, default=5)
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-extra", action="store_true",
                    help="skip the batched 0-D, variable-weight Couette, serving and largest-request measurements")
-    p.add_argument("--only-extra", default=None, choices=["batched_0d", "varweight", "serving", "largest_request"],
+    p.add_argument("--only-extra", default=None,
+                   choices=["batched_0d", "varweight", "serving", "largest_request", "readme_0d"],
                    help="run one of the extra measurements alone and print its result")
     p.add_argument("--seed", type=int, default=1234)
     p.add_argument("--launches", type=int, default=0, choices=[0, 1, 2],
@@ -245,34 +253,117 @@ def batched_0d(mz, ctx, seed, steps=20, warmup=2):
     dom.step(plan(warmup), steps, inst)
     ms = ctx.timer_stop()
     cnt = dom.counters(reset=True)
-    # plain: one launch sequence per cell (the reference's call granularity)
+    # plain: whole-domain standalone calls per step (ntc_equal_weight! over
+    # every cell, then compute_props!), no graph, no fusion
+    plain_steps = 3
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for k in range(plain_steps):
+        dom.ntc(0, 0, dt, warmup + steps + 1 + k, equal_weight=True)
+        mz.compute_props(dom, inst)
+    ctx.synchronize()
+    plain_s = (time.perf_counter() - t0) / plain_steps
+    # secondary: one ntc! launch per cell (the reference's call granularity)
     ctx.synchronize()
     t0 = time.perf_counter()
     for c in range(n_cells):
-        dom.ntc(0, 0, dt, warmup + steps + 1, cells=(c, c + 1), equal_weight=True)
+        dom.ntc(0, 0, dt, warmup + steps + plain_steps + 1, cells=(c, c + 1), equal_weight=True)
     mz.compute_props(dom, inst)
     ctx.synchronize()
-    plain_s = time.perf_counter() - t0
+    per_cell_s = time.perf_counter() - t0
     value = n * steps / (ms / 1e3)
     out = {"workload": "0-D Ar relaxation, 65,536 cells, N log-uniform [50, 4000], bi-Maxwellian 2000/300/300 K",
-           "particles": n, "steps": steps, "mapping": {"lanes_per_cell": lanes, "block_per_cell_from": big}, "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
-           "collisions_per_s": cnt["accepted"] / (ms / 1e3), "plain_value": n / plain_s,
+           "particles": n, "steps": steps, "mapping": {"lanes_per_cell": lanes, "block_per_cell_from": big},
+           "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+           "collisions_per_s": cnt["accepted"] / (ms / 1e3),
+           "plain_value": n / plain_s, "plain_ms_per_step": 1e3 * plain_s,
+           "plain_form": "whole-domain standalone calls per step (ntc over every cell, compute_props), no graph",
            "batched_over_plain": value / (n / plain_s),
+           "per_cell_value": n / per_cell_s, "batched_over_per_cell": value / (n / per_cell_s),
            # 0-D step: v and w read (32 B) and v written (24 B) per particle-step
            "hbm_frac_algorithmic": 56.0 * value / (measured_peaks()[0] * 1e9)}
     dom.close()
     return out
 
 
+def readme_0d(mz, ctx, seed, batch=4096, n_steps=800):
+    """The README's 0-D case (README.md:91-106, test_2species.jl): 400 Ar at
+    3000 K and 4000 He at 360 K in one cell, Fnum 5e12, V 1, dt 2.5e-3 s, 800
+    steps of ntc! for (Ar,Ar), (He,Ar), (He,He) and compute_props!.  Plain:
+    one instance, mz_step over its 800 steps (graph-replayed).  Batched:
+    `batch` instances with their own random streams as the cells of one
+    domain, the same 800 steps.  The oracle runs one instance on one host
+    core."""
+    import numpy as np
+
+    sp = [mz.Species("Ar", mz.AR_MASS), mz.Species("He", mz.HE_MASS)]
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    T0, N0, Fnum, dt = (3000.0, 360.0), (400, 4000), 5e12, 2.5e-3
+
+    def run(cells):
+        dom = mz.Domain(ctx, cells, sp, [N0[0] * cells + 64, N0[1] * cells + 64], interactions=inter, seed=seed)
+        for s in range(2):
+            dom.sample_cells(s, [N0[s]] * cells, T0[s], Fnum, step=0)
+        for s1 in range(2):
+            for s2 in range(2):
+                dom.set_sigma_g_w_max(s1, s2, mz.estimate_sigma_g_w_max(inter[s1][s2], sp[s1], sp[s2], T0[s1],
+                                                                        T0[s2], Fnum))
+        inst = mz.PhysProps(dom)
+        p = mz._lib.StepPlan()
+        p.dims, p.collide, p.equal_weight, p.props, p.dt, p.step0, p.use_graph = 0, 1, 1, 1, dt, 0, 1
+        ctx.synchronize()
+        dom.counters(reset=True)
+        ctx.timer_start()
+        dom.step(p, n_steps, inst)
+        ms = ctx.timer_stop()
+        cnt = dom.counters(reset=True)
+        T = inst.fetch()["T"].mean(axis=0)
+        dom.close()
+        ps = cells * sum(N0) * n_steps
+        return {"instances": cells, "value": ps / (ms / 1e3), "unit": "particle-steps/s", "ms_total": ms,
+                "ms_per_step": ms / n_steps, "collisions_per_s": cnt["accepted"] / (ms / 1e3),
+                "T_final_mean": [float(T[0]), float(T[1])]}
+
+    plain = run(1)
+    batched = run(batch)
+    # the oracle: one instance on one host core
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    o = oracle.Oracle(1, 2, [s.mass for s in sp])
+    t = mz.VHS
+    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    for s in range(2):
+        o.pv_create(s, N0[s] + 64)
+        o.sample_equal_weight(s, 1, N0[s], T0[s], Fnum, seed=seed, step=0)
+    o.estimate_sigma_g_w_max(list(T0), Fnum)
+    t0 = time.perf_counter()
+    for tt in range(1, n_steps + 1):
+        for s2 in range(2):
+            for s1 in range(s2, 2):
+                o.ntc_cells(s1, s2, dt, None, seed, tt, equal_weight=True)
+        o.compute_props(mode=0)
+    cpu_s = time.perf_counter() - t0
+    cpu = {"value": sum(N0) * n_steps / cpu_s, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+           "sample": f"one instance, {n_steps} steps"}
+    return {"workload": "README 0-D Ar/He relaxation: 400 Ar at 3000 K + 4000 He at 360 K, Fnum 5e12, V 1, "
+                        "dt 2.5e-3, 800 steps, ntc! for every pair + compute_props! per step",
+            "plain": plain, "batched": batched, "batched_over_plain": batched["value"] / plain["value"],
+            "cpu_oracle": cpu}
+
+
 def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
-    """Variable-weight Couette (test/test_1D_couette_varweight.jl's loop at the
+    """Variable-weight Couette (couette_varweight_octree.jl's loop at the
     configuration's size): 1,000 cells over L = 5e-4 m, Ar at n = 1e23 and
     273 K, 1,000 particles per cell with seeded log-uniform weights over two
     decades, diffuse walls at -/+500 m/s, dt = 0.2 / nu.  One step = ntc! with
     splitting for every cell, octree N:2 merging of the cells above 1,200
-    particles down to 300 (one launch), convection, sort,
-    compute_props_sorted!.  The plain form calls ntc! and the merge cell by
-    cell (the reference's loop) for one step."""
+    particles down to 300, convection, sort, compute_props_sorted!.  Batched:
+    mz_step (device-resident, graph-replayed).  Plain: the same step as
+    whole-domain standalone calls; secondary: ntc! and the merge cell by cell
+    (the reference's loop)."""
     import numpy as np
 
     nx, ppc, threshold, target = 1000, 1000, 1200, 300
@@ -297,8 +388,16 @@ def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
     octree = mz.OctreeN2Merge(max_Nbins=6000)
     props = mz.PhysProps(dom)
 
-    def one_step(step, plain=False):
-        if plain:
+    def plan(step0, k, graph=True):
+        p = mz._lib.StepPlan()
+        p.dims, p.collide, p.equal_weight, p.props = 1, 1, 0, 1
+        p.dt, p.dw_tol, p.step0, p.use_graph = dt, 1e-16, step0, 1 if graph else 0
+        p.grid, p.walls = grid.c_struct(), walls.c_struct()
+        p.merge_threshold, p.merge_target, p.octree = threshold, target, octree.params
+        return p
+
+    def standalone_step(step, per_cell=False):
+        if per_cell:
             for c in range(nx):
                 dom.ntc(0, 0, dt, step, cells=(c, c + 1), equal_weight=False)
                 dom.merge_octree(0, octree, target, threshold=threshold, cells=(c, c + 1), grid=grid, step=step)
@@ -309,44 +408,66 @@ def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
         dom.sort(0, grid)
         mz.compute_props_sorted(dom, props)
 
-    for t in range(1, warmup + 1):
-        one_step(t)
-    dom.counters(reset=True)
+    dom.step(plan(0, warmup), warmup, props)
+    # per-kernel shares: the same steps with every launch bracketed by events
+    # (no graph: a graph's launches are not timed one by one)
+    ctx.set_kernel_timing(True)
+    dom.step(plan(warmup, steps, graph=False), steps, props)
     ctx.synchronize()
+    timings = ctx.kernel_timings()
+    ctx.set_kernel_timing(False)
+    ctx.synchronize()
+    n_start = dom.info(0)["n_total"]
+    dom.counters(reset=True)
     ctx.timer_start()
-    live = 0
-    for t in range(warmup + 1, warmup + steps + 1):
-        live += dom.info(0)["n_total"]
-        one_step(t)
+    dom.step(plan(warmup + steps, steps), steps, props)
     ms = ctx.timer_stop()
     cnt = dom.counters(reset=True)
+    n_end = dom.info(0)["n_total"]
+    live = 0.5 * (n_start + n_end)
+    # plain: whole-domain standalone calls, then the per-cell form
+    t_plain = warmup + 2 * steps + 1
     ctx.synchronize()
     n_plain = dom.info(0)["n_total"]
     t0 = time.perf_counter()
-    one_step(warmup + steps + 1, plain=True)
+    for k in range(3):
+        standalone_step(t_plain + k)
     ctx.synchronize()
-    plain_s = time.perf_counter() - t0
-    value = live / (ms / 1e3)
+    plain_s = (time.perf_counter() - t0) / 3
+    n_pc = dom.info(0)["n_total"]
+    t0 = time.perf_counter()
+    standalone_step(t_plain + 3, per_cell=True)
+    ctx.synchronize()
+    per_cell_s = time.perf_counter() - t0
+    value = live * steps / (ms / 1e3)
+    tot = sum(v[0] for v in timings.values()) or 1.0
     out = {"workload": "1-D Couette, variable weight (2 decades), 1,000 cells x 1,000 initial particles, "
                        "ntc! with splitting + octree merge 1,200 -> 300 + convect + sort + props",
-           "mean_live_particles": live / steps, "steps": steps, "value": value, "unit": "particle-steps/s",
+           "mean_live_particles": live, "steps": steps, "value": value, "unit": "particle-steps/s",
            "ms_per_step": ms / steps, "collisions_per_s": cnt["accepted"] / (ms / 1e3),
            "splits_per_step": cnt["splits"] / steps, "merged_cells_per_step": cnt["merges"] / steps,
-           "plain_value": n_plain / plain_s, "batched_over_plain": value / (n_plain / plain_s),
+           "form": "mz_step, device-resident and graph-replayed",
+           "plain_value": n_plain / plain_s, "plain_ms_per_step": 1e3 * plain_s,
+           "plain_form": "whole-domain standalone calls per step (ntc, merge, convect, sort, props)",
+           "batched_over_plain": value / (n_plain / plain_s),
+           "per_cell_value": n_pc / per_cell_s, "batched_over_per_cell": value / (n_pc / per_cell_s),
+           "kernel_share": {k: round(v[0] / tot, 4) for k, v in sorted(timings.items(), key=lambda kv: -kv[1][0])},
            # 1-D step: every live particle read and written once (56 B each way)
            "hbm_frac_algorithmic": 112.0 * value / (measured_peaks()[0] * 1e9)}
     dom.close()
     return out
 
 
-def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
+def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=50):
     """Serving loop: seeded Poisson arrivals (mean `rate` per s over `window_s`)
     of 0-D relaxation requests, 70 % Ar and 30 % Ar + He, particles
     log-uniform in [200, 200,000] per species, temperatures uniform in [300,
     5000] K, steps uniform in [50, 2000]; a common number density (Fnum = n V /
-    N), dt = 2.5e-3 s.  Requests are admitted by slots and a particle budget,
+    N), dt = 2.5e-3 s.  Requests are admitted by free slots and free device
+    memory (the server's storage grows into free HBM, 2 GiB kept free), and
     co-batched per step; p50 / p99 latency from arrival to result.  The plain
-    form runs requests one at a time on the same GPU."""
+    form runs the first `plain_sample` requests one at a time on the same
+    GPU."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -362,13 +483,13 @@ def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
         T = [rng.uniform(300.0, 5000.0), rng.uniform(300.0, 5000.0) if two else 0.0]
         reqs.append((float(t), dict(counts=c, T=T, Fnum=2.2e16 / sum(c), n_steps=int(rng.integers(50, 2001)),
                                     seed=int(seed) * 100_000 + k)))
-    srv = mz.Server(ctx, sp, inter, 2.5e-3, 1024, [40_000_000, 40_000_000])
+    srv = mz.Server(ctx, sp, inter, 2.5e-3, 1024, 0)
     lat, ids, elapsed = srv.serve(reqs)
     info = srv.info()
     srv.close()
     lat = np.array(lat)
     # plain: the first requests one at a time (arrival at 0, no overlap)
-    one = mz.Server(ctx, sp, inter, 2.5e-3, 1, [400_000, 400_000])
+    one = mz.Server(ctx, sp, inter, 2.5e-3, 1, 0)
     ps = 0
     t0 = time.perf_counter()
     for _, kw in reqs[:plain_sample]:
@@ -381,6 +502,7 @@ def serving(mz, ctx, seed, window_s=3.0, rate=200.0, plain_sample=6):
             "requests": len(reqs), "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "value": info["particle_steps"] / elapsed,
             "unit": "particle-steps/s", "elapsed_s": elapsed, "server_steps": info["steps"],
+            "admission": "free slots and free device memory (cudaMemGetInfo less 2 GiB)",
             "plain_value": ps / plain_s, "plain_sample": f"first {plain_sample} requests one at a time",
             "batched_over_plain": (info["particle_steps"] / elapsed) / (ps / plain_s)}
 
@@ -500,7 +622,7 @@ def run_gpu(args):
     seed = args.seed + 7919 * rank  # independent replicas
     if args.only_extra:
         fn = {"batched_0d": batched_0d, "varweight": varweight_couette, "serving": serving,
-              "largest_request": largest_request}[args.only_extra]
+              "largest_request": largest_request, "readme_0d": readme_0d}[args.only_extra]
         print(json.dumps({args.only_extra: fn(mz, ctx, seed)}), flush=True)
         ctx.close()
         return
@@ -571,46 +693,36 @@ def run_gpu(args):
         avg_launch_s = kms / klaunch / 1e3
     peak, peak_kind = measured_peaks()
     achieved = ALG_BYTES * n / avg_launch_s / 1e9
-    # DRAM bytes per particle of the step's particle kernel(s) from the
-    # committed ncu summary (captured on a smaller case; traffic scales with
-    # particles)
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "step_cell_traffic.md")
-    if os.path.exists(tfile):
-        key = "dram_bytes_per_particle_two_launch" if two else "dram_bytes_per_particle"
-        with open(tfile) as f:
-            m = re.search(r"^" + key + r":\s*([0-9.eE+-]+)", f.read(), re.M)
-        if m:
-            traffic = float(m.group(1)) * n
+    # DRAM bytes per particle of the step's particle kernel(s), measured with
+    # ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the same step at
+    # 10,000 cells x 400 particles; traffic scales with the particles a launch
+    # moves, so it is scaled to this launch's particle count
+    traffic = (DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH if two else DRAM_BYTES_PER_PARTICLE_FUSED) * n
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": ALG_BYTES * n,
                 "kernel_share": {k: v[0] / tot for k, v in sorted(timings.items(), key=lambda kv: -kv[1][0])}}
     # secondary bound: the FP64 pipe.  GB300 spends 16 SM cycles on every FP64
     # warp instruction (2 DFMA per SM per clock); the step's FP64 warp
-    # instructions per particle come from the committed ncu capture of the
-    # full-step kernel (0.81: collisions, convection, both props passes), so
-    # their pipe time at the clock seen during the timed region is a floor
-    ffile = os.path.join(ROOT, "profiles", "step_cell_couette_4e6.md")
-    if os.path.exists(ffile):
-        with open(ffile) as f:
-            m = re.search(r"^fp64_warp_inst_per_particle:\s*([0-9.eE+-]+)", f.read(), re.M)
-        if m:
-            inst_pp = float(m.group(1))
-            ck = clk if isinstance(clk, dict) else {}
-            sm_hz = 1e6 * (ck.get("sm_mhz") or ck.get("sm_max_mhz") or 2070.0)
-            import torch
+    # instructions per particle (collisions, convection, both props passes)
+    # were counted with ncu on the full-step kernel, so their pipe time at the
+    # clock seen during the timed region is a floor
+    ck = clk if isinstance(clk, dict) else {}
+    sm_hz = 1e6 * (ck.get("sm_mhz") or ck.get("sm_max_mhz") or 2070.0)
+    import torch
 
-            n_sms = torch.cuda.get_device_properties(local).multi_processor_count
-            floor_s = inst_pp * n * 16.0 / (n_sms * sm_hz)
-            roofline["secondary"] = {
-                "bound": "fp64", "fp64_warp_inst_per_particle": inst_pp, "pipe_cycles_per_warp_inst": 16,
-                "sm_mhz": sm_hz / 1e6, "floor_ms_per_step": floor_s * 1e3,
-                "frac": floor_s / (ms / K / 1e3),
-                "source": "ncu capture of the full-step kernel, 4e6 particles (profiles/step_cell_couette_4e6.md)"}
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    floor_s = FP64_WARP_INST_PER_PARTICLE * n * 16.0 / (n_sms * sm_hz)
+    roofline["secondary"] = {
+        "bound": "fp64", "fp64_warp_inst_per_particle": FP64_WARP_INST_PER_PARTICLE,
+        "pipe_cycles_per_warp_inst": 16, "sm_mhz": sm_hz / 1e6, "floor_ms_per_step": floor_s * 1e3,
+        "frac": floor_s / (ms / K / 1e3),
+        "source": "ncu instruction counts of the full-step kernel at 10,000 cells x 400 particles"}
 
-    # plain form: the reference's call granularity -- one ntc launch per cell,
-    # then convect, sort and props as separate calls
+    # plain form: the same step as whole-domain standalone entry points, one
+    # call each per step with no graph and no fusion (ntc_equal_weight! over
+    # every cell, convect_particles!, sort_particles!, compute_props_sorted!);
+    # secondary: the reference's call granularity, one ntc! call per cell
     plain = None
     log("roofline: " + json.dumps({k: (v if not isinstance(v, dict) else None) for k, v in roofline.items()}))
     if not args.no_plain and rank == 0:
@@ -620,17 +732,31 @@ def run_gpu(args):
         t0 = time.perf_counter()
         for _ in range(args.plain_steps):
             rng.next_step()
-            for c in range(args.cells):
-                mz.ntc_equal_weight(rng, dom, c, 0, dt)
+            dom.ntc(0, 0, dt, rng.step, equal_weight=True)
             mz.convect_particles(rng, grid, walls, dom, 0, dt)
             mz.sort_particles(dom, 0, grid)
             mz.compute_props_sorted(dom, pp)
         ctx.synchronize()
         el = time.perf_counter() - t0
         pv = n * args.plain_steps / el
+        rng.next_step()
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for c in range(args.cells):
+            mz.ntc_equal_weight(rng, dom, c, 0, dt)
+        mz.convect_particles(rng, grid, walls, dom, 0, dt)
+        mz.sort_particles(dom, 0, grid)
+        mz.compute_props_sorted(dom, pp)
+        ctx.synchronize()
+        el1 = time.perf_counter() - t0
         plain = {"value": pv, "unit": "particle-steps/s", "steps": args.plain_steps,
-                 "ms_per_step": 1e3 * el / args.plain_steps, "launches_per_step": args.cells + 6,
-                 "batched_over_plain": value / world / pv}
+                 "ms_per_step": 1e3 * el / args.plain_steps, "launches_per_step": 7,
+                 "form": "whole-domain standalone entry points per step (ntc, convect, sort, props), no graph",
+                 "batched_over_plain": value / world / pv,
+                 "per_cell": {"value": n / el1, "ms_per_step": 1e3 * el1, "launches_per_step": args.cells + 6,
+                              "form": "one ntc! call per cell (the reference's call granularity), then "
+                                      "convect, sort, props",
+                              "batched_over_per_cell": value / world / (n / el1)}}
 
     # end to end through the C ABI with host buffers: upload the initial state,
     # K steps, read the cell properties back every step
@@ -675,7 +801,7 @@ def run_gpu(args):
         for a in (hw, hv, hx, hc, *snaps):
             a.close()
 
-    extra_0d = extra_srv = extra_vw = extra_big = None
+    extra_0d = extra_srv = extra_vw = extra_big = extra_readme = None
     log(f"e2e: {e2e}")
     if not args.no_extra and rank == 0:
         extra_0d = batched_0d(mz, ctx, seed)
@@ -686,6 +812,8 @@ def run_gpu(args):
         log(f"serving: {extra_srv}")
         extra_big = largest_request(mz, ctx, seed)
         log(f"largest request: {extra_big}")
+        extra_readme = readme_0d(mz, ctx, seed)
+        log(f"README 0-D: {extra_readme}")
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
@@ -696,15 +824,15 @@ def run_gpu(args):
         out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
                "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, sampled on the device)",
-               "config": workload(args) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                                           "mapping": {"lanes_per_cell": mapping[0],
-                                                       "launches_per_step": 2 if mapping[1] == 1 else 1,
-                                                       "autotune_steps": tune_steps}},
+               "config": workload(args),
+               "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+               "mapping": {"lanes_per_cell": mapping[0], "launches_per_step": 2 if mapping[1] == 1 else 1,
+                           "autotune_steps": tune_steps},
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),
                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
                "plain": plain, "batched_0d": extra_0d, "varweight_couette": extra_vw, "serving": extra_srv,
-               "largest_request": extra_big}
+               "largest_request": extra_big, "readme_0d": extra_readme}
         print(json.dumps(out), flush=True)
     ctx.close()
 

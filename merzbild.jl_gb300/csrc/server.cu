@@ -256,6 +256,11 @@ struct mz_server_s {
     std::unordered_map<int64_t, ReqRec> reqs;
     std::vector<int64_t> retired;   // ids retired by the last mz_server_step(_many) call
     int64_t particle_steps = 0;
+    // admission by free device memory (created with capacity 0): the lanes'
+    // particle storage grows at admission while cudaMemGetInfo's free bytes,
+    // less `headroom`, cover the larger storage; otherwise the request waits
+    bool hbm = false;
+    int64_t headroom = (int64_t)2 << 30;
 };
 
 namespace {
@@ -275,6 +280,29 @@ void ensure_rng_arrays(mz_domain* d)
         MZ_CK(cudaMalloc(&d->d_cell_step, n * sizeof(uint32_t)));
         MZ_CK(cudaMemsetAsync(d->d_cell_step, 0, n * sizeof(uint32_t), d->ctx->stream));
     }
+}
+
+// device bytes one particle slot of a species holds: two buffers of both
+// 32-byte records and the owner cell, plus the sort key and ticket
+constexpr int64_t SLOT_BYTES = 2 * (int64_t)(sizeof(PV) + sizeof(PX) + sizeof(int32_t)) + 2 * (int64_t)sizeof(int32_t);
+
+// free-memory admission: grow species s of lane domain d to hold `need`
+// slots if the device's free memory less the headroom allows (the old
+// storage is freed after the copy, so the new one must fit beside it)
+bool grow_for(mz_server* sv, mz_domain* d, int s, int64_t need)
+{
+    if (!sv->hbm) return false;
+    size_t free_b = 0, total_b = 0;
+    MZ_CK(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t avail = (int64_t)free_b - sv->headroom;
+    const int64_t cap = d->sp[s].capacity;
+    for (const int64_t want : {std::max<int64_t>(need, 2 * cap) + 1024, need + 1024}) {
+        if (want * SLOT_BYTES <= avail && want < (1ll << 31) - 2048) {
+            reserve_species(d, s, want);
+            return true;
+        }
+    }
+    return false;
 }
 
 // admit queued requests while slots and storage allow; FIFO, no overtaking
@@ -299,7 +327,8 @@ void admit(mz_server* sv, ServerLane& L)
             if (S.hw + want > S.capacity) {
                 // dead slots of retired requests block the admission: compact
                 if (S.n_total + want <= S.capacity && need[s] == 0 && !S.compact) launch_compact(d, s);
-                if (S.hw + want > S.capacity) fits = false;
+                // grow the storage into free device memory, or wait
+                if (S.hw + want > S.capacity && !grow_for(sv, d, s, S.hw + want)) fits = false;
             }
         }
         if (!fits) break;
@@ -516,6 +545,12 @@ int mz_server_create(mz_ctx* c, int32_t n_species, const double* mass, const mz_
     sv->ns = n_species;
     sv->slots = max_requests;
     sv->dt = dt;
+    int64_t cap[MZ_MAX_SPECIES];
+    for (int s = 0; s < n_species; ++s) {
+        // capacity 0: admission by free device memory, storage grown on demand
+        if (capacity[s] <= 0) sv->hbm = true;
+        cap[s] = capacity[s] > 0 ? capacity[s] : 4096;
+    }
     // each lane on streams of its own, so that the two overlap
     for (int l = 0; l < 2; ++l) {
         mz_ctx* cl = nullptr;
@@ -523,7 +558,7 @@ int mz_server_create(mz_ctx* c, int32_t n_species, const double* mass, const mz_
         if (rc != MZ_OK) throw MzError(rc, "mz_server_create: lane streams");
         sv->lane[l].ctx = cl;  // freed with the lane if the set-up throws
         sv->lane[l].own_ctx = true;
-        lane_init(sv, sv->lane[l], cl, true, max_requests, capacity, mass, inter);
+        lane_init(sv, sv->lane[l], cl, true, max_requests, cap, mass, inter);
     }
     *out = sv;
     guard.p = nullptr;
@@ -538,6 +573,14 @@ int mz_server_destroy(mz_server* sv)
     lane_free(sv->lane[1]);
     delete sv;
     return MZ_OK;
+}
+
+int mz_server_set_hbm_headroom(mz_server* sv, int64_t bytes)
+{
+    API_TRY
+    MZ_REQUIRE(sv && bytes >= 0, "mz_server_set_hbm_headroom: bad argument");
+    sv->headroom = bytes;
+    API_CATCH(sv ? sv->ctx : nullptr)
 }
 
 /* requests of at least `particles` particles (all species) run in the lane
@@ -555,9 +598,16 @@ int mz_server_submit(mz_server* sv, const mz_request* r, int64_t* id)
     API_TRY
     MZ_REQUIRE(sv && r && id, "mz_server_submit: NULL argument");
     MZ_REQUIRE(r->n_steps >= 1 && r->Fnum > 0.0 && r->V > 0.0, "mz_server_submit: bad request");
+    size_t free_b = 0, total_b = 0;
+    if (sv->hbm) MZ_CK(cudaMemGetInfo(&free_b, &total_b));
     for (int s = 0; s < sv->ns; ++s) {
-        MZ_REQUIRE(r->count[s] >= 0 && r->count[s] <= sv->lane[0].dom->sp[s].capacity,
-                   "mz_server_submit: request larger than the particle budget");
+        if (sv->hbm)
+            MZ_REQUIRE(r->count[s] >= 0 && r->count[s] < (1ll << 31) - 4096 &&
+                           r->count[s] * SLOT_BYTES <= (int64_t)total_b - sv->headroom,
+                       "mz_server_submit: request larger than the device memory less the headroom");
+        else
+            MZ_REQUIRE(r->count[s] >= 0 && r->count[s] <= sv->lane[0].dom->sp[s].capacity,
+                       "mz_server_submit: request larger than the particle budget");
         MZ_REQUIRE(r->count[s] == 0 || r->T[s] > 0.0, "mz_server_submit: temperature must be positive");
     }
     int64_t total = 0;

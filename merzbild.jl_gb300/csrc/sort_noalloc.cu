@@ -15,9 +15,14 @@
 // output, all in device memory, and the stream.  The scratch array is shared
 // by every call: each call clears what must start at zero, and calls that
 // overlap on the GPU (different streams or devices sharing it concurrently on
-// one device) race on it -- serialise them.
+// one device) race on it -- serialise them.  Before returning, a call waits
+// for its stream (a wait on that stream alone, not the device-wide
+// synchronisation an allocation or free can take) to read the word that
+// reports keys outside [0, n_cells).
 #include "mz_host.h"
 #include "sortnet.cuh"
+
+#include <cuda.h>
 
 #include <cstdio>
 #include <mutex>
@@ -32,7 +37,44 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) int32_t g_noalloc_scratch[2 * MZ_NOALLOC_MAX_CELLS + 64];
 
 std::mutex g_mutex;
-int32_t* g_scratch_addr[kMaxDevices] = {nullptr};
+// the array's device address per device, and the id of the CUDA context it
+// belongs to: a device's primary context that was reset (cudaDeviceReset) is
+// recreated with a new id and the array with a new address
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    int32_t* addr;
+};
+ScratchAddr g_scratch[kMaxDevices] = {};
+
+// unique id of the calling thread's current CUDA context (cuCtxGetId, taken
+// from the driver through the runtime so the library needs no libcuda link);
+// 0 when there is none or the driver cannot say
+unsigned long long current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
 
 __device__ __forceinline__ int32_t clamp_key(int32_t k, int32_t n_cells, int32_t* status)
 {
@@ -155,23 +197,27 @@ __global__ void __launch_bounds__(256) k_na_segments(int32_t n_cells, const int3
     }
 }
 
-// device address of the scratch array for the current device, looked up once
+// device address of the scratch array for the current device: looked up
+// (cudaGetSymbolAddress, with the device current) on the first call in each
+// CUDA context of the device, then taken from the cache
 int32_t* scratch_for_current_device(int* device_out)
 {
     int dev = 0;
     MZ_CK(cudaGetDevice(&dev));
     MZ_REQUIRE(dev >= 0 && dev < kMaxDevices, "mz_sort_keys_noalloc: device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            throw MzError(MZ_E_CUDA, std::string("mz_sort_keys_noalloc: cudaGetSymbolAddress: ") +
-                                         cudaGetErrorString(e));
-        g_scratch_addr[dev] = (int32_t*)p;
-    }
     *device_out = dev;
-    return g_scratch_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (id != 0 && g_scratch[dev].ctx_id == id && g_scratch[dev].addr) return g_scratch[dev].addr;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        throw MzError(MZ_E_CUDA, std::string("mz_sort_keys_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    // the lookup made the device's context current on this thread; without a
+    // context id (an old driver) the address is looked up on every call
+    g_scratch[dev].ctx_id = current_context_id();
+    g_scratch[dev].addr = static_cast<int32_t*>(p);
+    return g_scratch[dev].addr;
 }
 
 }  // namespace

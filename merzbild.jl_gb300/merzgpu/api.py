@@ -380,6 +380,34 @@ class Domain:
                        np.int64)
         return out, nt.value
 
+    # validators (particles.jl:805-1025) -----------------------------------
+    def _check(self, species, mode):
+        ok, detail = C.c_int32(), C.c_int64()
+        self._ck(lib().mz_check_indexing(self.h, int(species), int(mode), C.byref(ok), C.byref(detail)))
+        return bool(ok.value), int(detail.value)
+
+    def check_pia_is_correct(self, species):
+        """(True, 0), or (False, first bad cell 1-based), or (False, 0) for a wrong n_total."""
+        return self._check(species, 0)
+
+    def check_unique_index(self, species):
+        """(True, 0), or (False, n_index / -n_index / -1) as the reference returns."""
+        return self._check(species, 1)
+
+    def check_unique_buffer(self, species):
+        return self._check(species, 2)
+
+    def count_disordered_particles(self, species, use_offset=True):
+        return self._check(species, 3 if use_offset else 4)[1]
+
+    def set_indexer(self, species, indexer, n_total):
+        """Write indexer rows (n_local, start1, end1, n_group1, start2, end2,
+        n_group2), 0-based, as given (mz_set_indexer)."""
+        ind = (L.ParticleIndexer * self.n_cells)()
+        for c in range(self.n_cells):
+            ind[c] = L.ParticleIndexer(*[int(a) for a in indexer[c]])
+        self._ck(lib().mz_set_indexer(self.h, int(species), ind, int(n_total)))
+
     # collisions ----------------------------------------------------------
     def set_sigma_g_w_max(self, s1, s2, values):
         v = f64(np.broadcast_to(np.asarray(values, float), (self.n_cells,)))
@@ -648,6 +676,11 @@ class Server:
         """mz_server_set_lane_split: requests of at least `particles` particles
         go to the lane of large requests (0: one lane for all)."""
         self._ck(lib().mz_server_set_lane_split(self.h, int(particles)))
+
+    def set_hbm_headroom(self, nbytes):
+        """mz_server_set_hbm_headroom: device memory that admission by free
+        memory (a server created with capacity 0) leaves free."""
+        self._ck(lib().mz_server_set_hbm_headroom(self.h, int(nbytes)))
 
     def submit(self, counts, T, Fnum, n_steps, seed, V=1.0):
         r = L.Request()

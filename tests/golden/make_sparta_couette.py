@@ -1,6 +1,7 @@
 """Extract the SPARTA Couette solution that ships with the reference's tests
-into tests/golden/sparta_couette.json (run in a checkout that has the
-reference next to it; the JSON is committed).
+into tests/golden/sparta_couette.json (the JSON is committed).
+
+Usage: python tests/golden/make_sparta_couette.py <reference>/test/data/external
 
 Source files (reference repository, test/data/external): in.Couette (the
 SPARTA input: 50 cells over 5e-4 m, Ar VHS d = 4.11e-10 m, omega = 0.81,
@@ -16,7 +17,9 @@ import json
 import os
 import sys
 
-SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test/data/external"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_sparta_couette.py <directory holding in.Couette and the *.grid.50000 files>")
+SRC = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "sparta_couette.json")
 
 

@@ -164,3 +164,46 @@ def test_two_lanes_give_the_results_of_one(ctx):
         assert m["state"] == mz._lib.MZ_REQ_DONE and a["steps_done"] == m["steps_done"]
         for key in ("np", "n", "T", "v"):
             assert a[key] == m[key], (seed, key)
+
+
+def test_admission_by_free_device_memory_queues_what_does_not_fit(ctx):
+    """A server created with capacity 0 admits by free device memory: with the
+    headroom set just below the free memory, a request of 1.5 M particles
+    (216 MB of particle storage) waits in its queue while a small request
+    runs and finishes; once the headroom is lowered it is admitted, and its
+    result equals the same request served alone."""
+    torch = pytest.importorskip("torch")
+    big = ((1_500_000, 0), (2000.0, 0.0), 3, 41)
+    small = ((500, 700), (900.0, 400.0), 12, 42)
+    sp = species(["Ar", "He"])
+    inter = mz.interactions_from_vhs(sp, mz.VHS)
+    srv = mz.Server(ctx, sp, inter, DT, 8, 0)
+    srv.set_lane_split(4096)
+    free, _ = torch.cuda.mem_get_info(0)
+    srv.set_hbm_headroom(free - (64 << 20))
+    ids = {}
+    for c, T, n, seed in (big, small):
+        ids[seed] = srv.submit(c, T, _fnum(c), n, seed)
+    for _ in range(40):
+        srv.step(1)
+        if srv.result(ids[42])["state"] == mz._lib.MZ_REQ_DONE:
+            break
+    assert srv.result(ids[42])["state"] == mz._lib.MZ_REQ_DONE
+    assert srv.result(ids[41])["state"] == mz._lib.MZ_REQ_QUEUED
+    srv.set_hbm_headroom(1 << 30)
+    for _ in range(40):
+        srv.step(1)
+        if srv.result(ids[41])["state"] == mz._lib.MZ_REQ_DONE:
+            break
+    mixed = srv.result(ids[41])
+    assert mixed["state"] == mz._lib.MZ_REQ_DONE
+    srv.close()
+    alone = _run(_server(ctx, capacity=2_000_000), [big])[41]
+    for k in ("np", "n", "v", "T"):
+        assert np.array_equal(np.asarray(mixed[k]), np.asarray(alone[k])), k
+    # a request larger than the whole device memory less the headroom is refused
+    srv = mz.Server(ctx, sp, inter, DT, 4, 0)
+    _, total = torch.cuda.mem_get_info(0)
+    with pytest.raises(Exception):
+        srv.submit((total // 100, 0), (300.0, 0.0), 1e10, 1, 7)
+    srv.close()

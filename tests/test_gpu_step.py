@@ -102,7 +102,8 @@ def test_fused_couette_matches_reference_loop(ctx, orc, graph, steps):
     cf = dom.collision_factors(0, 0)
     smax, cnt = o.cf_get(0, 0)
     assert np.array_equal(cf["n_coll_performed"], cnt[:, 3])
-    assert dom.counters()["accepted"] == np.int64(0) + dom.counters()["accepted"]  # counters readable
+    # the device counters add up the per-cell collisions of every step
+    assert dom.counters()["accepted"] >= int(cf["n_coll_performed"].sum()) > 0
 
 
 def test_fused_0d_two_species_matches_reference_loop(ctx, orc):

@@ -64,3 +64,46 @@ def test_noalloc_sort_matches_regular_sort_on_consecutive_calls():
     assert lib.mz_sort_keys_noalloc(stream, None, 0, mz._lib.NOALLOC_MAX_CELLS + 1, None,
                                     C.c_void_p(d_start.data_ptr())) == mz._lib.MZ_E_ARG
     ctx.close()
+
+
+def test_noalloc_sort_at_its_maximum_and_with_a_bad_key():
+    """At MZ_NOALLOC_MAX_CELLS cells (the one-block scan then runs 256 cells
+    per thread) the permutation is numpy's stable argsort and the cell starts
+    the prefix sums of the counts; a key equal to n_cells is clamped and
+    reported as MZ_E_STATE, and the next call is clean again."""
+    torch = pytest.importorskip("torch")
+    import merzgpu.build as b
+
+    b.build()
+    lib = mz.lib()
+    torch.cuda.set_device(0)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n_cells = mz._lib.NOALLOC_MAX_CELLS
+    rng = np.random.default_rng(11)
+    for n in (3 * n_cells, 1000):
+        keys = rng.integers(0, n_cells, n).astype(np.int32)
+        d_keys = torch.from_numpy(keys).cuda()
+        d_perm = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+        d_start = torch.full((n_cells + 1,), -1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        rc = lib.mz_sort_keys_noalloc(stream, C.c_void_p(d_keys.data_ptr()), n, n_cells,
+                                      C.c_void_p(d_perm.data_ptr()), C.c_void_p(d_start.data_ptr()))
+        assert rc == mz._lib.MZ_OK
+        assert np.array_equal(d_perm.cpu().numpy(), np.argsort(keys, kind="stable").astype(np.int32))
+        start = np.concatenate(([0], np.cumsum(np.bincount(keys, minlength=n_cells))))
+        assert np.array_equal(d_start.cpu().numpy(), start.astype(np.int32))
+    n_cells, n = 50, 400
+    keys = rng.integers(0, n_cells, n).astype(np.int32)
+    keys[123] = n_cells
+    d_keys = torch.from_numpy(keys).cuda()
+    d_perm = torch.zeros((n,), dtype=torch.int32, device="cuda")
+    d_start = torch.zeros((n_cells + 1,), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    args = (stream, C.c_void_p(d_keys.data_ptr()), n, n_cells, C.c_void_p(d_perm.data_ptr()),
+            C.c_void_p(d_start.data_ptr()))
+    assert lib.mz_sort_keys_noalloc(*args) == mz._lib.MZ_E_STATE
+    d_keys[123] = n_cells - 1
+    torch.cuda.synchronize()
+    assert lib.mz_sort_keys_noalloc(*args) == mz._lib.MZ_OK
+    keys[123] = n_cells - 1
+    assert np.array_equal(d_perm.cpu().numpy(), np.argsort(keys, kind="stable").astype(np.int32))
