@@ -408,7 +408,11 @@ def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
         dom.sort(0, grid)
         mz.compute_props_sorted(dom, props)
 
-    dom.step(plan(0, warmup), warmup, props)
+    # the mapping (lanes per cell of the splitting NTC) from timed trial steps
+    lanes, _ = dom.autotune(plan(0, 1), trial_steps=2)
+    tuned = 3 * 2 * 2  # three mappings, two rounds, two steps each
+    dom.step(plan(tuned, warmup), warmup, props)
+    warmup += tuned
     # per-kernel shares: the same steps with every launch bracketed by events
     # (no graph: a graph's launches are not timed one by one)
     ctx.set_kernel_timing(True)
@@ -446,7 +450,7 @@ def varweight_couette(mz, ctx, seed, steps=40, warmup=5):
            "mean_live_particles": live, "steps": steps, "value": value, "unit": "particle-steps/s",
            "ms_per_step": ms / steps, "collisions_per_s": cnt["accepted"] / (ms / 1e3),
            "splits_per_step": cnt["splits"] / steps, "merged_cells_per_step": cnt["merges"] / steps,
-           "form": "mz_step, device-resident and graph-replayed",
+           "form": "mz_step, device-resident and graph-replayed", "lanes_per_cell": lanes,
            "plain_value": n_plain / plain_s, "plain_ms_per_step": 1e3 * plain_s,
            "plain_form": "whole-domain standalone calls per step (ntc, merge, convect, sort, props)",
            "batched_over_plain": value / (n_plain / plain_s),

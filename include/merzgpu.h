@@ -377,15 +377,16 @@ int mz_merge_octree_n2(mz_domain* dom, int32_t species, int64_t cell_begin, int6
  * Maxwellian with per-axis temperatures T3[c][3] (T3 NULL: T3_all) or BKW
  * (distribution 1, T3[c][0] as T), weights Fnum[c] * 10^(span * (2U - 1))
  * (span 0: equal weight), positions uniform in box6[c] = {xlo, xhi, ylo,
- * yhi, zlo, zhi} (NULL: unit cube).  (distributions_and_sampling.jl:432-509,
- * 195-213, grid_uniform1D.jl:117-219) */
+ * yhi, zlo, zhi} (NULL: unit cube), velocity offsets (the keywords vx0, vy0,
+ * vz0) v0[c][3] or, with v0 NULL, v0_all[3] for every cell (both NULL: none).
+ * (distributions_and_sampling.jl:432-509, 195-213, grid_uniform1D.jl:117-219) */
 int mz_sample_cells(mz_domain* dom, int32_t species, const int64_t* counts, const double* T3, const double* T3_all,
                     const double* Fnum, double log10_weight_span, const double* box6, int32_t distribution,
-                    uint64_t step);
-/* sample_particles_equal_weight!(rng, grid, ..., ndens::Float64, T, Fnum)
- * (grid_uniform1D.jl:198-219) */
+                    uint64_t step, const double* v0, const double* v0_all);
+/* sample_particles_equal_weight!(rng, grid, ..., ndens::Float64, T, Fnum; vx0, vy0, vz0)
+ * (grid_uniform1D.jl:198-219); v0 = {vx0, vy0, vz0} or NULL */
 int mz_sample_grid_ndens(mz_domain* dom, int32_t species, const mz_grid1d* grid, double ndens, double T, double Fnum,
-                         uint64_t step);
+                         uint64_t step, const double* v0);
 
 /* ---------------------------------------------------------------- fused step */
 /* n_steps steps of the fused pipeline; inst receives the props of the last
@@ -480,8 +481,10 @@ int mz_server_set_hbm_headroom(mz_server* server, int64_t bytes);
  * 24 * trial_steps steps for 0-D plans and 12 * trial_steps for 1-D, and
  * every mapping gives the same results); the fastest is kept for later
  * mz_step calls whose plan leaves big_cell at 0.  *big_cell_out receives the
- * threshold (0-D) or 1 for the two-launch step (1-D).  No counterpart in the
- * reference. */
+ * threshold (0-D) or 1 for the two-launch step (1-D).  A variable-weight plan
+ * (equal_weight = 0) tries only the lanes per cell of its splitting NTC
+ * (6 * trial_steps steps) and *big_cell_out receives 0.  No counterpart in
+ * the reference. */
 int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
 
 /* ---------------------------------------------------------------- counters */

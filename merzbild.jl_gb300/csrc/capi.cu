@@ -877,7 +877,8 @@ int mz_merge_octree_n2(mz_domain* d, int32_t s, int64_t cb, int64_t ce, int64_t 
 }
 
 int mz_sample_cells(mz_domain* d, int32_t s, const int64_t* counts, const double* T3, const double* T3_all,
-                    const double* Fnum, double span, const double* box6, int32_t distribution, uint64_t step)
+                    const double* Fnum, double span, const double* box6, int32_t distribution, uint64_t step,
+                    const double* v0, const double* v0_all)
 {
     API_TRY
     MZ_REQUIRE(d && counts && Fnum && s >= 0 && s < d->ns, "mz_sample_cells: bad argument");
@@ -885,20 +886,20 @@ int mz_sample_cells(mz_domain* d, int32_t s, const int64_t* counts, const double
     MZ_REQUIRE(distribution == 0 || distribution == 1, "mz_sample_cells: distribution must be 0 or 1");
     MZ_REQUIRE(d->mass[s] > 0.0, "mz_sample_cells: species mass not set");
     MZ_CK(cudaSetDevice(d->ctx->device));
-    launch_sample_cells(d, s, counts, nullptr, T3, T3_all, Fnum, span, box6, distribution, step);
+    launch_sample_cells(d, s, counts, nullptr, T3, T3_all, Fnum, span, box6, distribution, step, v0, v0_all);
     check_status(d);
     API_CATCH(d->ctx)
 }
 
 int mz_sample_grid_ndens(mz_domain* d, int32_t s, const mz_grid1d* g, double ndens, double T, double Fnum,
-                         uint64_t step)
+                         uint64_t step, const double* v0)
 {
     API_TRY
     MZ_REQUIRE(d && g && s >= 0 && s < d->ns && Fnum > 0.0, "mz_sample_grid_ndens: bad argument");
     MZ_REQUIRE(g->n_cells == d->n_cells, "mz_sample_grid_ndens: grid and domain cell counts differ");
     MZ_REQUIRE(d->mass[s] > 0.0, "mz_sample_grid_ndens: species mass not set");
     MZ_CK(cudaSetDevice(d->ctx->device));
-    launch_sample_grid(d, s, g, ndens, T, Fnum, step);
+    launch_sample_grid(d, s, g, ndens, T, Fnum, step, v0);
     check_status(d);
     API_CATCH(d->ctx)
 }

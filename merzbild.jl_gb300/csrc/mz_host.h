@@ -207,8 +207,10 @@ void launch_convect(mz_domain* d, int s, const mz_grid1d* g, const mz_walls1d* w
                     int32_t flags, double* surf = nullptr);
 void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const int32_t* counts_dev,
                          const double* T3, const double* T3_all, const double* Fnum, double span, const double* box6,
-                         int32_t distribution, uint64_t step);
-void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step);
+                         int32_t distribution, uint64_t step, const double* v0 = nullptr,
+                         const double* v0_all = nullptr);
+void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step,
+                        const double* v0_all = nullptr);
 void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold, int64_t target,
                   const mz_octree_params* prm, const mz_grid1d* grid, uint64_t step, int64_t* n_merged);
 // merging inside the fused step: no host synchronisation; the step index and

@@ -30,6 +30,8 @@ struct SampleArgs {
     double dx;
     int dist;             // 0 Maxwellian, 1 BKW
     uint32_t step;
+    const double* v0;     // n_cells x 3 velocity offsets (vx0, vy0, vz0) or nullptr
+    double v0_all[3];     // the offset of every cell when v0 is nullptr
 };
 
 // indexers of the sampled cells (lists appended at base[c])
@@ -115,6 +117,17 @@ __global__ void __launch_bounds__(256) k_sample(DomainView d, int s, SampleArgs 
             vy = sqrt(2.0 * K_B * T[1] / S.mass) * (vr * cos(t2));
             vz = sqrt(2.0 * K_B * T[2] / S.mass) * (vr * sin(t2));
         }
+        // the velocity offset of the keywords vx0, vy0, vz0
+        // (distributions_and_sampling.jl:498-508)
+        if (a.v0) {
+            vx += a.v0[3 * (int64_t)c];
+            vy += a.v0[3 * (int64_t)c + 1];
+            vz += a.v0[3 * (int64_t)c + 2];
+        } else {
+            vx += a.v0_all[0];
+            vy += a.v0_all[1];
+            vz += a.v0_all[2];
+        }
         double w = Fn;
         if (a.span > 0.0) w = Fn * pow(10.0, a.span * (2.0 * st.uniform() - 1.0));
         S.A.wv[q] = PV{w, vx, vy, vz};
@@ -167,7 +180,7 @@ static void run_sample(mz_domain* d, int s, SampleArgs a, int32_t* counts_dev)
 
 void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const int32_t* /*counts_dev*/,
                          const double* T3, const double* T3_all, const double* Fnum, double span, const double* box6,
-                         int32_t distribution, uint64_t step)
+                         int32_t distribution, uint64_t step, const double* v0, const double* v0_all)
 {
     mz_ctx* c = d->ctx;
     const int64_t nc = d->n_cells;
@@ -179,7 +192,7 @@ void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const 
     // device staging: counts -> species fill array (free outside the sort)
     SpeciesHost& S = d->sp[s];
     MZ_CK(cudaMemcpyAsync(S.fill, cnt.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-    double *dT3 = nullptr, *dF = nullptr, *dB = nullptr;
+    double *dT3 = nullptr, *dF = nullptr, *dB = nullptr, *dV0 = nullptr;
     MZ_CK(cudaMalloc(&dF, nc * sizeof(double)));
     MZ_CK(cudaMemcpyAsync(dF, Fnum, nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     if (T3) {
@@ -190,7 +203,13 @@ void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const 
         MZ_CK(cudaMalloc(&dB, 6 * nc * sizeof(double)));
         MZ_CK(cudaMemcpyAsync(dB, box6, 6 * nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     }
+    if (v0) {
+        MZ_CK(cudaMalloc(&dV0, 3 * nc * sizeof(double)));
+        MZ_CK(cudaMemcpyAsync(dV0, v0, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
     SampleArgs a{};
+    a.v0 = dV0;
+    for (int k = 0; k < 3; ++k) a.v0_all[k] = v0_all ? v0_all[k] : 0.0;
     a.T3 = dT3;
     for (int k = 0; k < 3; ++k) a.T3_all[k] = T3_all ? T3_all[k] : 0.0;
     a.Fnum = dF;
@@ -206,14 +225,17 @@ void launch_sample_cells(mz_domain* d, int s, const int64_t* counts_host, const 
         cudaFree(dF);
         cudaFree(dT3);
         cudaFree(dB);
+        cudaFree(dV0);
         throw;
     }
     cudaFree(dF);
     cudaFree(dT3);
     cudaFree(dB);
+    cudaFree(dV0);
 }
 
-void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step)
+void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, double T, double Fnum, uint64_t step,
+                        const double* v0_all)
 {
     mz_ctx* c = d->ctx;
     const int64_t nc = d->n_cells;
@@ -235,6 +257,8 @@ void launch_sample_grid(mz_domain* d, int s, const mz_grid1d* g, double ndens, d
     a.dx = g->dx;
     a.dist = 0;
     a.step = (uint32_t)step;
+    a.v0 = nullptr;
+    for (int k = 0; k < 3; ++k) a.v0_all[k] = v0_all ? v0_all[k] : 0.0;
     try {
         run_sample(d, s, a, S.fill);
         MZ_CK(cudaStreamSynchronize(c->stream));

@@ -1003,16 +1003,25 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
     }
     MZ_CK(cudaMemsetAsync(S.counts, 0, (d->n_cells + 1) * sizeof(int32_t), c->stream));
     const bool want_props = plan->props && (inst || (avg && plan->avg_start > 0));
-    const int G = ntc_group_width(d->n_cells);
+    // lanes per cell of the splitting NTC (the autotuner's choice, else 8):
+    // a batch ends at its first split, so a cell's batches hold ~2-3
+    // candidates and narrow groups let one FP64 instruction serve several
+    // cells; with few cells, one-warp blocks spread the warps over every SM
+    const int G = d->tuned_lanes ? d->tuned_lanes : 8;
     using KNtc = void (*)(DomainView, int, double, const uint32_t*, const int*, const int32_t*, const int32_t*);
     const KNtc kntc = G == 8 ? k_vw_ntc<8> : (G == 16 ? k_vw_ntc<16> : k_vw_ntc<32>);
     const int cblocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells, 256), (int64_t)c->num_sms * 8));
-    const int nblocks =
-        (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells * G, 256), (int64_t)c->num_sms * 16));
+    const int64_t ntc_warps = div_up(d->n_cells, 32 / G);
+    const int ntc_threads = ntc_warps >= 8 * (int64_t)c->num_sms ? 256 : 32;
+    const int nblocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>(div_up(ntc_warps * 32, ntc_threads), (int64_t)c->num_sms * 16 * (256 / ntc_threads)));
+    // the gather takes one cell per warp; with few cells, two-warp blocks
+    // spread them over every SM
+    const int gthreads = d->n_cells >= 8 * 3 * (int64_t)c->num_sms ? 256 : 64;
     int per_sm = 0;
-    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_gather, 256, 0));
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_gather, gthreads, 0));
     const int gblocks = (int)std::max<int64_t>(
-        1, std::min<int64_t>(div_up(d->n_cells, 8), (int64_t)c->num_sms * std::max(per_sm, 1)));
+        1, std::min<int64_t>(div_up(d->n_cells, gthreads / 32), (int64_t)c->num_sms * std::max(per_sm, 1)));
     VwDev* V = d->d_vw;
     const int* abort = &V->abort;
 
@@ -1043,7 +1052,8 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
             }
             MZ_LAUNCH(c, "vw_check", k_vw_check, 1, 1, 0, V, s, (long long)S.capacity);
             if (plan->collide)
-                MZ_LAUNCH(c, "vw_ntc", kntc, nblocks, 256, 0, v, s, plan->dw_tol, d->d_step, abort, S.work, S.fill);
+                MZ_LAUNCH(c, "vw_ntc", kntc, nblocks, ntc_threads, 0, v, s, plan->dw_tol, d->d_step, abort, S.work,
+                          S.fill);
             if (merging)
                 launch_merge_fused(d, s, plan->merge_threshold, plan->merge_target, &plan->octree,
                                    plan->dims == 1 ? &plan->grid : nullptr, d->d_step, abort, d->vw_nmax,
@@ -1069,7 +1079,7 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
             b.props = want_props ? 1 : 0;
             b.physics = 0;
             b.advance = 0;
-            MZ_LAUNCH(c, "step_cell_final", k_cell_gather, gblocks, 256, 0, v, b);
+            MZ_LAUNCH(c, "step_cell_final", k_cell_gather, gblocks, gthreads, 0, v, b);
             S.cur ^= 1;
         };
         const int64_t todo = n_steps - done;
@@ -1133,7 +1143,9 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     const int32_t big_c[4] = {512, 2048, 8192, -1};
     // the second choice: the block-per-cell threshold (0-D) or the fused
     // against the two-launch step (1-D)
-    const int nb = plan->dims == 0 ? 4 : 2;
+    // a variable-weight plan has only the lanes per cell of its splitting NTC
+    const bool vw = !plan->equal_weight;
+    const int nb = vw ? 1 : (plan->dims == 0 ? 4 : 2);
     const int nconf = 3 * nb;
     mz_step_plan p = *plan;
     p.big_cell = 0;
@@ -1145,6 +1157,7 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     MZ_CK(cudaEventCreate(&e1));
     auto apply = [&](int k) {
         d->tuned_lanes = lanes_c[k / nb];
+        if (vw) return;
         d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
         d->tuned_split = plan->dims == 0 ? 0 : k % nb;
     };
@@ -1169,5 +1182,5 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     cudaEventDestroy(e1);
     apply((int)(std::min_element(total.begin(), total.end()) - total.begin()));
     if (lanes_out) *lanes_out = d->tuned_lanes;
-    if (big_out) *big_out = plan->dims == 0 ? d->tuned_big : d->tuned_split;
+    if (big_out) *big_out = vw ? 0 : (plan->dims == 0 ? d->tuned_big : d->tuned_split);
 }

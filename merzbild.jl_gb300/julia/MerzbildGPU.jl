@@ -5,19 +5,27 @@ Julia binding of libmerzgpu.so (include/merzgpu.h): the per-step DSMC path of
 Merzbild.jl (NTC collisions, 1-D convection, grid sorting, cell properties,
 octree merging, sampling) on a GB300 GPU.
 
-The module adds methods to Merzbild's own functions for a device-resident
-particle type, so a time loop written against Merzbild keeps its calls and
-swaps its particle containers:
+The module adds methods to Merzbild's own functions for device containers,
+with the reference's positional arguments, so a time loop written against
+Merzbild keeps its calls and swaps its containers:
 
-    ctx = DeviceContext(0)
-    dp  = DeviceParticles(ctx, n_cells, species_data, interactions, capacity)
+    dp = DeviceParticles(DeviceContext(0), grid, species_data, interaction_data, capacity)
+    particles, pia = device_particles(dp), DevicePIA(dp)
+    collision_factors = create_collision_factors_array(pia, interaction_data, species_data, T, Fnum)
+    rng = DeviceRNG(seed)
     for t in 1:n_timesteps
-        rng.step = t
-        ntc_equal_weight!(rng, dp, (1, n_cells), 1, Δt)
-        convect_particles!(rng, grid, walls, dp, 1, Δt)
-        sort_particles!(grid, dp, 1)
-        compute_props_sorted!(dp, props)
+        for cell in 1:grid.n_cells
+            ntc_equal_weight!(rng, collision_factors[1, 1, cell], collision_data, interaction_data,
+                              particles[1], pia, cell, 1, Δt, grid.cells[cell].V)
+        end
+        convect_particles!(rng, grid, boundaries, particles[1], pia, 1, species_data, Δt)
+        sort_particles!(DeviceGridSort(dp), grid, particles[1], pia, 1)
+        compute_props_sorted!(particles, pia, species_data, phys_props)
     end
+
+Its own forms take ranges of cells (one launch for many cells) and an
+explicit step (`rng.step = t`), and `step!` runs whole fused steps replayed
+from a CUDA graph.
 
 Conventions at the boundary: the C ABI is 0-based (cells, slots); this
 module takes and returns Merzbild's 1-based cells.  Random numbers come from
@@ -27,6 +35,13 @@ carries a seed and the time-step index instead of a generator state.
 module MerzbildGPU
 
 import Merzbild  # setup estimates (estimate_sigma_g_w_max) stay the reference's own
+# the module's methods extend Merzbild's own functions, so a loop written
+# against Merzbild dispatches to the device for device containers
+import Merzbild: ntc!, ntc_equal_weight!, convect_particles!, convect_particles_and_compute_cell!, sort_particles!,
+                 squash_pia!, compute_props!, compute_props_sorted!, compute_props_with_total_moments!,
+                 avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, swpm!,
+                 write_netcdf, close_netcdf, create_collision_factors_array, check_pia_is_correct,
+                 check_unique_index, check_unique_buffer, count_disordered_particles
 
 export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, DeviceWalls1D, DeviceOctree,
        upload!, download, ntc!, ntc_equal_weight!, convect_particles!, convect_particles_and_compute_cell!,
@@ -34,7 +49,10 @@ export DeviceContext, DeviceParticles, DeviceProps, DeviceRNG, DeviceGrid1D, Dev
        avg_props!, clear_props!, merge_octree_N2_based!, sample_particles_equal_weight!, step!, counters,
        DeviceSurfProps, set_step_surface!, DeviceNCDataHolder, DeviceNCDataHolderSurf, write_netcdf, close_netcdf,
        swpm!, create_collision_factors_swpm_array!, snapshot!, snapshot_wait, unpack_snapshot!, pinned_vector,
-       free_pinned!, DeviceServer, submit!, server_step!, request_result, retired_requests, set_lane_split!
+       free_pinned!, DeviceServer, submit!, server_step!, request_result, retired_requests, set_lane_split!,
+       set_hbm_headroom!, DevicePIA, DeviceParticleVector, device_particles, DeviceCollisionFactors, DeviceGridSort,
+       set_cell_volumes!, set_indexer!, check_pia_is_correct, check_unique_index, check_unique_buffer,
+       count_disordered_particles, create_collision_factors_array
 
 const libmz = joinpath(@__DIR__, "..", "merzgpu", "lib", "libmerzgpu.so")
 const MZ_MAX_SPECIES = 4
@@ -96,6 +114,8 @@ struct MzStepPlan
     use_graph::Int32; big_cell::Int32
     grid::DeviceGrid1D; walls::DeviceWalls1D
     launches::Int32
+    hit_queue_capacity::Int64
+    merge_threshold::Int64; merge_target::Int64; octree::DeviceOctree
 end
 
 # ------------------------------------------------------------------ handles
@@ -115,6 +135,7 @@ mutable struct DeviceParticles
     ptr::Ptr{Cvoid}
     n_cells::Int
     n_species::Int
+    V::Vector{Float64}   # host copy of the cell volumes on the device
 end
 
 """
@@ -129,7 +150,7 @@ function DeviceParticles(ctx::DeviceContext, n_cells, species_data, interactions
     r = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:mz_domain_create, libmz), Cint, (Ptr{Cvoid}, Int64, Int32, Ptr{Int64}, Ref{Ptr{Cvoid}}),
                 ctx.ptr, n_cells, ns, cap, r), ctx)
-    dp = DeviceParticles(ctx, r[], n_cells, ns)
+    dp = DeviceParticles(ctx, r[], n_cells, ns, ones(n_cells))
     finalizer(d -> ccall((:mz_domain_destroy, libmz), Cint, (Ptr{Cvoid},), d.ptr), dp)
     check(ccall((:mz_set_species, libmz), Cint, (Ptr{Cvoid}, Ptr{Float64}), dp.ptr, [s.mass for s in species_data]), ctx)
     tab = [MzInteraction(interactions[s1, s2].m_r, interactions[s1, s2].μ1, interactions[s1, s2].μ2,
@@ -164,12 +185,33 @@ function DeviceProps(dp::DeviceParticles; moments_list=Int32[], Tref=300.0, nden
     p
 end
 
-"""Seed and time-step index of the counter-based streams (replaces `rng`)."""
+"""
+Seed and time-step index of the counter-based streams (replaces `rng`).
+
+The functions with the reference's signatures (`ntc!(rng, collision_factors,
+...)` etc.) advance `step` themselves: a call that comes back to a cell that
+the same kind of call (and species pair) already drew for in the current
+step starts the next step -- the reference's drivers visit every cell once per
+step in increasing order.  The functions of this module's own forms take
+`step` as it is.
+"""
 mutable struct DeviceRNG
     seed::UInt64
     step::UInt64
+    seen::Dict{Tuple{Symbol,Int,Int},Int}  # (kind, species1, species2) => last cell drawn for in this step
 end
-DeviceRNG(seed::Integer) = DeviceRNG(UInt64(seed), UInt64(0))
+DeviceRNG(seed::Integer) = DeviceRNG(UInt64(seed), UInt64(0), Dict{Tuple{Symbol,Int,Int},Int}())
+DeviceRNG(seed::Integer, step::Integer) = DeviceRNG(UInt64(seed), UInt64(step), Dict{Tuple{Symbol,Int,Int},Int}())
+
+function drop_in_step!(rng::DeviceRNG, kind::Symbol, species1::Integer, species2::Integer, cell::Integer)
+    key = (kind, Int(species1), Int(species2))
+    if rng.step == 0 || cell <= get(rng.seen, key, 0)
+        rng.step += 1
+        empty!(rng.seen)
+    end
+    rng.seen[key] = cell
+    rng.step
+end
 
 function check(rc, ctx)
     rc == 0 && return nothing
@@ -258,8 +300,10 @@ function set_sigma_g_w_max!(dp::DeviceParticles, species1, species2, values::Vec
                 dp.ptr, species1 - 1, species2 - 1, values), dp.ctx)
 end
 
-set_cell_volumes!(dp::DeviceParticles, V::Vector{Float64}) =
+function set_cell_volumes!(dp::DeviceParticles, V::Vector{Float64})
     check(ccall((:mz_set_cell_volumes, libmz), Cint, (Ptr{Cvoid}, Ptr{Float64}), dp.ptr, V), dp.ctx)
+    dp.V .= V
+end
 
 # ------------------------------------------------------------------ convection and sorting
 """convect_particles! (convection_1D.jl:130-157)."""
@@ -368,24 +412,52 @@ function merge_octree_N2_based!(rng::DeviceRNG, octree::DeviceOctree, dp::Device
     n[]
 end
 
-"""sample_particles_equal_weight!(rng, grid, ..., ndens, T, Fnum) (grid_uniform1D.jl:198-219)."""
-sample_particles_equal_weight!(rng::DeviceRNG, grid::DeviceGrid1D, dp::DeviceParticles, species, ndens, T, Fnum) =
+"""sample_particles_equal_weight!(rng, grid, ..., ndens, T, Fnum; vx0, vy0, vz0) (grid_uniform1D.jl:198-219)."""
+sample_particles_equal_weight!(rng::DeviceRNG, grid::DeviceGrid1D, dp::DeviceParticles, species, ndens, T, Fnum;
+                               vx0=0.0, vy0=0.0, vz0=0.0) =
     check(ccall((:mz_sample_grid_ndens, libmz), Cint,
-                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Float64, Float64, Float64, UInt64),
-                dp.ptr, species - 1, grid, ndens, T, Fnum, rng.step), dp.ctx)
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Float64, Float64, Float64, UInt64, Ptr{Float64}),
+                dp.ptr, species - 1, grid, ndens, T, Fnum, rng.step, Float64[vx0, vy0, vz0]), dp.ctx)
+
+"""sample_particles_equal_weight!(rng, particles, pia, cell, species, nparticles, m, T, Fnum, xlo, xhi, ylo,
+yhi, zlo, zhi; distribution, vx0, vy0, vz0) (distributions_and_sampling.jl:477-509) for one cell."""
+function sample_particles_equal_weight!(rng::DeviceRNG, dp::DeviceParticles, cell, species, nparticles, T, Fnum,
+                                        xlo, xhi, ylo, yhi, zlo, zhi; distribution=:Maxwellian, vx0=0.0, vy0=0.0,
+                                        vz0=0.0)
+    counts = zeros(Int64, dp.n_cells)
+    counts[cell] = nparticles
+    Fn = fill(Float64(Fnum), dp.n_cells)
+    box = zeros(6, dp.n_cells)
+    box[:, cell] .= (xlo, xhi, ylo, yhi, zlo, zhi)
+    check(ccall((:mz_sample_cells, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64, Ptr{Float64},
+                 Int32, UInt64, Ptr{Float64}, Ptr{Float64}),
+                dp.ptr, species - 1, counts, C_NULL, Float64[T, T, T], Fn, 0.0, box,
+                distribution == :BKW ? 1 : 0, rng.step, C_NULL, Float64[vx0, vy0, vz0]), dp.ctx)
+end
 
 # ------------------------------------------------------------------ fused steps
 """
-    step!(dp, n_steps; grid, walls, Δt, step0, inst, avg, avg_start, n_avg)
+    step!(dp, n_steps; grid, walls, Δt, step0, inst, avg, avg_start, n_avg, dims,
+          equal_weight, merge_threshold, merge_target, octree)
 
-`n_steps` fused steps (ntc_equal_weight! -> convect -> sort -> props ->
-avg_props!), replayed from a CUDA graph: the loop body of
-simulations/1D/couette_benchmarking.jl:58-85 in one call.
+`n_steps` fused steps replayed from a CUDA graph: with `equal_weight=true`
+ntc_equal_weight! -> convect -> sort -> props -> avg_props!, the loop body of
+simulations/1D/couette_benchmarking.jl:58-85; with `equal_weight=false` ntc!
+with splitting and the octree merge of cells above `merge_threshold`
+particles down to `merge_target` before convection, the loop body of
+simulations/1D/couette_varweight_octree.jl:85-135.  `dims=0` runs 0-D cells
+(no convection).
 """
-function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D, walls::DeviceWalls1D, Δt, step0=0,
+function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D=DeviceGrid1D(1.0, dp.n_cells, 1.0, 1.0, 0.0, 1.0),
+               walls::Union{Nothing,DeviceWalls1D}=nothing, Δt, step0=0,
                inst::Union{Nothing,DeviceProps}=nothing, avg::Union{Nothing,DeviceProps}=nothing,
-               avg_start=0, n_avg=1, dims=1)
-    plan = MzStepPlan(dims, 1, 1, 1, avg_start, n_avg, Δt, 1e-16, step0, 1, 0, grid, walls, 0)
+               avg_start=0, n_avg=1, dims=1, equal_weight=true, merge_threshold=0, merge_target=0,
+               octree::DeviceOctree=DeviceOctree(), dw_tol=1e-16)
+    w = walls === nothing ? DeviceWalls1D((0.0, 0.0), ntuple(_ -> 0.0, 6), (0.0, 0.0),
+                                          ntuple(_ -> 0.0, 2 * MZ_MAX_SPECIES)) : walls
+    plan = MzStepPlan(dims, 1, equal_weight ? 1 : 0, 1, avg_start, n_avg, Δt, dw_tol, step0, 1, 0, grid, w, 0, 0,
+                      merge_threshold, merge_target, octree)
     check(ccall((:mz_step, libmz), Cint, (Ptr{Cvoid}, Ref{MzStepPlan}, Int64, Ptr{Cvoid}, Ptr{Cvoid}),
                 dp.ptr, plan, n_steps, inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr),
           dp.ctx)
@@ -643,8 +715,271 @@ function retired_requests(srv::DeviceServer)
     ids
 end
 
+# ------------------------------------------------------------------ the reference's signatures
+# Stand-ins for the reference's containers.  A time loop written against
+# Merzbild (simulations/**, test/**) keeps its calls and their positional
+# arguments; only the set-up builds device containers:
+#
+#     dp = DeviceParticles(ctx, grid, species_data, interaction_data, capacity)
+#     particles = device_particles(dp); pia = DevicePIA(dp)
+#     collision_factors = create_collision_factors_array(pia, interaction_data, species_data, T, Fnum)
+#     gridsorter = DeviceGridSort(dp); rng = DeviceRNG(seed)
+#     ... then the reference's loop body, e.g. couette_benchmarking.jl:58-85:
+#     ntc_equal_weight!(rng, collision_factors[1, 1, cell], collision_data, interaction_data,
+#                       particles[1], pia, cell, 1, Δt, grid.cells[cell].V)
+#
+# Arguments the device keeps for itself (collision_data scratch, the
+# interaction, which the domain was created with) are accepted and unused.
+
+"""
+    DevicePIA(dp)
+
+`ParticleIndexerArray` (particles.jl:110-141) of a `DeviceParticles`: the
+indexers live on the device.
+"""
+struct DevicePIA
+    dp::DeviceParticles
+end
+
+"""
+    DeviceParticleVector(dp, species)
+
+`ParticleVector` (particles.jl:194-212) of one species of a `DeviceParticles`.
+"""
+struct DeviceParticleVector
+    dp::DeviceParticles
+    species::Int
+end
+
+"""`particles[s]` for every species, as the reference's drivers index them."""
+device_particles(dp::DeviceParticles) = [DeviceParticleVector(dp, s) for s in 1:dp.n_species]
+
+"""
+    DeviceCollisionFactors(dp)
+
+The array of `CollisionFactors` (create_collision_factors_array,
+collision_ntc.jl:46-155) of a `DeviceParticles`; `cf[s1, s2, cell]` is the
+handle the reference's `ntc!` takes, the factors stay on the device.
+"""
+struct DeviceCollisionFactors
+    dp::DeviceParticles
+end
+struct DeviceCollisionFactorsCell
+    dp::DeviceParticles
+    species1::Int
+    species2::Int
+    cell::Int
+end
+Base.getindex(cf::DeviceCollisionFactors, s1::Integer, s2::Integer, cell::Integer) =
+    DeviceCollisionFactorsCell(cf.dp, s1, s2, cell)
+Base.size(cf::DeviceCollisionFactors) = (cf.dp.n_species, cf.dp.n_species, cf.dp.n_cells)
+
+"""`GridSortInPlace` (grid_sorting.jl:10-27): the device sort keeps its buffers on the device."""
+struct DeviceGridSort
+    dp::DeviceParticles
+end
+
+"""
+    DeviceParticles(ctx, grid, species_data, interactions, capacity; seed=1234)
+
+A `DeviceParticles` on the cells of a 1-D grid, with the grid's cell volumes.
+"""
+function DeviceParticles(ctx::DeviceContext, grid::Merzbild.Grid1DUniform, species_data, interactions, capacity;
+                         seed=1234)
+    dp = DeviceParticles(ctx, grid.n_cells, species_data, interactions, capacity; seed=seed)
+    set_cell_volumes!(dp, [c.V for c in grid.cells])
+    dp
+end
+
+function same_domain(dp::DeviceParticles, others...)
+    for o in others
+        o.dp === dp || throw(ErrorException("device containers of different DeviceParticles"))
+    end
+    dp
+end
+
+function check_volume(dp::DeviceParticles, cell, V)
+    dp.V[cell] == V || throw(ErrorException("cell $cell: volume $V differs from the device's $(dp.V[cell]); " *
+                                            "set the volumes with set_cell_volumes! or DeviceParticles(ctx, grid, ...)"))
+end
+
+device_grid(grid::DeviceGrid1D) = grid
+device_grid(grid::Merzbild.Grid1DUniform) = DeviceGrid1D(grid)
+device_walls(walls::DeviceWalls1D) = walls
+device_walls(walls::Merzbild.MaxwellWalls1D) = DeviceWalls1D(walls)
+
+function ntc_call(rng::DeviceRNG, kind::Symbol, cf::DeviceCollisionFactorsCell, pia::DevicePIA, cell, s1, s2, Δt, V,
+                  flags, dw_tol)
+    dp = same_domain(pia.dp, cf)
+    (cf.species1 == s1 && cf.species2 == s2 && cf.cell == cell) ||
+        throw(ErrorException("collision factors of species ($(cf.species1), $(cf.species2)), cell $(cf.cell) " *
+                             "passed for species ($s1, $s2), cell $cell"))
+    check_volume(dp, cell, V)
+    step = drop_in_step!(rng, kind, s1, s2, cell)
+    check(ccall((:mz_ntc, libmz), Cint, (Ptr{Cvoid}, Int32, Int32, Float64, Int64, Int64, UInt64, Int32, Float64),
+                dp.ptr, s1 - 1, s2 - 1, Δt, cell - 1, cell, step, flags, dw_tol), dp.ctx)
+end
+
+"""ntc! of one species (collision_ntc.jl:338)."""
+Merzbild.ntc!(rng::DeviceRNG, collision_factors::DeviceCollisionFactorsCell, collision_data, interaction,
+              particles::DeviceParticleVector, pia::DevicePIA, cell, species, Δt, V; dw_tol=1e-16) =
+    ntc_call(rng, :ntc, collision_factors, same_pv(pia, particles), cell, species, species, Δt, V, 0, dw_tol)
+
+"""ntc! of two species (collision_ntc.jl:412)."""
+Merzbild.ntc!(rng::DeviceRNG, collision_factors::DeviceCollisionFactorsCell, collision_data, interaction,
+              particles_1::DeviceParticleVector, particles_2::DeviceParticleVector, pia::DevicePIA,
+              cell, species1, species2, Δt, V; dw_tol=1e-16) =
+    ntc_call(rng, :ntc, collision_factors, same_pv(pia, particles_1, particles_2), cell, species1, species2, Δt, V,
+             0, dw_tol)
+
+"""ntc_equal_weight! of one species (collision_ntc.jl:479)."""
+Merzbild.ntc_equal_weight!(rng::DeviceRNG, collision_factors::DeviceCollisionFactorsCell, collision_data,
+                           interaction, particles::DeviceParticleVector, pia::DevicePIA, cell, species, Δt, V) =
+    ntc_call(rng, :ntc, collision_factors, same_pv(pia, particles), cell, species, species, Δt, V,
+             MZ_NTC_EQUAL_WEIGHT, 1e-16)
+
+"""ntc_equal_weight! of two species (collision_ntc.jl:554)."""
+Merzbild.ntc_equal_weight!(rng::DeviceRNG, collision_factors::DeviceCollisionFactorsCell, collision_data,
+                           interaction, particles_1::DeviceParticleVector, particles_2::DeviceParticleVector,
+                           pia::DevicePIA, cell, species1, species2, Δt, V) =
+    ntc_call(rng, :ntc, collision_factors, same_pv(pia, particles_1, particles_2), cell, species1, species2, Δt,
+             V, MZ_NTC_EQUAL_WEIGHT, 1e-16)
+
+function same_pv(pia::DevicePIA, pvs::DeviceParticleVector...)
+    same_domain(pia.dp, pvs...)
+    pia
+end
+
+"""create_collision_factors_array(pia) (collision_ntc.jl:93): the device's
+collision factors of every pair and cell, (σ g w)_max as last set."""
+Merzbild.create_collision_factors_array(pia::DevicePIA) = DeviceCollisionFactors(pia.dp)
+
+"""create_collision_factors_array(pia, interactions, species_data, T_list, Fnum; mult_factor)
+(collision_ntc.jl:120): (σ g w)_max of every pair in every cell, estimated as
+the reference does (estimate_sigma_g_w_max!, collision_utils.jl:464-478)."""
+function Merzbild.create_collision_factors_array(pia::DevicePIA, interactions, species_data, T_list, Fnum::Real;
+                                                 mult_factor=1.0)
+    dp = pia.dp
+    for (k, species2) in enumerate(species_data), (i, species1) in enumerate(species_data)
+        v = Merzbild.estimate_sigma_g_w_max(interactions[i, k], species1, species2, T_list[i], T_list[k], Fnum;
+                                            mult_factor=mult_factor)
+        set_sigma_g_w_max!(dp, i, k, fill(v, dp.n_cells))
+    end
+    DeviceCollisionFactors(dp)
+end
+Merzbild.create_collision_factors_array(pia::DevicePIA, interactions, species_data, T::Real, Fnum::Real;
+                                        mult_factor=1.0) =
+    Merzbild.create_collision_factors_array(pia, interactions, species_data, fill(T, length(species_data)), Fnum;
+                                            mult_factor=mult_factor)
+
+"""compute_props! (physical_props.jl:104)."""
+Merzbild.compute_props!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA, species_data,
+                        phys_props::DeviceProps) = compute_props!(same_pv(pia, particles...).dp, phys_props)
+
+"""compute_props_with_total_moments! (physical_props.jl:168)."""
+Merzbild.compute_props_with_total_moments!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA,
+                                           species_data, phys_props::DeviceProps) =
+    compute_props_with_total_moments!(same_pv(pia, particles...).dp, phys_props)
+
+"""compute_props_sorted! (physical_props.jl:370; every cell) and its grid
+forms (:393, :452), number densities when `phys_props` computes them.  The
+forms with a `cell_chunk` (:317, :393; the reference's threads each take a
+chunk) compute every cell at once on the device: the chunk's cells get the
+values the reference computes, the other cells are recomputed from the same
+state."""
+Merzbild.compute_props_sorted!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA, species_data,
+                               phys_props::DeviceProps) = compute_props_sorted!(same_pv(pia, particles...).dp, phys_props)
+Merzbild.compute_props_sorted!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA, species_data,
+                               phys_props::DeviceProps, cell_chunk) =
+    compute_props_sorted!(same_pv(pia, particles...).dp, phys_props)
+Merzbild.compute_props_sorted!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA, species_data,
+                               phys_props::DeviceProps, grid::Merzbild.Grid1DUniform) =
+    compute_props_sorted!(same_pv(pia, particles...).dp, phys_props)
+Merzbild.compute_props_sorted!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA, species_data,
+                               phys_props::DeviceProps, grid::Merzbild.Grid1DUniform, cell_chunk) =
+    compute_props_sorted!(same_pv(pia, particles...).dp, phys_props)
+
+"""convect_particles! (convection_1D.jl:130) and with surface sampling (:176)."""
+function Merzbild.convect_particles!(rng::DeviceRNG, grid, boundaries, particles::DeviceParticleVector,
+                                     pia::DevicePIA, species, species_data, Δt)
+    dp = same_pv(pia, particles).dp
+    step = drop_in_step!(rng, :convect, species, species, 1)
+    check(ccall((:mz_convect_1d, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ref{DeviceWalls1D}, Float64, UInt64, Int32),
+                dp.ptr, species - 1, device_grid(grid), device_walls(boundaries), Δt, step, 0), dp.ctx)
+end
+function Merzbild.convect_particles!(rng::DeviceRNG, grid, boundaries, particles::DeviceParticleVector,
+                                     pia::DevicePIA, species, species_data, surf_props::DeviceSurfProps, Δt)
+    dp = same_pv(pia, particles).dp
+    step = drop_in_step!(rng, :convect, species, species, 1)
+    check(ccall((:mz_convect_1d_surf, libmz), Cint,
+                (Ptr{Cvoid}, Int32, Ref{DeviceGrid1D}, Ref{DeviceWalls1D}, Float64, UInt64, Int32, Ptr{Cvoid}),
+                dp.ptr, species - 1, device_grid(grid), device_walls(boundaries), Δt, step, 0, surf_props.ptr), dp.ctx)
+end
+
+"""sort_particles!(gridsort, grid, particles, pia, species) (grid_sorting.jl:58)
+and without the grid, from the cells stored in the particles (:128)."""
+Merzbild.sort_particles!(gridsort::DeviceGridSort, grid, particles::DeviceParticleVector, pia::DevicePIA, species) =
+    sort_particles!(device_grid(grid), same_pv(pia, particles).dp, species)
+Merzbild.sort_particles!(gridsort::DeviceGridSort, particles::DeviceParticleVector, pia::DevicePIA, species) =
+    sort_particles!(same_pv(pia, particles).dp, species)
+
+"""merge_octree_N2_based!(rng, octree, particles, pia, cell, species, target_np[, grid])
+(merging_octree_N2.jl:1060, :1088)."""
+function Merzbild.merge_octree_N2_based!(rng::DeviceRNG, octree::DeviceOctree, particles::DeviceParticleVector,
+                                         pia::DevicePIA, cell, species, target_np)
+    step = drop_in_step!(rng, :merge, species, species, cell)
+    merge_octree_N2_based!(DeviceRNG(rng.seed, step), octree, same_pv(pia, particles).dp, cell, species, target_np)
+end
+function Merzbild.merge_octree_N2_based!(rng::DeviceRNG, octree::DeviceOctree, particles::DeviceParticleVector,
+                                         pia::DevicePIA, cell, species, target_np, grid::Merzbild.Grid1DUniform)
+    step = drop_in_step!(rng, :merge, species, species, cell)
+    merge_octree_N2_based!(DeviceRNG(rng.seed, step), octree, same_pv(pia, particles).dp, cell, species, target_np;
+                           grid=device_grid(grid))
+end
+
+"""squash_pia!(pv, pia, species) (particles.jl:622) and of every species (:695)."""
+Merzbild.squash_pia!(pv::DeviceParticleVector, pia::DevicePIA, species) = squash_pia!(same_pv(pia, pv).dp, species)
+function Merzbild.squash_pia!(particles::AbstractVector{DeviceParticleVector}, pia::DevicePIA)
+    dp = same_pv(pia, particles...).dp
+    for s in 1:dp.n_species
+        squash_pia!(dp, s)
+    end
+end
+
+"""The reference's indexing checks (particles.jl:805-1025) on the device
+layout: the same return values."""
+function check_indexing(dp::DeviceParticles, species, mode)
+    ok = Ref{Int32}(0)
+    detail = Ref{Int64}(0)
+    check(ccall((:mz_check_indexing, libmz), Cint, (Ptr{Cvoid}, Int32, Int32, Ref{Int32}, Ref{Int64}),
+                dp.ptr, species - 1, mode, ok, detail), dp.ctx)
+    ok[] != 0, detail[]
+end
+Merzbild.check_pia_is_correct(pia::DevicePIA, species) = check_indexing(pia.dp, species, 0)
+Merzbild.check_unique_index(pv::DeviceParticleVector, pia::DevicePIA, species) =
+    check_indexing(same_pv(pia, pv).dp, species, 1)
+Merzbild.check_unique_buffer(pv::DeviceParticleVector) = check_indexing(pv.dp, pv.species, 2)
+Merzbild.count_disordered_particles(pv::DeviceParticleVector, pia::DevicePIA, species; use_offset=true) =
+    check_indexing(same_pv(pia, pv).dp, species, use_offset ? 3 : 4)[2]
+
+"""Write a species' indexer rows as given (mz_set_indexer): 1-based
+`ParticleIndexer`-like rows (n_local, start1, end1, n_group1, start2, end2,
+n_group2), one per cell."""
+function set_indexer!(dp::DeviceParticles, species, rows::AbstractMatrix{<:Integer}, n_total)
+    tab = [MzParticleIndexer(rows[c, 1], rows[c, 4] > 0 ? rows[c, 2] - 1 : 0, rows[c, 4] > 0 ? rows[c, 3] - 1 : -1,
+                             rows[c, 4], rows[c, 7] > 0 ? rows[c, 5] - 1 : 0, rows[c, 7] > 0 ? rows[c, 6] - 1 : -1,
+                             rows[c, 7]) for c in 1:dp.n_cells]
+    check(ccall((:mz_set_indexer, libmz), Cint, (Ptr{Cvoid}, Int32, Ptr{MzParticleIndexer}, Int64),
+                dp.ptr, species - 1, tab, n_total), dp.ctx)
+end
+
 """Requests of at least `particles` particles run in the lane of large requests (0: one lane)."""
 set_lane_split!(srv::DeviceServer, particles) =
     check(ccall((:mz_server_set_lane_split, libmz), Cint, (Ptr{Cvoid}, Int64), srv.ptr, particles), srv.ctx)
+
+"""Device memory that admission by free memory (a server created with capacity 0) leaves free."""
+set_hbm_headroom!(srv::DeviceServer, bytes::Integer) =
+    check(ccall((:mz_server_set_hbm_headroom, libmz), Cint, (Ptr{Cvoid}, Int64), srv.ptr, bytes), srv.ctx)
 
 end # module

@@ -117,8 +117,8 @@ _SIGS = {
     "mz_sort": (i32, [vp, i32, P(Grid1D), P(i64)]),
     "mz_squash": (i32, [vp, i32]),
     "mz_merge_octree_n2": (i32, [vp, i32, i64, i64, i64, i64, P(OctreeParams), P(Grid1D), u64, P(i64)]),
-    "mz_sample_cells": (i32, [vp, i32, P(i64), P(d), P(d), P(d), d, P(d), i32, u64]),
-    "mz_sample_grid_ndens": (i32, [vp, i32, P(Grid1D), d, d, d, u64]),
+    "mz_sample_cells": (i32, [vp, i32, P(i64), P(d), P(d), P(d), d, P(d), i32, u64, P(d), P(d)]),
+    "mz_sample_grid_ndens": (i32, [vp, i32, P(Grid1D), d, d, d, u64, P(d)]),
     "mz_step": (i32, [vp, P(StepPlan), i64, vp, vp]),
     "mz_get_counters": (i32, [vp, P(Counters), i32]),
     "mz_step_autotune": (i32, [vp, P(StepPlan), i64, P(i32), P(i32)]),

@@ -464,7 +464,11 @@ class Domain:
         return n.value
 
     # sampling --------------------------------------------------------------
-    def sample_cells(self, species, counts, T, Fnum, step=0, log10_weight_span=0.0, box=None, distribution=0):
+    def sample_cells(self, species, counts, T, Fnum, step=0, log10_weight_span=0.0, box=None, distribution=0,
+                     v0=None):
+        """sample_particles_equal_weight! for every cell at once; v0: the
+        velocity offset (vx0, vy0, vz0) of every cell, or one per cell
+        (n_cells x 3)."""
         counts = np.ascontiguousarray(np.broadcast_to(np.asarray(counts, np.int64), (self.n_cells,)))
         T = np.asarray(T, float)
         T3 = T3_all = None
@@ -476,13 +480,22 @@ class Domain:
             T3 = f64(np.broadcast_to(T.reshape(self.n_cells, -1), (self.n_cells, 3)))
         F = f64(np.broadcast_to(np.asarray(Fnum, float), (self.n_cells,)))
         b = None if box is None else f64(np.broadcast_to(np.asarray(box, float), (self.n_cells, 6)))
+        v0c = v0a = None
+        if v0 is not None:
+            v = np.asarray(v0, float)
+            if v.shape == (3,):
+                v0a = f64(v)
+            else:
+                v0c = f64(np.broadcast_to(v.reshape(self.n_cells, 3), (self.n_cells, 3)))
         self._ck(lib().mz_sample_cells(self.h, species, ptr(counts, C.c_int64), ptr(T3), ptr(T3_all), ptr(F),
-                                       float(log10_weight_span), ptr(b), int(distribution), int(step)))
+                                       float(log10_weight_span), ptr(b), int(distribution), int(step), ptr(v0c),
+                                       ptr(v0a)))
 
-    def sample_grid_ndens(self, species, grid, ndens, T, Fnum, step=0):
+    def sample_grid_ndens(self, species, grid, ndens, T, Fnum, step=0, v0=None):
         g = grid.c_struct()
+        v = None if v0 is None else f64(np.asarray(v0, float).reshape(3))
         self._ck(lib().mz_sample_grid_ndens(self.h, species, C.byref(g), float(ndens), float(T), float(Fnum),
-                                            int(step)))
+                                            int(step), ptr(v)))
 
     # fused -----------------------------------------------------------------
     def step(self, plan, n_steps, inst=None, avg=None):

@@ -1793,11 +1793,14 @@ void orc_sample_particles_equal_weight(void* h, int32_t s, int64_t cell, int64_t
 // sample_particles_equal_weight!(rng, grid, ..., ndens::Float64, T, Fnum),
 // grid_uniform1D.jl:198-219; the fractional extra particle uses its own stream.
 void orc_sample_grid_ndens(void* h, int32_t s, double L, int64_t nx, double wall_offset, double ndens, double T,
-                           double Fnum, uint64_t seed, uint64_t step)
+                           double Fnum, uint64_t seed, uint64_t step, const double* v0_in)
 {
     Orc* o = (Orc*)h;
     Grid1D g = make_grid(L, nx, wall_offset);
+    // the keywords vx0, vy0, vz0 of grid_uniform1D.jl:215-219
     double v0[3] = {0, 0, 0};
+    if (v0_in)
+        for (int k = 0; k < 3; ++k) v0[k] = v0_in[k];
     for (int64_t cell = 1; cell <= nx; ++cell) {
         double xlo = (double)(cell - 1) * g.dx, xhi = (double)cell * g.dx;
         double n_in_cell = ndens * g.dx;

@@ -98,7 +98,7 @@ def lib():
             "orc_check_unique_index": (i64, [vp, i32]),
             "orc_check_unique_buffer": (i64, [vp, i32]),
             "orc_sample_particles_equal_weight": (None, [vp, i32, i64, i64, d, d, P(d), u64, u64, i32, P(d)]),
-            "orc_sample_grid_ndens": (None, [vp, i32, d, i64, d, d, d, d, u64, u64]),
+            "orc_sample_grid_ndens": (None, [vp, i32, d, i64, d, d, d, d, u64, u64, P(d)]),
             "orc_stream_draws": (None, [u64, C.c_uint32, C.c_uint32, u64, C.c_uint32, C.c_uint32, i64, P(d)]),
             "orc_philox": (None, [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
             "orc_tgamma": (d, [d]),
@@ -393,8 +393,9 @@ class Oracle:
         v = np.ascontiguousarray(v0, float)
         self.L.orc_sample_particles_equal_weight(self.h, s, cell, n, T, Fnum, _p(b), seed, step, distribution, _p(v))
 
-    def sample_grid_ndens(self, s, L, nx, ndens, T, Fnum, seed=0, step=0, wall_offset=1e-12):
-        self.L.orc_sample_grid_ndens(self.h, s, L, nx, wall_offset, ndens, T, Fnum, seed, step)
+    def sample_grid_ndens(self, s, L, nx, ndens, T, Fnum, seed=0, step=0, wall_offset=1e-12, v0=(0.0, 0.0, 0.0)):
+        v = np.ascontiguousarray(v0, float).reshape(3)
+        self.L.orc_sample_grid_ndens(self.h, s, L, nx, wall_offset, ndens, T, Fnum, seed, step, _p(v))
 
     def com_g_scatter(self, s1, s2, p1, p2, seed=0, scatter=True):
         a = np.ascontiguousarray(p1, float).copy()

@@ -203,6 +203,29 @@ def test_fused_varweight_step_equals_standalone_loop(ctx, orc, graph):
         dom.close()
 
 
+def test_varweight_lanes_per_cell_change_no_result(ctx):
+    """8, 16 or 32 lanes per cell in the splitting NTC (chosen by
+    mz_step_autotune on real steps): the same particles after the same steps."""
+    nx, ppc, steps, threshold, target, seed = 40, 150, 14, 170, 90, 55
+    sp, inter, grid, walls, dt, smax, arrays = _varweight_state(nx, ppc, seed)
+    octree = mz.OctreeN2Merge(max_Nbins=6000)
+    runs = []
+    for tune in (True, False):
+        dom = mz.Domain(ctx, nx, sp, 8 * nx * ppc, interactions=inter, seed=seed)
+        dom.upload(0, *arrays)
+        dom.set_cell_volumes(grid.V)
+        dom.set_sigma_g_w_max(0, 0, smax)
+        done = 0
+        if tune:
+            lanes, big = dom.autotune(_vw_plan(grid, walls, dt, octree, threshold, target), trial_steps=1)
+            assert lanes in (8, 16, 32) and big == 0
+            done = 6
+        dom.step(_vw_plan(grid, walls, dt, octree, threshold, target, step0=done), steps - done)
+        runs.append(device_logical(dom, 0))
+        dom.close()
+    assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][0], runs[1][0])
+
+
 def test_fused_varweight_couette_at_the_benchmark_size_matches_oracle(ctx, orc):
     """The variable-weight Couette configuration: 1,000 cells, 1,000 initial
     particles per cell with weights log-uniform over two decades, merging of
@@ -290,17 +313,39 @@ def test_fused_varweight_step_grows_storage_and_resumes(ctx):
         assert np.array_equal(states[0][1], ca) and np.array_equal(states[0][0], a)
 
 
+def _one_cell_oracle(orc, sp, rows_by_species, smax, capacity):
+    """A one-cell oracle (the reference's 0-D variable-weight tests simulate
+    one cell: with several cells and no sort between steps, a cell's next
+    split would extend its group 2 over the next cell's, particles.jl:311-315)."""
+    t = mz.VHS
+    o = orc.Oracle(1, len(sp), [s.mass for s in sp])
+    if len(sp) == 1:
+        o.load_interactions(*t["Ar,Ar"])
+    else:
+        o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
+                            [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
+    for s, rows in enumerate(rows_by_species):
+        o.set_particles_simple(s, np.ones(rows.shape[0], np.int64), rows)
+        o.pv_resize(s, capacity)
+    for (s1, s2), v in smax.items():
+        o.cf_set_smax(s1, s2, v)
+    return o
+
+
 def test_fused_varweight_0d_and_mixture_match_oracle(ctx, orc):
     """0-D variable-weight steps (test_bkw_varweight_octree.jl's loop: ntc!,
     merge, compute_props!) on the device-resident path, and a two-species
     mixture with unequal weights (test_2species_varweight_octree.jl), which
-    mz_step runs with the standalone kernels step by step: both against the
-    oracle."""
+    mz_step runs with the standalone kernels step by step.  Every device cell
+    draws the streams of cell 0 (mz_set_cell_rng), so each equals a one-cell
+    oracle run of the reference loop on that cell's particles."""
     sp = species(["Ar"])
     inter = interactions(sp)
     counts = np.array([300, 1800, 800, 120, 2600, 40])
-    seed, steps, threshold, target, dt, Fnum = 19, 4, 1000, 400, 2e-3, 1e12
-    dom = mz.Domain(ctx, len(counts), sp, 6 * int(counts.sum()), interactions=inter, seed=seed)
+    n_cells = len(counts)
+    seed, steps, threshold, target, dt, Fnum = 19, 4, 1000, 400, 0.2, 1e12
+    dom = mz.Domain(ctx, n_cells, sp, 6 * int(counts.sum()), interactions=inter, seed=seed)
+    dom.set_cell_rng(rids=np.zeros(n_cells, np.uint32))
     dom.sample_cells(0, counts, 500.0, Fnum, step=0, log10_weight_span=2.0)
     smax = mz.estimate_sigma_g_w_max(inter[0][0], sp[0], sp[0], 500.0, 500.0, Fnum)
     dom.set_sigma_g_w_max(0, 0, smax)
@@ -308,28 +353,31 @@ def test_fused_varweight_0d_and_mixture_match_oracle(ctx, orc):
     octree = mz.OctreeN2Merge(max_Nbins=6000)
     inst = mz.PhysProps(dom)
     dom.step(_vw_plan(None, None, dt, octree, threshold, target, dims=0), steps, inst)
-    o = oracle_state(orc, len(counts), sp, mz.VHS, [(w, v, x, cell)], capacity=6 * int(counts.sum()))
-    o.cf_set_smax(0, 0, smax)
-    oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
-    merged = _oracle_varweight_loop(o, oc, None, None, dt, seed, steps, threshold, target)
-    assert dom.counters()["merges"] == merged and merged >= 2
-    orows, oc_cells = oracle_logical(o, 0)
+    assert dom.counters()["splits"] > 100
     drows, dc_cells = device_logical(dom, 0)
-    assert np.array_equal(oc_cells, dc_cells)
-    assert_close_rows(orows, drows, 1e-11, "0-D variable-weight cells")
     r = inst.fetch()
-    ref = o.compute_props(mode=0)
-    assert_close_rows(r["T"][:, 0:1], ref["T"][0].reshape(-1, 1), 1e-11, "0-D T")
+    oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
+    merged = 0
+    for c in range(n_cells):
+        rows = np.column_stack([w, v, x])[cell == c]
+        o = _one_cell_oracle(orc, sp, [rows], {(0, 0): smax}, 6 * int(counts.sum()))
+        merged += _oracle_varweight_loop(o, oc, None, None, dt, seed, steps, threshold, target)
+        orows, _ = oracle_logical(o, 0)
+        assert_close_rows(orows, drows[dc_cells == c], 1e-11, f"0-D variable-weight cell {c}")
+        ref = o.compute_props(mode=0)
+        assert abs(r["T"][c, 0] - ref["T"][0][0]) <= 1e-11 * ref["T"][0][0], c
+    assert dom.counters()["merges"] == merged and merged >= 2
     dom.close()
 
     # two species, unequal weights: ntc! for (Ar,Ar), (He,Ar), (He,He), then
-    # merging of each species
+    # merging of each species (test_2species_varweight_octree.jl:57-80)
     sp2 = species(["Ar", "He"])
     inter2 = interactions(sp2)
-    n_cells, seed = 4, 23
+    n_cells, seed, steps = 4, 23, 3
     cnt2 = [np.array([400, 900, 150, 600]), np.array([1200, 300, 800, 500])]
     Fn = (2e12, 5e11)
     dom = mz.Domain(ctx, n_cells, sp2, 20000, interactions=inter2, seed=seed)
+    dom.set_cell_rng(rids=np.zeros(n_cells, np.uint32))
     for s, T0 in enumerate((3000.0, 360.0)):
         dom.sample_cells(s, cnt2[s], T0, Fn[s], step=0, log10_weight_span=1.0)
     arrays = [dom.download(s) for s in range(2)]
@@ -339,33 +387,22 @@ def test_fused_varweight_0d_and_mixture_match_oracle(ctx, orc):
             T1, T2 = (3000.0, 360.0)[s1], (3000.0, 360.0)[s2]
             smax2[s1, s2] = mz.estimate_sigma_g_w_max(inter2[s1][s2], sp2[s1], sp2[s2], T1, T2, max(Fn))
             dom.set_sigma_g_w_max(s1, s2, smax2[s1, s2])
-    dom.step(_vw_plan(None, None, 1e-3, octree, 1000, 500, dims=0), 3)
-    t = mz.VHS
-    o = orc.Oracle(n_cells, 2, [s.mass for s in sp2])
-    o.load_interactions([[t["Ar,Ar"][0], t["Ar,He"][0]], [t["Ar,He"][0], t["He,He"][0]]],
-                        [[t["Ar,Ar"][1], t["Ar,He"][1]], [t["Ar,He"][1], t["He,He"][1]]], 273.0)
-    for s in range(2):
-        w, v, x, cell = arrays[s]
-        o.set_particles_simple(s, cell.astype(np.int64) + 1, np.column_stack([w, v, x]))
-        o.pv_resize(s, 20000)
-    for (s1, s2), val in smax2.items():
-        o.cf_set_smax(s1, s2, val)
-    for step in range(1, 4):
-        # cell by cell, every pair on the cell (the reference's mixture loop):
-        # a cell's split particles then stay one contiguous group 2
-        for c in range(1, n_cells + 1):
+    dom.step(_vw_plan(None, None, 0.2, octree, 1000, 500, dims=0), steps)
+    assert dom.counters()["splits"] > 100
+    dev = [device_logical(dom, s) for s in range(2)]
+    for c in range(n_cells):
+        rows = [np.column_stack(a[:3])[a[3] == c] for a in arrays]
+        o = _one_cell_oracle(orc, sp2, rows, smax2, 20000)
+        for step in range(1, steps + 1):
             for s2 in range(2):
                 for s1 in range(s2, 2):
-                    o.ntc(s1, s2, c, 1e-3, 1.0, seed, step, equal_weight=False)
-        ind, _, _ = o.pia_get()
+                    o.ntc(s1, s2, 1, 0.2, 1.0, seed, step, equal_weight=False)
+            ind, _, _ = o.pia_get()
+            for s in range(2):
+                if ind[s, 0, 0] > 1000:
+                    o.merge_octree(oc, s, 1, 500, seed=seed, step=step)
         for s in range(2):
-            for c in np.nonzero(ind[s, :, 0] > 1000)[0]:
-                o.merge_octree(oc, s, int(c) + 1, 500, seed=seed, step=step)
-            o.squash(s)
-    for s in range(2):
-        orows, oc_cells = oracle_logical(o, s)
-        drows, dc_cells = device_logical(dom, s)
-        assert np.array_equal(oc_cells, dc_cells), s
-        assert_close_rows(orows, drows, 1e-11, f"mixture species {s}")
-    assert dom.counters()["splits"] > 0
+            orows, _ = oracle_logical(o, s)
+            drows, dcells = dev[s]
+            assert_close_rows(orows, drows[dcells == c], 1e-11, f"mixture cell {c} species {s}")
     dom.close()

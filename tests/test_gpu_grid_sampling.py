@@ -77,3 +77,50 @@ def test_grid_sampling_and_props(ctx):
     assert np.all(np.abs(r["T"][:, 0] - T) / T < tb)
     assert np.all(np.abs(r["v"][:, :, 0]) < vb)
     dom.close()
+
+
+def test_sampling_with_drift_matches_the_oracle(ctx, orc):
+    """The keywords vx0, vy0, vz0 of sample_particles_equal_weight!
+    (distributions_and_sampling.jl:477-509, grid_uniform1D.jl:198-219): a
+    different offset per cell, one offset for every cell, and the
+    number-density form, against the oracle on the same streams (the
+    oracle's restatement of the drift is pinned statistically by
+    tests/test_oracle_statistics.py)."""
+    sp = species(["Ar"])
+    n_cells, ppc, T, Fn, seed = 6, 700, 400.0, 1e12, 29
+    v0 = np.array([[100.0 * c, -50.0 * c, 3.0 * c] for c in range(n_cells)])
+    for per_cell in (True, False):
+        dom = mz.Domain(ctx, n_cells, sp, 2 * ppc * n_cells, seed=seed)
+        if per_cell:
+            dom.sample_cells(0, ppc, T, Fn, step=0, v0=v0)
+        else:
+            dom.sample_cells(0, ppc, T, Fn, step=0, v0=v0[2])
+        o = orc.Oracle(n_cells, 1, [sp[0].mass])
+        o.pv_create(0, 2 * ppc * n_cells)
+        for c in range(n_cells):
+            o.sample_equal_weight(0, c + 1, ppc, T, Fn, seed=seed, step=0, v0=v0[c] if per_cell else v0[2])
+        rows, cells = o.logical(0)
+        w, v, x, cell = dom.download(0)
+        assert np.array_equal(cells - 1, cell)
+        drows = np.column_stack([w, v, x])
+        scale = np.maximum(np.abs(rows).max(axis=0), np.abs(drows).max(axis=0))
+        assert np.all(np.abs(rows - drows) <= 1e-13 * scale), per_cell
+        # the offsets are there: mean velocity per cell near v0
+        for c in range(n_cells):
+            vc = v[cell == c].mean(axis=0)
+            assert np.all(np.abs(vc - (v0[c] if per_cell else v0[2])) < 5 * np.sqrt(mz.K_B * T / sp[0].mass / ppc))
+        dom.close()
+    grid = mz.Grid1DUniform(5e-4, n_cells)
+    drift = np.array([250.0, -120.0, 40.0])
+    dom = mz.Domain(ctx, n_cells, sp, 4000 * n_cells, seed=seed)
+    dom.sample_grid_ndens(0, grid, 1e23, T, grid.dx * 1e23 / 800.5, step=0, v0=drift)
+    o = orc.Oracle(n_cells, 1, [sp[0].mass])
+    o.pv_create(0, 4000 * n_cells)
+    o.sample_grid_ndens(0, grid.L, n_cells, 1e23, T, grid.dx * 1e23 / 800.5, seed=seed, step=0, v0=drift)
+    rows, cells = o.logical(0)
+    w, v, x, cell = dom.download(0)
+    assert np.array_equal(cells - 1, cell)
+    drows = np.column_stack([w, v, x])
+    scale = np.maximum(np.abs(rows).max(axis=0), np.abs(drows).max(axis=0))
+    assert np.all(np.abs(rows - drows) <= 1e-13 * scale)
+    dom.close()
