@@ -37,6 +37,7 @@ ALG_BYTES = 112  # per particle-step: every particle read once and written once 
 # instructions per particle of a whole step
 DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH = 256.7
 DRAM_BYTES_PER_PARTICLE_FUSED = 386.6
+FORMS = ("one fused launch", "two launches", "gathering and physics warps side by side")
 FP64_WARP_INST_PER_PARTICLE = 0.814
 
 
@@ -58,7 +59,7 @@ def parse():
                    choices=["batched_0d", "varweight", "serving", "largest_request", "readme_0d"],
                    help="run one of the extra measurements alone and print its result")
     p.add_argument("--seed", type=int, default=1234)
-    p.add_argument("--launches", type=int, default=0, choices=[0, 1, 2],
+    p.add_argument("--launches", type=int, default=0, choices=[0, 1, 2, 3],
                    help="1 or 2 kernel launches per step instead of the autotuner's choice (no autotuning; for "
                         "profiling runs)")
     return p.parse_args()
@@ -638,19 +639,20 @@ def run_gpu(args):
     inst = mz.PhysProps(dom)
     avg = mz.PhysProps(dom)
     K, W = args.steps, args.warmup
-    # the autotuner times each mapping (lanes per cell x one or two launches
-    # per step) on real steps, two rounds of 8 steps each before the warm-up,
+    # the autotuner times each mapping (lanes per cell x the three launch
+    # forms: one fused launch, two launches, gathering and physics warps side
+    # by side) on real steps, two rounds of 8 steps each before the warm-up,
     # then W untimed warm-up steps
     if args.launches:
         # a fixed mapping: the default lanes per cell and the launches asked for
         tune_steps = 0
-        mapping = (8 if args.cells >= 4096 else (16 if args.cells >= 1024 else 32), 1 if args.launches == 2 else 0)
+        mapping = (8 if args.cells >= 4096 else (16 if args.cells >= 1024 else 32), args.launches - 1)
     else:
-        tune_steps = 12 * 8
+        tune_steps = 18 * 8
         mapping = dom.autotune(make_plan(mz, grid, walls, dt, 0, K), trial_steps=8)
     dom.step(make_plan(mz, grid, walls, dt, tune_steps, K, launches=args.launches), W, inst, avg)
     ctx.synchronize()
-    log(f"warm-up done (mapping: {mapping[0]} lanes per cell, {2 if mapping[1] == 1 else 1} launches per step)")
+    log(f"warm-up done (mapping: {mapping[0]} lanes per cell, launch form {FORMS[mapping[1]]})")
     mz.clear_props(avg)
     dom.counters(reset=True)
     step0 = tune_steps + W
@@ -701,7 +703,11 @@ def run_gpu(args):
     # ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the same step at
     # 10,000 cells x 400 particles; traffic scales with the particles a launch
     # moves, so it is scaled to this launch's particle count
-    traffic = (DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH if two else DRAM_BYTES_PER_PARTICLE_FUSED) * n
+    traffic = None
+    if two:
+        traffic = DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH * n
+    elif mapping[1] == 0:
+        traffic = DRAM_BYTES_PER_PARTICLE_FUSED * n
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": ALG_BYTES * n,
@@ -830,7 +836,7 @@ def run_gpu(args):
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, sampled on the device)",
                "config": workload(args),
                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-               "mapping": {"lanes_per_cell": mapping[0], "launches_per_step": 2 if mapping[1] == 1 else 1,
+               "mapping": {"lanes_per_cell": mapping[0], "launch_form": FORMS[mapping[1]],
                            "autotune_steps": tune_steps},
                "collisions_per_s": coll, "candidates_per_s": cand,
                "hbm_frac_algorithmic": ALG_BYTES * value / world / (peak * 1e9),

@@ -123,8 +123,11 @@ typedef struct {
                              (0: 2,048; < 0: never); results do not depend on it */
     mz_grid1d grid;
     mz_walls1d walls;
-    int32_t launches;     /* 1-D: launches per step, 1 (fused) or 2 (sort + gather + props, then NTC +
-                             convection); 0: the autotuner's choice, else 1.  Results do not depend on it */
+    int32_t launches;     /* 1-D: 1 (one fused launch), 2 (sort + gather + props, then NTC + convection
+                             in a second launch) or 3 (one launch in which some warps of every block sort,
+                             gather and compute props cell by cell while the others collide and convect
+                             the cells already gathered); 0: the autotuner's choice, else 1.  Results do
+                             not depend on it */
     int64_t hit_queue_capacity; /* 1-D: entries of the queue of particles that reach a wall (0: a
                                    sixteenth of the particles, at least 4,096); particles beyond it are
                                    reflected inside the step kernel.  Results do not depend on it */
@@ -254,7 +257,9 @@ int mz_host_free(void* ptr);
 
 /* ---------------------------------------------------------------- convection */
 /* convect_particles! (convection_1D.jl:130-157) or, with
- * MZ_CONVECT_COMPUTE_CELL, convect_particles_and_compute_cell! (:225-255) */
+ * MZ_CONVECT_COMPUTE_CELL, convect_particles_and_compute_cell! (:225-255).
+ * grid: the domain's grid or, without MZ_CONVECT_COMPUTE_CELL, the global
+ * grid that a slab domain is part of (mz_slab_extract) */
 int mz_convect_1d(mz_domain* dom, int32_t species, const mz_grid1d* grid, const mz_walls1d* walls, double dt,
                   uint64_t step, int32_t flags);
 
@@ -474,14 +479,14 @@ int mz_server_set_hbm_headroom(mz_server* server, int64_t bytes);
 /* Choose the fused step's mapping by timing it: every combination of lanes
  * per cell in the warp-group NTC (8, 16, 32) and, for 0-D plans, of the
  * block-per-cell threshold (512, 2,048, 8,192 particles, never) or, for 1-D
- * plans, of one fused launch per step against two (sort + gather + props,
- * then NTC + convection) runs trial_steps real steps of `plan` twice, in
+ * plans, of the plan's launches 1, 2 and 3 runs trial_steps real steps of `plan` twice, in
  * two rounds of opposite order whose times add up (starting at
  * plan->step0; the state advances by
- * 24 * trial_steps steps for 0-D plans and 12 * trial_steps for 1-D, and
+ * 24 * trial_steps steps for 0-D plans and 18 * trial_steps for 1-D, and
  * every mapping gives the same results); the fastest is kept for later
  * mz_step calls whose plan leaves big_cell at 0.  *big_cell_out receives the
- * threshold (0-D) or 1 for the two-launch step (1-D).  A variable-weight plan
+ * threshold (0-D) or, for 1-D, the launches value minus one (0 fused, 1 two
+ * launches, 2 gathering and physics warps side by side).  A variable-weight plan
  * (equal_weight = 0) tries only the lanes per cell of its splitting NTC
  * (6 * trial_steps steps) and *big_cell_out receives 0.  No counterpart in
  * the reference. */
@@ -496,6 +501,32 @@ int mz_get_counters(mz_domain* dom, mz_counters* out, int32_t reset);
  * s[i], c[i] = sin, cos of 2 pi m[i] 2^-52 for 52-bit integers m[i] (the
  * uniform draw's mantissa).  Host arrays of n elements; for accuracy tests. */
 int mz_sincos_2pi(mz_ctx* ctx, int64_t n, const uint64_t* m, double* s, double* c);
+
+/* ---------------------------------------------------------------- slabs */
+/* One 1-D grid over several GPUs, one process each (exchange_particles! and
+ * sort_particles_after_exchange!, parallel.jl:281-532, move particles
+ * between the cell chunks of a multithreaded run).  A rank's domain holds
+ * the cells [c0, c0 + n_cells) of the global grid `grid` (give them the
+ * global cell ids with mz_set_cell_rng, so every stream is the one a single
+ * domain would draw), convects on the global grid and walls
+ * (mz_convect_1d without MZ_CONVECT_COMPUTE_CELL), then:
+ *   mz_slab_extract : frees the particles now outside the slab and stages
+ *                     them, *n_left for the left neighbour and *n_right for
+ *                     the right one, in slot order;
+ *   mz_slab_fetch   : copies them to the host, 7 doubles per particle
+ *                     (w, vx, vy, vz, x, y, z);
+ *   mz_slab_insert  : after the caller's exchange with the neighbours,
+ *                     rebuilds the storage as [from the left | own | from the
+ *                     right] and sorts it by cell.
+ * Every cell's particles end in the order a single domain over the whole
+ * grid gives them, so a sharded equal-weight run equals the single-domain
+ * run bit for bit.  A particle that crossed a whole neighbour's slab in one
+ * step is clamped into the slab and reported (MZ_E_STATE). */
+int mz_slab_extract(mz_domain* dom, int32_t species, const mz_grid1d* grid, int64_t c0, int64_t* n_left,
+                    int64_t* n_right);
+int mz_slab_fetch(mz_domain* dom, int32_t species, double* left, double* right);
+int mz_slab_insert(mz_domain* dom, int32_t species, const mz_grid1d* grid, int64_t c0, const double* from_left,
+                   int64_t n_left, const double* from_right, int64_t n_right);
 
 /* ---------------------------------------------------------------- validators */
 /* The reference's indexing checks (particles.jl:805-1025) on the device

@@ -124,7 +124,8 @@ void check_status(mz_domain* d)
         if (st & ST_MERGE_BINS) m += " octree bin limit reached;";
         if (st & ST_SEGMENT) m += " cell too large for the sort path;";
         if (st & ST_WALL_HITS) m += " wall-hit cap reached;";
-        throw MzError(MZ_E_STATE, m);
+        if (st & ST_TIMEOUT) m += " a bounded wait for gathered cells gave up;";
+        throw MzError((st & ST_TIMEOUT) ? MZ_E_TIMEOUT : MZ_E_STATE, m);
     }
 }
 
@@ -422,6 +423,8 @@ int mz_domain_destroy(mz_domain* d)
     cudaFree(d->d_hitq);
     cudaFree(d->d_vw);
     cudaFreeHost(d->h_vw);
+    cudaFree(d->d_ready);
+    free_slab_scratch(d);
     cudaFreeHost(d->h_scalar);
     delete d;
     return MZ_OK;
@@ -837,7 +840,10 @@ int mz_convect_1d(mz_domain* d, int32_t s, const mz_grid1d* g, const mz_walls1d*
 {
     API_TRY
     MZ_REQUIRE(d && g && w && s >= 0 && s < d->ns, "mz_convect_1d: bad argument");
-    MZ_REQUIRE(g->n_cells == d->n_cells, "mz_convect_1d: grid and domain cell counts differ");
+    // a slab of a larger grid convects on the global grid and walls without
+    // computing cells (mz_slab_extract maps positions to cells afterwards)
+    MZ_REQUIRE(g->n_cells == d->n_cells || (!(flags & MZ_CONVECT_COMPUTE_CELL) && g->n_cells > d->n_cells),
+               "mz_convect_1d: grid and domain cell counts differ");
     MZ_CK(cudaSetDevice(d->ctx->device));
     launch_convect(d, s, g, w, dt, step, flags);
     API_CATCH(d->ctx)

@@ -126,13 +126,16 @@ struct mz_domain_s {
     mz_surf_props* step_surf_avg = nullptr;
     // fused step: RNG step index and last-block counter
     uint32_t* d_step = nullptr;
-    unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block, next big cell, big last block}
+    unsigned int* d_done = nullptr;  // fused step: {last block, next cell, wall hits queued, wall last block, next big cell, big last block, next consumer cell, launch epoch}
     void* d_hitq = nullptr;          // fused step: wall-hit queue (int4 entries)
     int64_t hitq_cap = 0;
     // fused-step mapping chosen by mz_step_autotune (0: the default rules)
     int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
     int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
-    int32_t tuned_split = 0;    // 1-D: 1 = gather + props and NTC + convection in two launches
+    int32_t tuned_split = 0;    // 1-D: 1 = gather + props and NTC + convection in two launches,
+                                // 2 = one launch with gathering and physics warps side by side
+    int* d_ready = nullptr;     // per-cell publication words of that launch
+    struct mz_slab_scratch* slab = nullptr;  // slab exchange scratch (slab.cu)
     // fused variable-weight step
     VwDev* d_vw = nullptr;
     VwDev* h_vw = nullptr;      // pinned mirror
@@ -231,6 +234,7 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
 void launch_fill_i32(mz_ctx* c, int32_t* p, int64_t n, int32_t v);
 void reserve_species(mz_domain* d, int s, int64_t cap);
 void launch_key_from_cell(mz_domain* d, int s);
+void free_slab_scratch(mz_domain* d);
 void launch_avg(mz_ctx* c, double* avg, const double* inst, int64_t n, double inv);
 
 // Lanes per cell in the NTC kernels.  A conflict-free batch of a cell with n

@@ -34,6 +34,7 @@ enum : int {
     ST_MERGE_BINS = 4,    // octree bin scratch exhausted
     ST_SEGMENT = 8,       // sort segment too large for the sorting path
     ST_WALL_HITS = 16,    // wall-hit loop reached its iteration cap
+    ST_TIMEOUT = 32,      // a bounded wait for another warp's data gave up
 };
 
 // ------------------------------------------------------------------ RNG
@@ -186,6 +187,15 @@ __device__ __forceinline__ PX ldg_px(const PX* p)
     const double2* q = reinterpret_cast<const double2*>(p);
     const double2 a = __ldg(q), b = __ldg(q + 1);
     return PX{a.x, a.y, b.x, b.y};
+}
+
+// the same records through L2 only (ld.global.cg): for records another SM
+// wrote earlier in the same launch, which this SM's L1 may hold stale
+__device__ __forceinline__ PV ldcg_pv(const PV* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return PV{a.x, a.y, b.x, b.y};
 }
 
 struct Indexer {  // {start1, n_group1, start2, n_group2}, 0-based slots

@@ -61,7 +61,36 @@ struct StepArgs {
     double* surf_avg;     // their average, or nullptr
     double surf_factor[MZ_MAX_SPECIES];  // mass / dt per species (surface_props_scale!)
     const int* abort;     // variable-weight step: nonzero = the step was abandoned (do nothing), or nullptr
+    // producer / consumer launch (k_cell_ws): gathered cells are published
+    // in ready[c] with the launch's tag (*epoch + 1, unique per launch)
+    int* ready;
+    unsigned int* epoch;
+    unsigned int* cons_next;  // next cell for the consumer warps
+    int producer_warps;       // warps per block that gather
 };
+
+// release store / acquire load of a publication word (GPU scope)
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// bounded wait until *p == v: back-off sleeps, at most ~2^24 tries (seconds);
+// false when it gave up
+__device__ __forceinline__ bool wait_for(const int* p, int v)
+{
+    for (int k = 0; k < (1 << 24); ++k) {
+        if (ld_acquire(p) == v) return true;
+        __nanosleep(k < 64 ? 32 : 256);
+    }
+    return false;
+}
 
 // cells of the per-warp destination histogram of k_cell (48 KB per block)
 constexpr int CELL_WINDOW = 1536;
@@ -97,13 +126,18 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
 // MODE 0: the phases the launch's flags select; MODE 1: sort + gather + props
 // only (no NTC or convection code, so fewer registers and more resident
 // warps for this memory-bound part); MODE 2: NTC + convection in place only.
-template <int G, int MODE>
+// WS (k_cell_ws): MODE 1 warps publish every gathered cell; MODE 2 warps take
+// cells from their own counter, wait for the cells' publication and run NTC +
+// convection on the gathered buffer B, reading its records through L2.
+template <int G, int MODE, bool WS = false>
 __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a, int32_t* cell_hist)
 {
     constexpr int CPW = 32 / G;
     const bool gather_on = MODE == 1 ? true : (MODE == 2 ? false : a.gather != 0);
     const bool physics_on = MODE == 1 ? false : (MODE == 2 ? true : a.physics != 0);
+    const bool onB = gather_on || (WS && MODE == 2);  // the physics works on the gathered buffer
     const uint32_t step = *a.step_ptr;
+    const int tag = WS ? (int)(*a.epoch + 1u) : 0;
     const int lane = threadIdx.x & 31;
     int32_t* wh = cell_hist + (threadIdx.x >> 5) * CELL_WINDOW;
     if (MODE != 1) {
@@ -120,15 +154,25 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
     for (;;) {
         if (abandoned) break;
         unsigned int t = 0;
-        if (lane == 0) t = atomicAdd(a.next, (unsigned)CPW);
+        if (lane == 0) t = atomicAdd((WS && MODE == 2) ? a.cons_next : a.next, (unsigned)CPW);
         const int c0 = (int)__shfl_sync(0xFFFFFFFFu, t, 0);
         if (c0 >= d.n_cells) break;
         const int nq = min(CPW, d.n_cells - c0);
+        if (WS && MODE == 2) {
+            // wait until the producers have published these cells
+            bool ok = true;
+            if (lane < nq) ok = wait_for(a.ready + c0 + lane, tag);
+            if (!ok) set_status(d, ST_TIMEOUT);
+            __syncwarp();
+            __threadfence();
+        }
         // sort + gather (A -> B), then 1-D props of the freshly sorted state
         // (the gather accumulates the first props pass)
         for (int s = 0; s < ns; ++s) {
             const SpeciesView& S = d.sp[s];
-            const bool props1 = a.props && a.props_lag == 1;
+            // the physics-only mode never computes props (in the side-by-side
+            // launch the gathering warps do)
+            const bool props1 = MODE != 2 && a.props && a.props_lag == 1;
             double mn = 0.0, msx = 0.0, msy = 0.0, msz = 0.0;
             if (gather_on) {
                 for (int q = 0; q < nq; ++q) {
@@ -147,6 +191,13 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                 if (lane < nq)
                     write_props(a, (int64_t)(c0 + lane) + (int64_t)d.n_cells * s, r, S.ind[c0 + lane].n1, step);
             }
+        }
+        if (WS && MODE == 1) {
+            // publish: every lane's stores of these cells before the flag
+            __threadfence();
+            __syncwarp();
+            if (lane < nq) st_release(a.ready + c0 + lane, tag);
+            continue;
         }
         __syncwarp();
         if (!physics_on && !(a.props && a.props_lag == 0)) continue;
@@ -177,9 +228,9 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                     R.smax = cf.smax;
                     R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
                     if (ncoll > 0)
-                        R = ntc_cell<true, G>(d, d.inter[cfi], single, c, ncoll, cf.smax, gather_on ? S1.B : S1.A,
-                                              gather_on ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
-                                              0, 0.0, seed, pc, stp, rid);
+                        R = ntc_cell<true, G, WS>(d, d.inter[cfi], single, c, ncoll, cf.smax, onB ? S1.B : S1.A,
+                                                  onB ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
+                                                  0, 0.0, seed, pc, stp, rid);
                     if (grp.rank == 0) {
                         cand += ncoll;
                         accd += R.perf;
@@ -214,7 +265,7 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
         const int kb = c0 + CPW / 2 - CELL_WINDOW / 2;
         for (int s = 0; s < ns; ++s) {
             const SpeciesView& S = d.sp[s];
-            const Cols& Q = gather_on ? S.B : S.A;
+            const Cols& Q = onB ? S.B : S.A;
             for (int q = 0; q < nq; ++q) {
                 const int cq = c0 + q;
                 const uint64_t seed = cell_seed(d, cq);
@@ -228,8 +279,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                     int32_t key = 0;
                     bool counted = false, hit = false;
                     if (in) {
-                        double x = Q.pos[qq].x;
-                        const double xn = fma(Q.wv[qq].vx, a.dt, x);
+                        double x = WS ? __ldcg(&Q.pos[qq].x) : Q.pos[qq].x;
+                        const double xn = fma(WS ? __ldcg(&Q.wv[qq].vx) : Q.wv[qq].vx, a.dt, x);
                         if (move_free(a.W, xn, x)) {
                             Q.pos[qq].x = x;
                             key = cell_of(d, x, a.W.inv_dx);
@@ -253,8 +304,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                         } else if (hit) {
                             Stream rs;
                             rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
-                            const PV r = Q.wv[qq];
-                            double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
+                            const PV r = WS ? ldcg_pv(Q.wv + qq) : Q.wv[qq];
+                            double x = WS ? __ldcg(&Q.pos[qq].x) : Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
                             SurfAcc one = {};
                             hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap, a.surf ? &one : nullptr, r.w);
                             if (a.surf)
@@ -310,6 +361,10 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
             *a.done = 0;
             *a.next = 0;
             if (a.join_blocks) *a.big_next = 0;
+            if (WS) {
+                *a.cons_next = 0;
+                *a.epoch = (unsigned)tag;
+            }
             if (a.advance) *a.step_ptr = step + 1;
             __threadfence();
         }
@@ -339,6 +394,23 @@ __global__ void __launch_bounds__(256, 2) k_cell_physics(DomainView d, StepArgs 
 {
     extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
     cell_body<G, 2>(d, a, cell_hist);
+}
+
+// The 1-D step in one launch with the two halves of the two-launch form side
+// by side: the first producer_warps warps of every block sort, gather and
+// compute props cell by cell (memory-bound) and publish each gathered cell;
+// the other warps take cells in groups of 32 / G, wait for them and run NTC
+// + convection on them (FP64-bound) while they are still in L2.  Producers
+// never wait, so every cell a consumer waits for is gathered by a running
+// producer.
+template <int G>
+__global__ void __launch_bounds__(256, 2) k_cell_ws(DomainView d, StepArgs a)
+{
+    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
+    if ((int)(threadIdx.x >> 5) < a.producer_warps)
+        cell_body<32, 1, true>(d, a, cell_hist);
+    else
+        cell_body<G, 2, true>(d, a, cell_hist);
 }
 
 __global__ void k_set_step(uint32_t* step, uint32_t value) { *step = value; }
@@ -800,11 +872,24 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         a.hitq_cap = (unsigned)std::min<int64_t>(std::min(want, d->hitq_cap), 0x7FFFFFFF);
     }
     const bool want_props = plan->props && (inst || a.has_avg);
-    const bool split = plan->dims == 1 && (plan->launches == 2 || (plan->launches == 0 && d->tuned_split > 0));
+    const bool split = plan->dims == 1 && (plan->launches == 2 || (plan->launches == 0 && d->tuned_split == 1));
+    // one launch with gathering and physics warps side by side (k_cell_ws)
+    const bool ws = plan->dims == 1 && (plan->launches == 3 || (plan->launches == 0 && d->tuned_split == 2));
+    if (ws) {
+        if (!d->d_ready) {
+            MZ_CK(cudaMalloc(&d->d_ready, d->n_cells * sizeof(int)));
+            MZ_CK(cudaMemsetAsync(d->d_ready, 0, d->n_cells * sizeof(int), c->stream));
+        }
+        a.ready = d->d_ready;
+        a.cons_next = d->d_done + 6;
+        a.epoch = d->d_done + 7;
+        a.producer_warps = 4;
+    }
     const int G = d->tuned_lanes ? d->tuned_lanes : ntc_group_width(d->n_cells);
     using KCell = void (*)(DomainView, StepArgs);
     const KCell kern_full = G == 8 ? k_cell<8> : (G == 16 ? k_cell<16> : k_cell<32>);
     const KCell kern_phys = G == 8 ? k_cell_physics<8> : (G == 16 ? k_cell_physics<16> : k_cell_physics<32>);
+    const KCell kern_ws = G == 8 ? k_cell_ws<8> : (G == 16 ? k_cell_ws<16> : k_cell_ws<32>);
     // a resident grid: as many blocks as fit at once, no more than the cells need
     auto resident = [&](KCell k, size_t smem, int cpw) {
         int per_sm = 0;
@@ -815,6 +900,13 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     const int blocks_full = resident(kern_full, CELL_SMEM, 32 / G);
     const int blocks_phys = plan->dims == 1 ? resident(kern_phys, CELL_SMEM, 32 / G) : 0;
     const int blocks_gather = plan->dims == 1 ? resident(k_cell_gather, 0, 1) : 0;
+    int blocks_ws = 0;
+    if (ws) {
+        int per_sm = 0;
+        MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_ws, 256, CELL_SMEM));
+        blocks_ws = (int)std::max<int64_t>(
+            1, std::min<int64_t>(div_up(d->n_cells, 8), (int64_t)c->num_sms * std::max(per_sm, 1)));
+    }
 
     auto cell_launch = [&](int gather, int props, int physics, int advance = 1) {
         StepArgs b = a;
@@ -853,7 +945,9 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
             MZ_CK(cudaMemsetAsync(b.surf, 0, (size_t)d->ns * 2 * SURF_Q * sizeof(double), c->stream));
         // 1-D launches that only sort + gather + props, or only collide and
         // convect, take the kernels compiled for that part alone
-        if (a.dims == 1 && gather && !physics)
+        if (a.dims == 1 && gather && physics && ws)
+            MZ_LAUNCH(c, name, kern_ws, blocks_ws, 256, CELL_SMEM, v, b);
+        else if (a.dims == 1 && gather && !physics)
             MZ_LAUNCH(c, name, k_cell_gather, blocks_gather, 256, 0, v, b);
         else if (a.dims == 1 && !gather && !props && physics)
             MZ_LAUNCH(c, name, kern_phys, blocks_phys, 256, CELL_SMEM, v, b);
@@ -1145,7 +1239,7 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     // against the two-launch step (1-D)
     // a variable-weight plan has only the lanes per cell of its splitting NTC
     const bool vw = !plan->equal_weight;
-    const int nb = vw ? 1 : (plan->dims == 0 ? 4 : 2);
+    const int nb = vw ? 1 : (plan->dims == 0 ? 4 : 3);
     const int nconf = 3 * nb;
     mz_step_plan p = *plan;
     p.big_cell = 0;

@@ -138,7 +138,7 @@ def bench_reference(ctx, orc):
                 last=last, avg=ref_avg)
 
 
-@pytest.mark.parametrize("launches", [2, 1])
+@pytest.mark.parametrize("launches", [2, 1, 3])
 def test_bench_couette_steps_match_oracle(ctx, bench_reference, launches):
     """mz_step on the benchmark workload (the graph-replayed step, fused or
     two launches per step) equals the reference loop: 50,000 cells exceed
@@ -160,7 +160,7 @@ def test_bench_couette_steps_match_oracle(ctx, bench_reference, launches):
     dom.close()
 
 
-@pytest.mark.parametrize("launches,hitq", [(1, 0), (2, 0), (1, 64), (2, 64)])
+@pytest.mark.parametrize("launches,hitq", [(1, 0), (2, 0), (3, 0), (1, 64), (2, 64), (3, 64)])
 def test_far_movers_on_a_multi_tile_grid_match_oracle(ctx, orc, launches, hitq):
     """7,000 cells (four scan tiles) and dt = 2e-7 s: particles move ~670
     cells per step (a standard deviation), so many destinations fall outside

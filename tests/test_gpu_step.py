@@ -252,19 +252,20 @@ def test_autotuned_mapping_changes_no_result(ctx, orc):
         done = 0
         if tune:
             dom.autotune(plan, trial_steps=1)
-            done = 12
-        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 16 - done)
+            done = 18
+        dom.step(couette_plan(grid, walls, dt, step0=done, props=False), 22 - done)
         states.append(device_logical(dom, 0))
         dom.close()
     assert np.array_equal(states[0][1], states[1][1]) and np.array_equal(states[0][0], states[1][0])
 
 
 def test_two_launch_step_equals_fused(ctx, orc):
-    """The 1-D step as one fused launch and as two (sort + gather + props, then
-    NTC + convection in place) gives the same particles and the same averaged
-    and instantaneous properties, and both equal the oracle loop's averages."""
+    """The 1-D step as one fused launch, as two (sort + gather + props, then
+    NTC + convection in place) and as one launch with gathering and physics
+    warps side by side gives the same particles and the same averaged and
+    instantaneous properties, and all equal the oracle loop's averages."""
     results = []
-    for launches in (1, 2):
+    for launches in (1, 2, 3):
         sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc, nx=60, ppc=100, seed=23)
         inst, avg = mz.PhysProps(dom), mz.PhysProps(dom)
         plan = couette_plan(grid, walls, dt, avg_start=3, n_avg=5)
@@ -274,10 +275,11 @@ def test_two_launch_step_equals_fused(ctx, orc):
         if launches == 2:
             ref_avg = oracle_couette(orc, o, grid, walls, dt, seed, 7, 3)
         dom.close()
-    (r1, i1, a1), (r2, i2, a2) = results
-    assert np.array_equal(r1[1], r2[1]) and np.array_equal(r1[0], r2[0])
-    for k in ("np", "n", "v", "T"):
-        assert np.array_equal(i1[k], i2[k]) and np.array_equal(a1[k], a2[k]), k
+    (r1, i1, a1) = results[0]
+    for r2, i2, a2 in results[1:]:
+        assert np.array_equal(r1[1], r2[1]) and np.array_equal(r1[0], r2[0])
+        for k in ("np", "n", "v", "T"):
+            assert np.array_equal(i1[k], i2[k]) and np.array_equal(a1[k], a2[k]), k
     assert_close_rows(a2["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T, two launches")
 
 
@@ -315,7 +317,7 @@ def test_two_species_couette_step_matches_reference_loop(ctx, orc):
             o.convect(s, L, nx, walls.as_flat_array(), dt, seed, step)
             o.sort(s, L=L, nx=nx)
     states = []
-    for launches in (1, 2):
+    for launches in (1, 2, 3):
         dom = mz.Domain(ctx, nx, sp, 4 * 60 * nx, interactions=inter, seed=seed)
         dom.set_cell_volumes(grid.V)
         for s in range(2):
@@ -328,8 +330,10 @@ def test_two_species_couette_step_matches_reference_loop(ctx, orc):
         states.append([device_logical(dom, s) for s in range(2)])
         dom.close()
     for s in range(2):
-        (r1, c1), (r2, c2) = states[0][s], states[1][s]
-        assert np.array_equal(c1, c2) and np.array_equal(r1, r2), f"species {s}: fused and two-launch differ"
+        (r1, c1) = states[0][s]
+        for other in states[1:]:
+            (r2, c2) = other[s]
+            assert np.array_equal(c1, c2) and np.array_equal(r1, r2), f"species {s}: the launch forms differ"
         orows, oc = oracle_logical(o, s)
         assert np.array_equal(oc, c1), f"species {s}: cells"
         assert_close_rows(orows, r1, 1e-11, f"species {s} after {steps} steps")
