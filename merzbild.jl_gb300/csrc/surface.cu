@@ -127,7 +127,8 @@ int mz_convect_1d_surf(mz_domain* d, int32_t s, const mz_grid1d* g, const mz_wal
     API_TRY
     MZ_REQUIRE(d && g && w && surf && surf->dom == d, "mz_convect_1d_surf: bad argument");
     MZ_REQUIRE(s >= 0 && s < d->ns, "mz_convect_1d_surf: bad species");
-    MZ_REQUIRE(g->n_cells == d->n_cells, "mz_convect_1d_surf: grid and domain cell counts differ");
+    MZ_REQUIRE(g->n_cells == d->n_cells || (!(flags & MZ_CONVECT_COMPUTE_CELL) && g->n_cells > d->n_cells),
+               "mz_convect_1d_surf: grid and domain cell counts differ");
     MZ_CK(cudaSetDevice(d->ctx->device));
     double* acc = surf->acc + (size_t)s * 2 * SURF_Q;
     MZ_CK(cudaMemsetAsync(acc, 0, 2 * SURF_Q * sizeof(double), d->ctx->stream));

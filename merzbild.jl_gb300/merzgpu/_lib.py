@@ -142,6 +142,9 @@ _SIGS = {
     "mz_server_set_lane_split": (i32, [vp, i64]),
     "mz_server_set_hbm_headroom": (i32, [vp, i64]),
     "mz_check_indexing": (i32, [vp, i32, i32, P(i32), P(i64)]),
+    "mz_slab_extract": (i32, [vp, i32, P(Grid1D), i64, P(i64), P(i64)]),
+    "mz_slab_fetch": (i32, [vp, i32, P(d), P(d)]),
+    "mz_slab_insert": (i32, [vp, i32, P(Grid1D), i64, P(d), i64, P(d), i64]),
     "mz_set_indexer": (i32, [vp, i32, P(ParticleIndexer), i64]),
     "mz_swpm": (i32, [vp, i32, d, d, i64, i64, u64]),
     "mz_props_snapshot": (i32, [vp, i32, P(d)]),

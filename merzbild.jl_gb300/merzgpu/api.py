@@ -441,6 +441,31 @@ class Domain:
         self._ck(lib().mz_convect_1d(self.h, species, C.byref(g), C.byref(w), float(dt), int(step),
                                      L.CONVECT_COMPUTE_CELL if compute_cell else 0))
 
+    # slabs of a larger grid (mz_slab_*) ---------------------------------------
+    def slab_extract(self, species, grid, c0):
+        """Free the particles that left the slab [c0, c0 + n_cells) of the
+        global grid and stage them; returns (to the left, to the right)."""
+        g = grid.c_struct()
+        nl, nr = C.c_int64(), C.c_int64()
+        self._ck(lib().mz_slab_extract(self.h, species, C.byref(g), int(c0), C.byref(nl), C.byref(nr)))
+        self._slab_pending = (nl.value, nr.value)
+        return nl.value, nr.value
+
+    def slab_fetch(self, species):
+        """The staged particles as two (n, 7) arrays of w, vx, vy, vz, x, y, z."""
+        nl, nr = self._slab_pending
+        left, right = np.empty((nl, 7)), np.empty((nr, 7))
+        self._ck(lib().mz_slab_fetch(self.h, species, ptr(left) if nl else None, ptr(right) if nr else None))
+        return left, right
+
+    def slab_insert(self, species, grid, c0, from_left, from_right):
+        """Add the arrivals from the neighbours and sort the slab by cell."""
+        g = grid.c_struct()
+        a = np.ascontiguousarray(from_left, np.float64).reshape(-1, 7)
+        b = np.ascontiguousarray(from_right, np.float64).reshape(-1, 7)
+        self._ck(lib().mz_slab_insert(self.h, species, C.byref(g), int(c0), ptr(a) if a.shape[0] else None,
+                                      a.shape[0], ptr(b) if b.shape[0] else None, b.shape[0]))
+
     def sort(self, species, grid=None, return_index=False):
         out = None
         if return_index:

@@ -88,6 +88,9 @@ struct Orc {
     std::vector<double> mass;
     std::vector<Interaction> inter;              // [s1 + ns * s2]
     std::vector<CollisionFactors> cf;            // [s1 + ns * (s2 + ns * (cell-1))]
+    // global id of cell 1 minus one: a slab of a larger grid keys the
+    // collision, convection and merge streams of its cell c on c - 1 + cell_offset
+    int64_t cell_offset = 0;
 
     ParticleIndexer& pi(int64_t cell, int s) { return indexer[(cell - 1) + n_cells * s]; }
     CollisionFactors& cfa(int s1, int s2, int64_t cell) {
@@ -409,7 +412,7 @@ void ntc_single(Orc& o, int s, int64_t cell, double dt, double V, uint64_t seed,
 {
     CollisionFactors& cf = o.cfa(s, s, cell);
     const uint32_t pc = pair_code(o, s, s);
-    const uint32_t rc = (uint32_t)(cell - 1);
+    const uint32_t rc = (uint32_t)(cell - 1 + o.cell_offset);
     int64_t np = o.pi(cell, s).n_local;
     cf.n1 = np;
     cf.n2 = np;
@@ -449,7 +452,7 @@ void ntc_two(Orc& o, int s1, int s2, int64_t cell, double dt, double V, uint64_t
 {
     CollisionFactors& cf = o.cfa(s1, s2, cell);
     const uint32_t pc = pair_code(o, s1, s2);
-    const uint32_t rc = (uint32_t)(cell - 1);
+    const uint32_t rc = (uint32_t)(cell - 1 + o.cell_offset);
     int64_t np1 = o.pi(cell, s1).n_local, np2 = o.pi(cell, s2).n_local;
     cf.n1 = np1;
     cf.n2 = np2;
@@ -491,7 +494,7 @@ void swpm_cell(Orc& o, int s, int64_t cell, double G, double dt, double V, uint6
 {
     CollisionFactors& cf = o.cfa(s, s, cell);
     const uint32_t pc = pair_code(o, s, s);
-    const uint32_t rc = (uint32_t)(cell - 1);
+    const uint32_t rc = (uint32_t)(cell - 1 + o.cell_offset);
     ParticleVector& P = o.pv[s];
     double w_max = 0.0;
     {
@@ -819,7 +822,8 @@ void convect_particles(Orc& o, int s, const Grid1D& g, const Walls& W, double dt
         ParticleIndexer p = o.pi(cell, s);
         int64_t j = 0;
         auto one = [&](int64_t i) {
-            orc_stream rng = orc_stream_make(seed, ORC_TAG_CONVECT, (uint32_t)s, step, (uint32_t)(cell - 1), (uint32_t)j);
+            orc_stream rng = orc_stream_make(seed, ORC_TAG_CONVECT, (uint32_t)s, step, (uint32_t)(cell - 1 + o.cell_offset),
+                                              (uint32_t)j);
             ++j;
             convect_single_particle(&rng, g, W, pv.at(i), s, dt, surf);
             if (compute_cell) pv.cell[i - 1] = get_cell(g, pv.at(i).x[0]);
@@ -1259,7 +1263,7 @@ void compute_new_particles(orc_stream* rng, Octree& oc, Orc& o, int s, int64_t c
 void merge_octree_N2_based(Octree& oc, Orc& o, int s, int64_t cell, int64_t target, const Grid1D* g, uint64_t seed,
                            uint64_t step)     // :1060-1066 and :1088-1094
 {
-    orc_stream rng = orc_stream_make(seed, ORC_TAG_MERGE, (uint32_t)s, step, (uint32_t)(cell - 1), 0);
+    orc_stream rng = orc_stream_make(seed, ORC_TAG_MERGE, (uint32_t)s, step, (uint32_t)(cell - 1 + o.cell_offset), 0);
     oc.Nbins = 0;
     resize_octree_buffers(oc, o.pi(cell, s).n_local);
     init_octree(oc, o, s, cell);
@@ -1386,6 +1390,7 @@ void orc_get_interaction(void* h, int32_t s1, int32_t s2, double* rec)
 }
 
 void orc_pv_create(void* h, int32_t s, int64_t np) { pv_init(((Orc*)h)->pv[s], np); }
+void orc_set_cell_offset(void* h, int64_t offset) { ((Orc*)h)->cell_offset = offset; }
 void orc_pv_resize(void* h, int32_t s, int64_t np) { pv_resize(((Orc*)h)->pv[s], np); }
 int64_t orc_pv_length(void* h, int32_t s) { return ((Orc*)h)->pv[s].length(); }
 

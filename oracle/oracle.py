@@ -55,6 +55,7 @@ def lib():
             "orc_load_interactions": (None, [vp, P(d), P(d), P(d)]),
             "orc_get_interaction": (None, [vp, i32, i32, P(d)]),
             "orc_pv_create": (None, [vp, i32, i64]),
+            "orc_set_cell_offset": (None, [vp, i64]),
             "orc_pv_resize": (None, [vp, i32, i64]),
             "orc_pv_length": (i64, [vp, i32]),
             "orc_pv_get": (None, [vp, i32, P(d), P(i64), P(i64), P(i64), P(i64)]),
@@ -183,6 +184,12 @@ class Oracle:
         self.L.orc_get_interaction(self.h, s1, s2, _p(r))
         keys = ["m_r", "mu1", "mu2", "vhs_d", "vhs_o", "vhs_Tref", "vhs_muref", "vhs_factor"]
         return dict(zip(keys, r))
+
+    def set_cell_offset(self, offset):
+        """Global id of cell 1 minus one, for a slab of a larger grid: the
+        collision, convection and merge streams of cell c are keyed on the
+        global cell c - 1 + offset."""
+        self.L.orc_set_cell_offset(self.h, int(offset))
 
     def pv_create(self, s, np_):
         self.L.orc_pv_create(self.h, s, np_)
