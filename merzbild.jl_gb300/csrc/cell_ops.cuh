@@ -86,9 +86,8 @@ __device__ __forceinline__ long long max_key(double s, bool present)
 // Candidates are evaluated in conflict-free batches of up to G (see ntc.cu).
 // A warp instruction serves every group, so with G = 8 one FP64 instruction
 // covers the candidates of four cells instead of the ~12 conflict-free
-// candidates one cell offers.  CG: read the records through L2 only (records
-// written by another SM during the same launch).
-template <bool EQW, int G, bool CG = false>
+// candidates one cell offers.
+template <bool EQW, int G>
 __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interaction& I, bool single, int c,
                                               int32_t ncoll, double smax, const Cols& P1, const Cols& P2,
                                               Indexer& p1, Indexer& p2, int32_t* cell1, int32_t* key1,
@@ -153,8 +152,8 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
         if (act) {
             si = map_slot(p1, i);
             sk = map_slot(p2, k);
-            a = CG ? ldcg_pv(P1.wv + si) : P1.wv[si];
-            b = CG ? ldcg_pv(P2.wv + sk) : P2.wv[sk];
+            a = P1.wv[si];
+            b = P2.wv[sk];
             // compute_g! (collision_utils.jl:388-391)
             const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
             g2 = (gx * gx + gy * gy) + gz * gz;

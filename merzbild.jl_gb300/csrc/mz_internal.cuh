@@ -189,15 +189,6 @@ __device__ __forceinline__ PX ldg_px(const PX* p)
     return PX{a.x, a.y, b.x, b.y};
 }
 
-// the same records through L2 only (ld.global.cg): for records another SM
-// wrote earlier in the same launch, which this SM's L1 may hold stale
-__device__ __forceinline__ PV ldcg_pv(const PV* p)
-{
-    const double2* q = reinterpret_cast<const double2*>(p);
-    const double2 a = __ldcg(q), b = __ldcg(q + 1);
-    return PV{a.x, a.y, b.x, b.y};
-}
-
 struct Indexer {  // {start1, n_group1, start2, n_group2}, 0-based slots
     int32_t start1, n1, start2, n2;
 };

@@ -152,6 +152,74 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
     }
 }
 
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only): the data in
+// flight holds no registers, so one warp can have a whole cell's records in
+// flight at once
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// sort_gather_regs with the gather staged in shared memory: every lane issues
+// the asynchronous copies of all its rows (64 bytes each) into `stage`
+// (STAGE_ROWS records of 64 bytes), waits for them, then writes the rows to B
+// with coalesced stores.  Each lane reads back only what it copied itself.
+constexpr int STAGE_ROWS = 512;
+
+template <int E>
+__device__ __forceinline__ void sort_gather_staged(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
+                                                   Sums4& acc, double2* stage)
+{
+    const int lane = threadIdx.x & 31;
+    int32_t v[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int q = r * 32 + lane;
+        v[r] = q < N ? S.idx[start + q] : INT_MAX;
+    }
+    warp_bitonic<E>(v);
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int q = r * 32 + lane;
+        if (q < N) {
+            const double2* pv = reinterpret_cast<const double2*>(S.A.wv + v[r]);
+            const double2* px = reinterpret_cast<const double2*>(S.A.pos + v[r]);
+            double2* o = stage + 4 * q;
+            cp_async16(o, pv);
+            cp_async16(o + 1, pv + 1);
+            cp_async16(o + 2, px);
+            cp_async16(o + 3, px + 1);
+        }
+    }
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int q = r * 32 + lane;
+        if (q < N) {
+            const double2* t = stage + 4 * q;
+            const double2 a = t[0], b = t[1], x0 = t[2], x1 = t[3];
+            double2* ov = reinterpret_cast<double2*>(S.B.wv + start + q);
+            double2* ox = reinterpret_cast<double2*>(S.B.pos + start + q);
+            ov[0] = a;
+            ov[1] = b;
+            ox[0] = x0;
+            ox[1] = x1;
+            const double w = a.x;
+            acc.n += w;
+            acc.sx += a.y * w;
+            acc.sy += b.x * w;
+            acc.sz += b.y * w;
+            S.cellB[start + q] = c;
+            S.key[start + q] = c;
+        }
+    }
+}
+
 // Segments above 512 particles take an out-of-line call, so the registers
 // their 32-row sort needs do not raise the register count of every caller.
 static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
@@ -187,6 +255,22 @@ __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32
             acc.sz += r.vz * r.w;
         }
     }
+    return acc;
+}
+
+// sort_gather_segment through a shared-memory stage of STAGE_ROWS records
+// (segments above that size take the register path)
+__device__ __forceinline__ Sums4 sort_gather_segment_staged(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
+                                                            double2* stage)
+{
+    Sums4 acc{0.0, 0.0, 0.0, 0.0};
+    if (N <= 0) return acc;
+    if (N <= 32) sort_gather_staged<1>(S, c, start, N, acc, stage);
+    else if (N <= 64) sort_gather_staged<2>(S, c, start, N, acc, stage);
+    else if (N <= 128) sort_gather_staged<4>(S, c, start, N, acc, stage);
+    else if (N <= 256) sort_gather_staged<8>(S, c, start, N, acc, stage);
+    else if (N <= STAGE_ROWS) sort_gather_staged<16>(S, c, start, N, acc, stage);
+    else return sort_gather_segment(S, c, start, N);
     return acc;
 }
 

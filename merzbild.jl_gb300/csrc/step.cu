@@ -126,11 +126,13 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
 // MODE 0: the phases the launch's flags select; MODE 1: sort + gather + props
 // only (no NTC or convection code, so fewer registers and more resident
 // warps for this memory-bound part); MODE 2: NTC + convection in place only.
-// WS (k_cell_ws): MODE 1 warps publish every gathered cell; MODE 2 warps take
-// cells from their own counter, wait for the cells' publication and run NTC +
-// convection on the gathered buffer B, reading its records through L2.
+// WS (k_cell_ws): MODE 1 warps gather through their shared-memory stage and
+// publish every gathered cell; MODE 2 warps take cells from their own
+// counter, wait for the cells' publication (acquire) and run NTC + convection
+// on the gathered buffer B.
 template <int G, int MODE, bool WS = false>
-__device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a, int32_t* cell_hist)
+__device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a, int32_t* cell_hist,
+                                          double2* stage = nullptr)
 {
     constexpr int CPW = 32 / G;
     const bool gather_on = MODE == 1 ? true : (MODE == 2 ? false : a.gather != 0);
@@ -177,7 +179,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
             if (gather_on) {
                 for (int q = 0; q < nq; ++q) {
                     const Indexer p = S.ind[c0 + q];
-                    const Sums4 t = sort_gather_segment(S, c0 + q, p.start1, p.n1);
+                    const Sums4 t = (WS && MODE == 1) ? sort_gather_segment_staged(S, c0 + q, p.start1, p.n1, stage)
+                                                      : sort_gather_segment(S, c0 + q, p.start1, p.n1);
                     if (props1) props_pass1_into_lane(t.n, t.sx, t.sy, t.sz, q, mn, msx, msy, msz);
                 }
                 __syncwarp();
@@ -228,9 +231,9 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                     R.smax = cf.smax;
                     R.perf = R.eqw = R.nsp1 = R.nsp2 = 0;
                     if (ncoll > 0)
-                        R = ntc_cell<true, G, WS>(d, d.inter[cfi], single, c, ncoll, cf.smax, onB ? S1.B : S1.A,
-                                                  onB ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0,
-                                                  0, 0.0, seed, pc, stp, rid);
+                        R = ntc_cell<true, G>(d, d.inter[cfi], single, c, ncoll, cf.smax, onB ? S1.B : S1.A,
+                                              onB ? S2.B : S2.A, q1, q2, nullptr, nullptr, nullptr, nullptr, 0, 0,
+                                              0.0, seed, pc, stp, rid);
                     if (grp.rank == 0) {
                         cand += ncoll;
                         accd += R.perf;
@@ -279,8 +282,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                     int32_t key = 0;
                     bool counted = false, hit = false;
                     if (in) {
-                        double x = WS ? __ldcg(&Q.pos[qq].x) : Q.pos[qq].x;
-                        const double xn = fma(WS ? __ldcg(&Q.wv[qq].vx) : Q.wv[qq].vx, a.dt, x);
+                        double x = Q.pos[qq].x;
+                        const double xn = fma(Q.wv[qq].vx, a.dt, x);
                         if (move_free(a.W, xn, x)) {
                             Q.pos[qq].x = x;
                             key = cell_of(d, x, a.W.inv_dx);
@@ -304,8 +307,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                         } else if (hit) {
                             Stream rs;
                             rs.init(seed, TAG_CONVECT, (uint32_t)s, stp, rid, (uint32_t)j);
-                            const PV r = WS ? ldcg_pv(Q.wv + qq) : Q.wv[qq];
-                            double x = WS ? __ldcg(&Q.pos[qq].x) : Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
+                            const PV r = Q.wv[qq];
+                            double x = Q.pos[qq].x, vx = r.vx, vy = r.vy, vz = r.vz;
                             SurfAcc one = {};
                             hits += convect_walls(rs, a.W, s, x, vx, vy, vz, a.dt, cap, a.surf ? &one : nullptr, r.w);
                             if (a.surf)
@@ -397,20 +400,30 @@ __global__ void __launch_bounds__(256, 2) k_cell_physics(DomainView d, StepArgs 
 }
 
 // The 1-D step in one launch with the two halves of the two-launch form side
-// by side: the first producer_warps warps of every block sort, gather and
-// compute props cell by cell (memory-bound) and publish each gathered cell;
-// the other warps take cells in groups of 32 / G, wait for them and run NTC
-// + convection on them (FP64-bound) while they are still in L2.  Producers
-// never wait, so every cell a consumer waits for is gathered by a running
-// producer.
+// by side, one block of WS_THREADS per SM: the first producer_warps warps sort,
+// gather and compute props cell by cell and publish each gathered cell; their
+// gathers go through a shared-memory stage of STAGE_ROWS records per warp, so
+// a few warps keep a whole cell's reads in flight each (the memory-bound
+// half needs bytes in flight, not warps).  The other warps take cells in
+// groups of 32 / G, wait for them and run NTC + convection on them
+// (FP64-bound) while their records are still in L2.  Producers never wait,
+// so every cell a consumer waits for is gathered by a running producer.
+constexpr int WS_THREADS = 512, WS_PRODUCERS = 4;
+constexpr size_t WS_SMEM = (size_t)(WS_THREADS / 32) * CELL_WINDOW * sizeof(int32_t) +
+                           (size_t)WS_PRODUCERS * STAGE_ROWS * 4 * sizeof(double2);
+
 template <int G>
-__global__ void __launch_bounds__(256, 2) k_cell_ws(DomainView d, StepArgs a)
+__global__ void __launch_bounds__(WS_THREADS, 1) k_cell_ws(DomainView d, StepArgs a)
 {
-    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp
-    if ((int)(threadIdx.x >> 5) < a.producer_warps)
-        cell_body<32, 1, true>(d, a, cell_hist);
-    else
+    extern __shared__ int32_t cell_hist[];  // CELL_WINDOW bins per warp, then the producers' stages
+    const int w = (int)(threadIdx.x >> 5);
+    if (w < a.producer_warps) {
+        double2* stage = reinterpret_cast<double2*>(cell_hist + (WS_THREADS / 32) * CELL_WINDOW) +
+                         (size_t)w * STAGE_ROWS * 4;
+        cell_body<32, 1, true>(d, a, cell_hist, stage);
+    } else {
         cell_body<G, 2, true>(d, a, cell_hist);
+    }
 }
 
 __global__ void k_set_step(uint32_t* step, uint32_t value) { *step = value; }
@@ -883,7 +896,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         a.ready = d->d_ready;
         a.cons_next = d->d_done + 6;
         a.epoch = d->d_done + 7;
-        a.producer_warps = 4;
+        a.producer_warps = WS_PRODUCERS;
     }
     const int G = d->tuned_lanes ? d->tuned_lanes : ntc_group_width(d->n_cells);
     using KCell = void (*)(DomainView, StepArgs);
@@ -902,10 +915,12 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
     const int blocks_gather = plan->dims == 1 ? resident(k_cell_gather, 0, 1) : 0;
     int blocks_ws = 0;
     if (ws) {
+        MZ_CK(cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM));
         int per_sm = 0;
-        MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_ws, 256, CELL_SMEM));
+        MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_ws, WS_THREADS, WS_SMEM));
+        MZ_REQUIRE(per_sm >= 1, "step: the side-by-side launch does not fit on an SM");
         blocks_ws = (int)std::max<int64_t>(
-            1, std::min<int64_t>(div_up(d->n_cells, 8), (int64_t)c->num_sms * std::max(per_sm, 1)));
+            1, std::min<int64_t>(div_up(d->n_cells, 8), (int64_t)c->num_sms * per_sm));
     }
 
     auto cell_launch = [&](int gather, int props, int physics, int advance = 1) {
@@ -946,7 +961,7 @@ void launch_step(mz_domain* d, const mz_step_plan* plan, int64_t n_steps, mz_pro
         // 1-D launches that only sort + gather + props, or only collide and
         // convect, take the kernels compiled for that part alone
         if (a.dims == 1 && gather && physics && ws)
-            MZ_LAUNCH(c, name, kern_ws, blocks_ws, 256, CELL_SMEM, v, b);
+            MZ_LAUNCH(c, name, kern_ws, blocks_ws, WS_THREADS, WS_SMEM, v, b);
         else if (a.dims == 1 && gather && !physics)
             MZ_LAUNCH(c, name, k_cell_gather, blocks_gather, 256, 0, v, b);
         else if (a.dims == 1 && !gather && !props && physics)
