@@ -287,6 +287,349 @@ __device__ __forceinline__ NtcResult ntc_cell(const DomainView& d, const Interac
     return R;
 }
 
+// ntc! with splitting (collision_ntc.jl:223-270) for one single-species cell,
+// one group of G lanes, with batches that run through several splits.
+//
+// In ntc_cell a batch ends at its first split, because the split appends a
+// particle and every later candidate draws its indices from the new count:
+// i = floor(rand() * n_local).  Here each lane evaluates its candidate for V
+// counts at once, n_local + v for v = 0 .. V-1 (its draws do not depend on
+// the count, only their scaling does), and the batch is then resolved in
+// candidate order, segment by segment: the lanes after the v-th split of the
+// batch take their version v values.  Within the batch the sequential loop is
+// reproduced exactly:
+//   * the running (sigma g w)_max is an inclusive max-scan over the resolved
+//     versions, so every acceptance test sees the maximum the loop would;
+//   * a candidate that touches a particle an earlier accepted candidate of
+//     the batch changed, or a particle a split of the batch created, ends the
+//     batch before it (rejected candidates change nothing, so only accepted
+//     ones count);
+//   * the batch ends after its V-th split.
+// All accepted candidates of a batch then collide at once, on disjoint
+// particles.  The position of a split-off particle (its parent's, unchanged
+// by collisions) is copied after the cell's loop; until then its key entry
+// holds the parent's slot.  (The chain of keys only leads back: a parent
+// split off in this call has a smaller slot than its children.)
+constexpr int NTC_SPLIT_VERSIONS = 3;
+
+template <int G, int V>
+__device__ __forceinline__ NtcResult ntc_cell_split(const DomainView& d, const Interaction& I, int c, int32_t ncoll,
+                                                    double smax, const Cols& P, Indexer& p, int32_t* cell,
+                                                    int32_t* key, int32_t b1, double dw_tol, uint64_t seed,
+                                                    uint32_t pc, uint32_t stp, uint32_t rid)
+{
+    const WarpGroup<G> grp;
+    const int gl = grp.rank;
+    const double vexp = fma(-2.0, I.vhs_o, 1.0);  // sigma_vhs exponent, collision_cross_sections.jl:179-181
+    const float lC = I.vhs_factor > 0.0 ? log2_pos(I.vhs_factor) : 1e30f;
+    const bool screen = fabsf(lC) < LOG_RANGE;
+    const float ex = 1.0f - (float)I.vhs_o;
+    NtcResult R;
+    R.perf = 0;
+    R.eqw = 0;
+    R.nsp1 = 0;
+    R.nsp2 = 0;
+    for (int32_t j0 = 0; j0 < ncoll;) {
+        const int32_t j = j0 + gl;
+        const bool valid = j < ncoll;
+        const int nvalid = min(G, ncoll - j0);
+        Stream st;
+        st.init(seed, TAG_CAND, pc, stp, rid, (uint32_t)j);
+        // the candidate's first six draws: i, k, then (k redrawn while equal
+        // to i) the acceptance draw and the two scattering draws
+        uint64_t D[6];
+        st.block_bits(0, D[0], D[1]);
+        st.block_bits(1, D[2], D[3]);
+        st.block_bits(2, D[4], D[5]);
+        auto draw = [&](int n) -> uint64_t {
+            uint64_t r = 0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+                if (q == n) r = D[q];
+            if (n >= 6) {
+                uint64_t x0, x1;
+                st.block_bits((uint32_t)n >> 1, x0, x1);
+                r = (n & 1) ? x1 : x0;
+            }
+            return r;
+        };
+        const int32_t nl = p.n1 + p.n2;
+        const int32_t st2 = p.n2 > 0 ? p.start2 : b1;  // group 2 once a split exists
+        const float l_smax = log2_pos(smax);
+        const bool screen_b = screen && fabsf(l_smax) < 2.0f * LOG_RANGE;
+        // per version: indices and slots (integer work only), then all the
+        // versions' particle loads in flight together
+        int32_t vi[V], vk[V], vsi[V], vsk[V], vnx[V];
+        bool vfresh[V];
+        // floor(U * n) for n = nl, nl + 1, ...: the exact products U 2^64 n
+        // (128 bits) step by U 2^64 from one count to the next
+        const uint64_t ai = D[0] & ~0xFFFull, ak = D[1] & ~0xFFFull;  // U * 2^64
+        uint64_t ihi = __umul64hi(ai, (uint64_t)nl), ilo = ai * (uint64_t)nl;
+        uint64_t khi = __umul64hi(ak, (uint64_t)nl), klo = ak * (uint64_t)nl;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int32_t n = nl + v;
+            if (v > 0) {
+                ilo += ai;
+                ihi += ilo < ai;
+                klo += ak;
+                khi += klo < ak;
+            }
+            int32_t i = -1, k = -2, nx = 2;
+            if (valid) {
+                // the FP64 product's rounding can only matter within half an
+                // ulp of the next integer (floor_u52_times)
+                i = ilo >= 0xFFFFFE0000000000ull ? floor_u52_times(D[0] >> 12, n) : (int32_t)ihi;
+                k = klo >= 0xFFFFFE0000000000ull ? floor_u52_times(D[1] >> 12, n) : (int32_t)khi;
+                int guard = 0;
+                while (i == k && guard++ < (1 << 20)) k = floor_u52_times(draw(nx++) >> 12, n);
+            }
+            vi[v] = i;
+            vk[v] = k;
+            vnx[v] = nx;
+            // a particle split off in this batch (index >= nl) is not written yet
+            vfresh[v] = valid && (i >= nl || k >= nl);
+            vsi[v] = i < p.n1 ? p.start1 + i : st2 + (i - p.n1);
+            vsk[v] = k < p.n1 ? p.start1 + k : st2 + (k - p.n1);
+        }
+        PV va[V], vb[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            if (valid && !vfresh[v]) {
+                va[v] = P.wv[vsi[v]];
+                vb[v] = P.wv[vsk[v]];
+            } else {
+                va[v] = PV{1.0, 0.0, 0.0, 0.0};
+                vb[v] = va[v];
+            }
+        }
+        // the scattering terms that depend on the draws alone, for the usual
+        // draw positions (no redraw of k): they overlap the loads here instead
+        // of lengthening the collision's dependent chain
+        double sphi0, cphi0;
+        sincos_2pi_u52(d.trig, D[3] >> 12, sphi0, cphi0);
+        const double ct0 = fma(2.0, u52_to_double(D[4] >> 12), -1.0);
+        const double sth0 = sqrt(1.0 - ct0 * ct0);
+        // g^2, weights, screened and exact sigma g w per version
+        bool vhas[V], vexact[V], veqw[V];
+        double vg2[V], vsgw[V];
+        float vls[V];
+        double g0 = 0.0;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const PV& a = va[v];
+            const PV& b = vb[v];
+            const double gx = a.vx - b.vx, gy = a.vy - b.vy, gz = a.vz - b.vz;
+            const double g2 = (gx * gx + gy * gy) + gz * gz;
+            const double wm = dmax_pos(a.w, b.w);
+            double sgw = -1.0;
+            bool has = false, exact = false, have_g = false;
+            double g = 0.0;
+            float ls = 0.0f;
+            if (valid && !vfresh[v]) {
+                if ((uint64_t)__double_as_longlong(g2) > G2_TINY_BITS) {
+                    has = true;
+                } else {
+                    g = sqrt(g2);
+                    have_g = true;
+                    has = g > EPS;
+                }
+                if (has) {
+                    const float lw = log2_pos(wm), lg = log2_pos(g2);
+                    ls = lC + lw + ex * lg;
+                    exact = !screen_b || fabsf(lw) >= LOG_RANGE || fabsf(lg) >= LOG_RANGE ||
+                            ls > l_smax - SCREEN_MARGIN;
+                    if (exact) {
+                        if (!have_g) g = sqrt(g2);
+                        sgw = I.vhs_factor * pow(g, vexp) * g * wm;
+                    }
+                }
+            }
+            if (v == 0) g0 = sqrt(g2);
+            veqw[v] = fabs(a.w - b.w) < dw_tol;  // an accepted collision without a split
+            vg2[v] = g2;
+            vsgw[v] = sgw;
+            vhas[v] = has;
+            vexact[v] = exact;
+            vls[v] = ls;
+        }
+        // resolution in candidate order, one segment per version
+        int s = 0, start = 0, end = -1;
+        long long mrun = __double_as_longlong(smax);
+        unsigned accm = 0u, splm = 0u;
+        int myv = 0;
+        bool myacc = false;
+        int32_t ci = -1, ck = -1;  // this lane's particles once it is an accepted candidate
+        while (end < 0) {
+            int32_t i = 0, k = 0, nx = 2;
+            bool fresh = false, has = false, exact = false, eqw = false;
+            double g2 = 0.0, wm = 0.0, sgw = -1.0;
+            float ls = 0.0f;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                if (v == s) {
+                    i = vi[v];
+                    k = vk[v];
+                    nx = vnx[v];
+                    fresh = vfresh[v];
+                    has = vhas[v];
+                    exact = vexact[v];
+                    eqw = veqw[v];
+                    g2 = vg2[v];
+                    wm = dmax_pos(va[v].w, vb[v].w);
+                    sgw = vsgw[v];
+                    ls = vls[v];
+                }
+            const bool live = valid && gl >= start;
+            // particles changed by accepted candidates of earlier segments
+            bool conf = live && fresh;
+            for (unsigned q = accm; q; q &= q - 1) {
+                const int a = __ffs(q) - 1;
+                const int32_t ta = grp.shfl(ci, a), tb = grp.shfl(ck, a);
+                conf |= live && (i == ta || i == tb || k == ta || k == tb);
+            }
+            // running (sigma g w)_max (collision_ntc.jl:229) through this lane:
+            // only exact values can raise it (screened ones lie below the
+            // batch's starting maximum), so the scan visits those lanes only
+            const long long key_me = max_key(sgw, live && has && exact);
+            long long mk = mrun;
+            for (unsigned q = grp.ballot(key_me >= 0); q; q &= q - 1) {
+                const int e = __ffs(q) - 1;
+                const long long ke = grp.shfl(key_me, e);
+                if (gl >= e) mk = max(mk, ke);
+            }
+            const double m = __longlong_as_double(mk);
+            // rand() < sigma_g_w / (sigma g w)_max (collision_ntc.jl:231)
+            bool acc = false;
+            if (live && has && !fresh) {
+                const uint64_t um = draw(nx) >> 12;
+                if (exact) {
+                    acc = u52_to_double(um) < sgw / m;
+                } else {
+                    const float lm = log2_pos(m);
+                    const float dl = ls - lm - log2_u52(um);
+                    if (dl > SCREEN_MARGIN && fabsf(lm) < 2.0f * LOG_RANGE) {
+                        acc = true;
+                    } else if (dl >= -SCREEN_MARGIN || fabsf(lm) >= 2.0f * LOG_RANGE) {
+                        const double g = sqrt(g2);
+                        const double se = I.vhs_factor * pow(g, vexp) * g * wm;
+                        acc = u52_to_double(um) < se / m;
+                    }
+                }
+            }
+            const bool spl = acc && !eqw;
+            // particles changed by earlier accepted candidates of this segment
+            const unsigned am = grp.ballot(acc);
+            for (unsigned q = am; q; q &= q - 1) {
+                const int a = __ffs(q) - 1;
+                const int32_t ta = grp.shfl(i, a), tb = grp.shfl(k, a);
+                if (gl > a) conf |= live && (i == ta || i == tb || k == ta || k == tb);
+            }
+            const unsigned cm = grp.ballot(conf), sm = grp.ballot(spl);
+            const int fc = cm ? __ffs(cm) - 1 : G;
+            const int fs = sm ? __ffs(sm) - 1 : G;
+            const bool stop = fc <= fs;
+            const int last = stop ? min(fc, nvalid) - 1 : fs;  // last lane of this segment
+            if (last >= start) {
+                const unsigned rng = (last - start + 1 >= 32 ? 0xFFFFFFFFu : ((1u << (last - start + 1)) - 1u)) << start;
+                if (gl >= start && gl <= last) {
+                    myv = s;
+                    myacc = acc;
+                    if (acc) {
+                        ci = i;
+                        ck = k;
+                    }
+                }
+                accm |= am & rng;
+                if (!stop) splm |= 1u << fs;
+                mrun = grp.shfl(mk, last);
+            }
+            if (stop) {
+                end = max(last + 1, start);
+            } else {
+                ++s;
+                start = fs + 1;
+                if (s == V || start >= nvalid) end = start;
+            }
+        }
+        // the batch's accepted candidates collide, on disjoint particles
+        const bool myspl = (splm >> gl) & 1u;
+        if (myacc) {
+            int32_t si = 0, sk = 0, nx = 2;
+            double g2 = 0.0;
+            PV a = va[0], b = vb[0];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                if (v == myv) {
+                    si = vsi[v];
+                    sk = vsk[v];
+                    nx = vnx[v];
+                    g2 = vg2[v];
+                    a = va[v];
+                    b = vb[v];
+                }
+            double wi = a.w, wk = b.w;  // weights after a split
+            const double g = myv == 0 ? g0 : sqrt(g2);
+            // compute_com! (collision_utils.jl:374-376)
+            const double cx = I.mu1 * a.vx + I.mu2 * b.vx;
+            const double cy = I.mu1 * a.vy + I.mu2 * b.vy;
+            const double cz = I.mu1 * a.vz + I.mu2 * b.vz;
+            if (myspl) {
+                // split the heavier particle; the new particle keeps the
+                // pre-collision velocity and position (collision_ntc.jl:235-267)
+                const bool heavy_i = a.w > b.w;
+                const int32_t src = heavy_i ? si : sk;
+                const PV& h = heavy_i ? a : b;
+                const double wl = heavy_i ? b.w : a.w;
+                const int32_t ns_ = b1 + R.nsp1 + __popc(splm & ((1u << gl) - 1u));
+                P.wv[ns_] = PV{h.w - wl, h.vx, h.vy, h.vz};
+                cell[ns_] = c;
+                key[ns_] = src;  // the position is copied after the loop
+                if (heavy_i)
+                    wi = wl;
+                else
+                    wk = wl;
+            }
+            // scatter_vhs! (collision_scattering.jl:17-29): phi = 2 pi rand(),
+            // cos(theta) = 2 rand() - 1
+            double sphi = sphi0, cphi = cphi0, ct = ct0, sth = sth0;
+            if (nx != 2) {
+                sincos_2pi_u52(d.trig, draw(nx + 1) >> 12, sphi, cphi);
+                ct = fma(2.0, u52_to_double(draw(nx + 2) >> 12), -1.0);
+                sth = sqrt(1.0 - ct * ct);
+            }
+            const double nxv = g * (sth * cphi), nyv = g * (sth * sphi), nzv = g * ct;
+            P.wv[si] = PV{wi, cx + I.mu2 * nxv, cy + I.mu2 * nyv, cz + I.mu2 * nzv};
+            P.wv[sk] = PV{wk, cx - I.mu1 * nxv, cy - I.mu1 * nyv, cz - I.mu1 * nzv};
+        }
+        const int nspl = __popc(splm);
+        R.perf += __popc(accm);
+        R.eqw += __popc(accm & ~splm);
+        if (nspl) {
+            if (p.n2 == 0) p.start2 = b1;
+            p.n2 += nspl;
+            R.nsp1 += nspl;
+        }
+        smax = __longlong_as_double(mrun);
+        grp.sync();
+        j0 += end;
+    }
+    // positions of the split-off particles: their parents', taken now.  A
+    // parent split off earlier in this call has no position yet; its key
+    // leads on to its own parent, and the first parent outside this call's
+    // splits holds the position of the whole line.
+    for (int32_t q = gl; q < R.nsp1; q += G) {
+        int32_t src = key[b1 + q];
+        for (int32_t h = 0; src >= b1 && src < b1 + R.nsp1 && h < R.nsp1; ++h) src = key[src];
+        P.pos[b1 + q] = P.pos[src];
+    }
+    grp.sync();
+    for (int32_t q = gl; q < R.nsp1; q += G) key[b1 + q] = c;
+    grp.sync();
+    R.smax = smax;
+    return R;
+}
+
 // ------------------------------------------------------------------ props
 struct CellMoments {
     double n, ux, uy, uz, T;

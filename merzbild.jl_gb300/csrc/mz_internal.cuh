@@ -101,6 +101,15 @@ struct Stream {
         const uint32_t lo = e ? buf[2] : buf[0], hi = e ? buf[3] : buf[1];
         return (uint64_t)lo | ((uint64_t)hi << 32);
     }
+    // draws 2 bk and 2 bk + 1 of the stream (bits() of those positions),
+    // without touching the stream's position
+    __host__ __device__ inline void block_bits(uint32_t bk, uint64_t& d0, uint64_t& d1) const
+    {
+        uint32_t c0 = bk, c1 = a, c2 = b, cc3 = c3;
+        philox4x32_10(c0, c1, c2, cc3, k0, k1);
+        d0 = (uint64_t)c0 | ((uint64_t)c1 << 32);
+        d1 = (uint64_t)c2 | ((uint64_t)cc3 << 32);
+    }
     // the 52-bit integer m of the next uniform U = m * 2^-52
     __host__ __device__ inline uint64_t u52() { return bits() >> 12; }
     // uniform in [0, 1), multiples of 2^-52: [1, 2) - 1 like Julia's rand(Float64)

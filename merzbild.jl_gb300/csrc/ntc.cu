@@ -69,9 +69,15 @@ __global__ void __launch_bounds__(256) k_ntc(DomainView d, int s1, int s2, uint3
         Indexer p2 = single ? p1 : S2.ind[c];
         const int32_t b1 = EQW ? 0 : base1[c];
         const int32_t b2 = EQW ? 0 : (single ? 0 : base2[c]);
-        const NtcResult R = ntc_cell<EQW, G>(d, I, single, c, ncoll, cfp->smax, S1.A, S2.A, p1, p2, S1.cell,
-                                             S1.key, S2.cell, S2.key, b1, b2, dw_tol, cell_seed(d, c), pc,
-                                             cell_step(d, c, step), cell_rid(d, c));
+        const NtcResult R =
+            (!EQW && single)
+                ? ntc_cell_split<G, NTC_SPLIT_VERSIONS>(d, I, c, ncoll, cfp->smax, S1.A, p1, S1.cell, S1.key, b1,
+                                                        dw_tol, cell_seed(d, c), pc, cell_step(d, c, step),
+                                                        cell_rid(d, c))
+                : ntc_cell<EQW, G>(d, I, single, c, ncoll, cfp->smax, S1.A, S2.A, p1, p2, S1.cell, S1.key, S2.cell,
+                                   S2.key, b1, b2, dw_tol, cell_seed(d, c), pc, cell_step(d, c, step),
+                                   cell_rid(d, c));
+        if (!EQW && single) p2 = p1;
         if (grp.rank == 0) {
             cfp->smax = R.smax;
             cfp->n_coll_performed = R.perf;

@@ -729,11 +729,10 @@ __global__ void __launch_bounds__(256) k_vw_ntc(DomainView d, int s, double dw_t
         const int32_t ncoll = cfp->n_coll;
         if (ncoll <= 0) continue;
         Indexer p1 = S.ind[c];
-        Indexer p2 = p1;
         const int32_t b1 = base[c];
-        const NtcResult R = ntc_cell<false, G>(d, I, true, c, ncoll, cfp->smax, S.A, S.A, p1, p2, S.cell, S.key,
-                                               S.cell, S.key, b1, 0, dw_tol, cell_seed(d, c), pc,
-                                               cell_step(d, c, step), cell_rid(d, c));
+        const NtcResult R = ntc_cell_split<G, NTC_SPLIT_VERSIONS>(d, I, c, ncoll, cfp->smax, S.A, p1, S.cell, S.key,
+                                                                  b1, dw_tol, cell_seed(d, c), pc,
+                                                                  cell_step(d, c, step), cell_rid(d, c));
         if (grp.rank == 0) {
             cfp->smax = R.smax;
             cfp->n_coll_performed = R.perf;
