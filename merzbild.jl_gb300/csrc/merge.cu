@@ -67,6 +67,7 @@ struct MergeArgs {
     const uint32_t* step_ptr;
     const int* abort;
     int32_t nmax;
+    int32_t min_n;  // warp kernel: cells of at most min_n particles are left to the block kernel
 };
 
 __device__ __forceinline__ double warp_min(double v)
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
                 if (q >= a.ce) break;
                 const Indexer p = d.sp[a.s].ind[q];
                 const int n = p.n1 + p.n2;
-                if (n > 0 && (a.threshold < 0 || n > a.threshold)) {
+                if (n > a.min_n && (a.threshold < 0 || n > a.threshold)) {
                     if (n > a.nmax) {  // larger than the scratch slices: leave the cell
                         set_status(d, ST_CAPACITY);
                         continue;
@@ -541,6 +542,482 @@ __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
         if (c >= a.ce) break;
         merge_cell(d, a, c, base);
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- block form
+// A cell of up to MB_N particles (target at most MB_BINS) merges in one block
+// of MB_THREADS threads with its particles, lists and bins in shared memory:
+// the particles are staged once in logical order (cv), the octree is built by
+// the first warp exactly as merge_cell builds it (indices into cv instead of
+// slots), and the parallel parts -- staging, bounds, the list-order copy, the
+// bin moments (one thread per bin, the wide bins one warp each) and the write-
+// back -- use every warp.  Same arithmetic in the same order as merge_cell.
+constexpr int MB_THREADS = 256, MB_N = 1536, MB_BINS = 384;
+constexpr size_t MB_OFF_PIS = (size_t)MB_BINS * sizeof(MergeBin);
+constexpr size_t MB_OFF_CV = MB_OFF_PIS + (size_t)MB_N * sizeof(int32_t);
+constexpr size_t MB_OFF_LV = MB_OFF_CV + (size_t)MB_N * sizeof(PV);
+constexpr size_t MB_OFF_R = MB_OFF_LV + (size_t)MB_N * sizeof(PV);  // lx; during the octree tmp, wl, tw, oct
+constexpr size_t MB_OFF_OV = MB_OFF_R + (size_t)MB_N * sizeof(PX);
+constexpr size_t MB_OFF_OX = MB_OFF_OV + (size_t)MB_BINS * sizeof(PV);
+constexpr size_t MB_SMEM = MB_OFF_OX + (size_t)MB_BINS * sizeof(PX);
+static_assert((size_t)MB_N * (sizeof(int32_t) + 2 * sizeof(double) + 1) <= (size_t)MB_N * sizeof(PX),
+              "octree scratch must fit the position region");
+
+// compute_octant through integer keys: for doubles that are not NaN, x > m
+// exactly when key(x) > key(m) as signed integers (-0.0 taken as +0.0), and
+// integer compares keep the FP64 pipe free
+__device__ __forceinline__ long long order_key(double x)
+{
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ __forceinline__ int octant_of_keys(const PV& v, const long long* km)
+{
+    return (order_key(v.vx) > km[0] ? 1 : 0) + (order_key(v.vy) > km[1] ? 2 : 0) + (order_key(v.vz) > km[2] ? 4 : 0);
+}
+
+__device__ __forceinline__ void bounds_of_list(const PV* cv, const int32_t* pis, int bs, int be, double* mn,
+                                               double* mx)
+{
+    const int lane = threadIdx.x & 31;
+    double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
+    double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
+    for (int i = bs + lane; i <= be; i += 32) {
+        const PV v = cv[pis[i]];
+        lo[0] = fmin(lo[0], v.vx);
+        lo[1] = fmin(lo[1], v.vy);
+        lo[2] = fmin(lo[2], v.vz);
+        hi[0] = fmax(hi[0], v.vx);
+        hi[1] = fmax(hi[1], v.vy);
+        hi[2] = fmax(hi[2], v.vz);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        mn[c] = warp_min(lo[c]);
+        mx[c] = warp_max(hi[c]);
+    }
+}
+
+__device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c, char* smem)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = MB_THREADS / 32;
+    const SpeciesView& S = d.sp[a.s];
+    const Cols& A = S.A;
+    MergeBin* bins = reinterpret_cast<MergeBin*>(smem);
+    int32_t* pis = reinterpret_cast<int32_t*>(smem + MB_OFF_PIS);
+    PV* cv = reinterpret_cast<PV*>(smem + MB_OFF_CV);
+    PV* lv = reinterpret_cast<PV*>(smem + MB_OFF_LV);
+    PX* lx = reinterpret_cast<PX*>(smem + MB_OFF_R);
+    int32_t* tmp = reinterpret_cast<int32_t*>(smem + MB_OFF_R);
+    double* wl = reinterpret_cast<double*>(smem + MB_OFF_R + (size_t)MB_N * sizeof(int32_t));
+    double* tw = wl + MB_N;
+    uint8_t* oct = reinterpret_cast<uint8_t*>(tw + MB_N);
+    PV* ov = reinterpret_cast<PV*>(smem + MB_OFF_OV);
+    PX* ox = reinterpret_cast<PX*>(smem + MB_OFF_OX);
+    __shared__ double s_red[NW][6];
+    __shared__ int s_nbins;
+    __shared__ int s_pos[MB_BINS], s_kbig[MB_BINS];
+    __shared__ int s_scan[NW][2];
+    const Indexer p = S.ind[c];
+    const int n = p.n1 + p.n2;
+
+    // init_octree! (:947-984): the cell's particles in logical order
+    for (int i = tid; i < n; i += MB_THREADS) {
+        cv[i] = A.wv[map_slot(p, i)];
+        pis[i] = i;
+    }
+    __syncthreads();
+    double mn[3], mx[3];
+    if (a.prm.init_bin_bounds == INIT_C) {
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = -299792458.0;
+            mx[k] = 299792458.0;
+        }
+    } else {
+        double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
+        double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
+        for (int i = tid; i < n; i += MB_THREADS) {
+            const PV v = cv[i];
+            lo[0] = fmin(lo[0], v.vx);
+            lo[1] = fmin(lo[1], v.vy);
+            lo[2] = fmin(lo[2], v.vz);
+            hi[0] = fmax(hi[0], v.vx);
+            hi[1] = fmax(hi[1], v.vy);
+            hi[2] = fmax(hi[2], v.vz);
+        }
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = warp_min(lo[k]);
+            hi[k] = warp_max(hi[k]);
+        }
+        if (lane == 0)
+            for (int k = 0; k < 3; ++k) {
+                s_red[warp][k] = lo[k];
+                s_red[warp][3 + k] = hi[k];
+            }
+        __syncthreads();
+        for (int k = 0; k < 3; ++k) {
+            double l = s_red[0][k], h = s_red[0][3 + k];
+            for (int w = 1; w < NW; ++w) {
+                l = fmin(l, s_red[w][k]);
+                h = fmax(h, s_red[w][3 + k]);
+            }
+            mn[k] = l;
+            mx[k] = h;
+        }
+        if (a.prm.init_bin_bounds == INIT_MINMAX_SYM)
+            for (int k = 0; k < 3; ++k) {
+                const double m = fmax(fabs(mn[k]), fabs(mx[k]));
+                mn[k] = -m;
+                mx[k] = m;
+            }
+    }
+
+    // compute_octree! (:998-1039) by the first warp
+    if (warp == 0) {
+        if (lane == 0) {
+            MergeBin b;
+            b.w = 1e50;
+            for (int k = 0; k < 3; ++k) {
+                b.vmin[k] = mn[k];
+                b.vmax[k] = mx[k];
+            }
+            b.np = n;
+            b.start = 0;
+            b.end = n - 1;
+            b.depth = 0;
+            b.refinable = (n > 2) && (a.prm.max_depth > 0);
+            b.pad = 0;
+            bins[0] = b;
+        }
+        int nbins = 1;
+        int total = n >= 2 ? 2 : n;  // total_post_merge_np
+        __syncwarp();
+        for (;;) {
+            double bw = -1.0;
+            int bid = -1;
+            for (int b = lane; b < nbins; b += 32) {
+                const MergeBin& B = bins[b];
+                if (B.refinable && B.w > bw) {
+                    bw = B.w;
+                    bid = b;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
+                const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+                if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
+                    bw = w2;
+                    bid = id2;
+                }
+            }
+            if (bid < 0) break;
+            if (total + 14 > a.target) break;
+
+            // split_bin! (:503-633)
+            const MergeBin P = bins[bid];
+            const int bs = P.start, be = P.end, nb = be - bs + 1;
+            double vmin[3], vmax[3];
+            for (int k = 0; k < 3; ++k) {
+                vmin[k] = P.vmin[k];
+                vmax[k] = P.vmax[k];
+            }
+            if (a.prm.bin_bounds_compute == BOUNDS_RECOMPUTE) bounds_of_list(cv, pis, bs, be, vmin, vmax);
+            double mid[3];
+            long long kmid[3];
+            for (int k = 0; k < 3; ++k) {
+                mid[k] = 0.5 * (vmin[k] + vmax[k]);
+                kmid[k] = order_key(mid[k]);
+            }
+            int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int i = lane; i < nb; i += 32) {
+                const PV v = cv[pis[bs + i]];
+                const int o = octant_of_keys(v, kmid);
+                oct[i] = (uint8_t)o;
+                wl[i] = v.w;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) cnt[k] += (o == k);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cnt[k] = __reduce_add_sync(0xFFFFFFFFu, cnt[k]);
+            __syncwarp();
+            int incl[8], run = 0;
+            int nne = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                run += cnt[k];
+                incl[k] = run;
+                nne += cnt[k] > 0;
+            }
+            int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int i0 = 0; i0 < nb; i0 += 32) {
+                const int i = i0 + lane;
+                const bool in = i < nb;
+                const int o = in ? oct[i] : 8;
+                const unsigned peers = __match_any_sync(0xFFFFFFFFu, o);
+                int r = __popc(peers & lanemask_lt()), end_o = 0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (o == k) {
+                        r += seen[k];
+                        end_o = incl[k];
+                    }
+                if (in) {
+                    tmp[end_o - 1 - r] = pis[bs + i];
+                    tw[end_o - 1 - r] = wl[i];
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
+            }
+            __syncwarp();
+            double wo = 0.0;
+            {
+                int lo = 0, hi = 0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (lane == k) {
+                        lo = incl[k] - cnt[k];
+                        hi = incl[k];
+                    }
+                for (int j = hi - 1; j >= lo; --j) wo += tw[j];
+            }
+            {
+                int kch = 0, startk = bs;
+                for (int k = 0; k < 8; ++k) {
+                    if (cnt[k] == 0) continue;
+                    const int id = kch == 0 ? bid : nbins + kch - 1;
+                    const double wk = __shfl_sync(0xFFFFFFFFu, wo, k);
+                    if (lane == 0) {
+                        MergeBin b;
+                        for (int q = 0; q < 3; ++q) {
+                            const bool upper = (k >> q) & 1;
+                            if (a.prm.bin_bounds_compute == BOUNDS_INHERIT) {
+                                b.vmin[q] = upper ? mid[q] : P.vmin[q];
+                                b.vmax[q] = upper ? P.vmax[q] : mid[q];
+                            } else {
+                                b.vmin[q] = P.vmin[q];
+                                b.vmax[q] = P.vmax[q];
+                            }
+                        }
+                        b.np = cnt[k];
+                        b.w = wk;
+                        b.depth = P.depth + 1;
+                        b.start = startk;
+                        b.end = startk + cnt[k] - 1;
+                        b.refinable = (cnt[k] > 2) && (b.depth < a.prm.max_depth);
+                        b.pad = 0;
+                        bins[id] = b;
+                    }
+                    total += cnt[k] >= 2 ? 2 : cnt[k];
+                    startk += cnt[k];
+                    ++kch;
+                }
+                total -= 2;
+            }
+            __syncwarp();
+            for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
+            nbins += nne - 1;
+            __syncwarp();
+            if (nbins + 7 > a.prm.max_Nbins) break;
+        }
+        if (lane == 0) s_nbins = nbins;
+    }
+    __syncthreads();
+    const int nbins = s_nbins;
+    // the particles in list order (the octree scratch is dead: lx takes it)
+    for (int i = tid; i < n; i += MB_THREADS) {
+        const int q = pis[i];
+        lv[i] = cv[q];
+        lx[i] = A.pos[map_slot(p, q)];
+    }
+    __syncthreads();
+    if (nbins == 1 && tid == 0) {
+        double w = 0.0;
+        for (int i = 0; i < n; ++i) w += lv[i].w;
+        bins[0].w = w;
+    }
+    __syncthreads();
+
+    // output position and rank among the bins of more than two particles of
+    // every bin, in bin order: an exclusive scan over the bins (two per thread)
+    int io[2] = {0, 0}, ib[2] = {0, 0};
+    for (int q = 0; q < 2; ++q) {
+        const int b = 2 * tid + q;
+        if (b < nbins) {
+            const MergeBin& B = bins[b];
+            const int npe = B.w == 0.0 ? 0 : B.np;
+            io[q] = npe >= 2 ? 2 : npe;
+            ib[q] = npe > 2 ? 1 : 0;
+        }
+    }
+    int so = io[0] + io[1], sb = ib[0] + ib[1];
+    int xo = so, xb = sb;  // inclusive within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t1 = __shfl_up_sync(0xFFFFFFFFu, xo, o), t2 = __shfl_up_sync(0xFFFFFFFFu, xb, o);
+        if (lane >= o) {
+            xo += t1;
+            xb += t2;
+        }
+    }
+    if (lane == 31) {
+        s_scan[warp][0] = xo;
+        s_scan[warp][1] = xb;
+    }
+    __syncthreads();
+    int wo0 = 0, wb0 = 0, tot_o = 0;
+    for (int w = 0; w < NW; ++w) {
+        if (w < warp) {
+            wo0 += s_scan[w][0];
+            wb0 += s_scan[w][1];
+        }
+        tot_o += s_scan[w][0];
+    }
+    {
+        int po = wo0 + xo - so, pb = wb0 + xb - sb;
+        for (int q = 0; q < 2; ++q) {
+            const int b = 2 * tid + q;
+            if (b < nbins) {
+                s_pos[b] = po;
+                s_kbig[b] = pb;
+            }
+            po += io[q];
+            pb += ib[q];
+        }
+    }
+    __syncthreads();
+
+    // the bins a thread sums alone, largest first: a warp's FP64 work is set
+    // by its largest bin, so bins of like size share a warp (counting sort by
+    // particle count, descending; s_order reuses the scan's word arrays)
+    __shared__ int s_hist[WIDE_BIN + 2];
+    __shared__ int s_order[MB_BINS];
+    for (int k = tid; k < WIDE_BIN + 2; k += MB_THREADS) s_hist[k] = 0;
+    __syncthreads();
+    for (int b = tid; b < nbins; b += MB_THREADS) {
+        const MergeBin& B = bins[b];
+        const int npe = B.w == 0.0 ? 0 : B.np;
+        atomicAdd(&s_hist[npe > WIDE_BIN ? WIDE_BIN + 1 : npe], 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int run = 0;
+        for (int k = WIDE_BIN + 1; k >= 0; --k) {
+            const int t = s_hist[k];
+            s_hist[k] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+    for (int b = tid; b < nbins; b += MB_THREADS) {
+        const MergeBin& B = bins[b];
+        const int npe = B.w == 0.0 ? 0 : B.np;
+        s_order[atomicAdd(&s_hist[npe > WIDE_BIN ? WIDE_BIN + 1 : npe], 1)] = b;
+    }
+    __syncthreads();
+
+    // compute_bin_props! (:646-700) and compute_new_particles! (:736-933)
+    Stream st;
+    st.init(cell_seed(d, c), TAG_MERGE, (uint32_t)a.s, cell_step(d, c, a.step), cell_rid(d, c), 0);
+    for (int r = tid; r < nbins; r += MB_THREADS) {
+        const int b = s_order[r];
+        const MergeBin B = bins[b];
+        const int npe = B.w == 0.0 ? 0 : B.np;
+        const int pos = s_pos[b];
+        if (npe > 2 && npe <= WIDE_BIN) {
+            double vm[3], xm[3], sv[3], sx[3];
+            bin_moments_lane(lv, lx, B.start, B.end, 1.0 / B.w, vm, xm, sv, sx);
+            emit_pair(a, st, s_kbig[b], B.w, vm, xm, sv, sx, ov + pos, ox + pos);
+        } else if (npe >= 1 && npe <= 2) {
+            for (int q = 0; q < npe; ++q) {
+                ov[pos + q] = lv[B.start + q];
+                ox[pos + q] = lx[B.start + q];
+            }
+        }
+    }
+    // bins of many particles: one warp each
+    for (int b0 = 0; b0 < nbins; b0 += 32) {
+        const int b = b0 + lane;
+        bool wide = false;
+        if (b < nbins) {
+            const MergeBin& B = bins[b];
+            wide = B.w != 0.0 && B.np > WIDE_BIN;
+        }
+        unsigned wmask = __ballot_sync(0xFFFFFFFFu, wide);
+        for (int r = 0; wmask; ++r) {
+            const int q = __ffs(wmask) - 1;
+            wmask &= wmask - 1;
+            if (r % NW != warp) continue;
+            const MergeBin B = bins[b0 + q];
+            double vm[3], xm[3], sv[3], sx[3];
+            bin_moments_warp(lv, lx, B.start, B.end, 1.0 / B.w, vm, xm, sv, sx);
+            if (lane == 0) {
+                const int pos = s_pos[b0 + q];
+                emit_pair(a, st, s_kbig[b0 + q], B.w, vm, xm, sv, sx, ov + pos, ox + pos);
+            }
+        }
+    }
+    __syncthreads();
+    const int cur = tot_o;
+    for (int j = tid; j < cur; j += MB_THREADS) {
+        const int32_t slot = map_slot(p, j);
+        A.wv[slot] = ov[j];
+        A.pos[slot] = ox[j];
+    }
+    for (int j = cur + tid; j < n; j += MB_THREADS) {
+        const int32_t slot = map_slot(p, j);
+        A.wv[slot].w = 0.0;
+        S.cell[slot] = -1;
+    }
+    if (tid == 0) {
+        Indexer q = p;
+        if (cur <= p.n1) {
+            q.n1 = cur;
+            q.n2 = 0;
+            q.start2 = 0;
+            if (cur == 0) q.start1 = 0;
+        } else {
+            q.n2 = cur - p.n1;
+        }
+        S.ind[c] = q;
+        if (n > cur) atomicAdd((unsigned long long*)a.deleted, (unsigned long long)(n - cur));
+        atomicAdd((unsigned long long*)a.merged, 1ull);
+        atomicAdd(&d.counters->merges, 1ull);
+    }
+}
+
+// Blocks take the next cell of up to MB_N particles from their own counter;
+// larger cells are left to k_merge.
+__global__ void __launch_bounds__(MB_THREADS, 1) k_merge_block(DomainView d, MergeArgs a, unsigned int* next)
+{
+    if (a.abort && *a.abort) return;
+    if (a.step_ptr) a.step = *a.step_ptr;
+    extern __shared__ __align__(16) char mb_smem[];
+    __shared__ int s_cell;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int c = a.ce;
+            for (;;) {
+                const int q = a.cb + (int)atomicAdd(next, 1u);
+                if (q >= a.ce) break;
+                const Indexer p = d.sp[a.s].ind[q];
+                const int n = p.n1 + p.n2;
+                if (n > 0 && n <= MB_N && (a.threshold < 0 || n > a.threshold)) {
+                    c = q;
+                    break;
+                }
+            }
+            s_cell = c;
+        }
+        __syncthreads();
+        const int c = s_cell;
+        __syncthreads();
+        if (c >= a.ce) break;
+        merge_cell_block(d, a, c, mb_smem);
+        __syncthreads();
     }
 }
 
@@ -615,6 +1092,28 @@ void ensure_merge_scratch(mz_domain* d, size_t need)
 
 }  // namespace
 
+namespace {
+// the block form takes the cells it can hold when the target fits its bins
+bool merge_block_usable(int64_t target) { return target <= MB_BINS; }
+
+// blocks of the block form that fit the GPU at once; the first call on a
+// device (made before any stream capture: merge_fused_reserve, launch_merge)
+// raises the kernel's shared-memory limit
+int merge_block_grid(mz_domain* d)
+{
+    static int grid[64] = {0};
+    const int dev = d->ctx->device;
+    if (dev >= 0 && dev < 64 && grid[dev] > 0) return grid[dev];
+    MZ_CK(cudaFuncSetAttribute(k_merge_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MB_SMEM));
+    int per_sm = 0;
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge_block, MB_THREADS, MB_SMEM));
+    MZ_REQUIRE(per_sm >= 1, "merge: the block form does not fit on an SM");
+    const int g = d->ctx->num_sms * per_sm;
+    if (dev >= 0 && dev < 64) grid[dev] = g;
+    return g;
+}
+}  // namespace
+
 int merge_fused_warps(mz_domain* d) { return d->ctx->num_sms * 2; }
 
 void merge_fused_reserve(mz_domain* d, int64_t nmax, int64_t target, const mz_octree_params* prm)
@@ -624,7 +1123,9 @@ void merge_fused_reserve(mz_domain* d, int64_t nmax, int64_t target, const mz_oc
     memset(&a, 0, sizeof a);
     merge_layout(a, nmax, target, prm->max_Nbins);
     ensure_merge_scratch(d, (size_t)merge_fused_warps(d) * a.stride);
+    if (merge_block_usable(target)) merge_block_grid(d);
 }
+
 
 void launch_merge_fused(mz_domain* d, int s, int64_t threshold, int64_t target, const mz_octree_params* prm,
                         const mz_grid1d* g, const uint32_t* step_ptr, const int* abort, int64_t nmax,
@@ -654,7 +1155,13 @@ void launch_merge_fused(mz_domain* d, int s, int64_t threshold, int64_t target, 
     a.step_ptr = step_ptr;
     a.abort = abort;
     DomainView v = make_view(d);
-    MZ_CK(cudaMemsetAsync(a.next, 0, sizeof(unsigned int), c->stream));
+    MZ_CK(cudaMemsetAsync(a.next, 0, 2 * sizeof(long long), c->stream));
+    if (merge_block_usable(target)) {
+        // cells of up to MB_N particles in the block form, the rest by warps
+        MZ_LAUNCH(c, "merge_block", k_merge_block, merge_block_grid(d), MB_THREADS, MB_SMEM, v, a,
+                  reinterpret_cast<unsigned int*>(words3 + 3));
+        a.min_n = MB_N;
+    }
     MZ_LAUNCH(c, "merge", k_merge, warps, 32, 0, v, a);
 }
 
@@ -699,8 +1206,17 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
     a.deleted = d->d_scalar + 2;
     a.merged = d->d_scalar + 3;
     a.next = reinterpret_cast<unsigned int*>(d->d_scalar + 8);
-    MZ_CK(cudaMemsetAsync(a.next, 0, sizeof(unsigned int), c->stream));
-    MZ_LAUNCH(c, "merge", k_merge, blocks, 32, 0, v, a);
+    MZ_CK(cudaMemsetAsync(d->d_scalar + 8, 0, 2 * sizeof(int64_t), c->stream));
+    bool warps_needed = true;
+    if (merge_block_usable(target)) {
+        // cells of up to MB_N particles in the block form, the rest by warps
+        const int bgrid = (int)std::min<int64_t>(ncells, (int64_t)merge_block_grid(d));
+        MZ_LAUNCH(c, "merge_block", k_merge_block, bgrid, MB_THREADS, MB_SMEM, v, a,
+                  reinterpret_cast<unsigned int*>(d->d_scalar + 9));
+        a.min_n = MB_N;
+        warps_needed = nmax > MB_N;
+    }
+    if (warps_needed) MZ_LAUNCH(c, "merge", k_merge, blocks, 32, 0, v, a);
     MZ_CK(cudaMemcpyAsync(d->h_scalar + 2, d->d_scalar + 2, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     MZ_CK(cudaStreamSynchronize(c->stream));
     SpeciesHost& S = d->sp[s];

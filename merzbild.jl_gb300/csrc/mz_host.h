@@ -88,7 +88,7 @@ struct VwSpecies {
     long long hw;        // slots in use at the start of a step (the live count after the last sort)
     long long hw_split;  // slots in use after this step's split reservations
     long long need;      // slots the abandoned step needed (VW_CAPACITY)
-    long long merge[3];  // merge kernel: particles deleted, cells merged, cell counter
+    long long merge[4];  // merge kernels: particles deleted, cells merged, cell counters of the warp and block forms
 };
 struct VwDev {
     VwSpecies sp[MZ_MAX_SPECIES];
@@ -218,7 +218,7 @@ void launch_merge(mz_domain* d, int s, int64_t cb, int64_t ce, int64_t threshold
                   const mz_octree_params* prm, const mz_grid1d* grid, uint64_t step, int64_t* n_merged);
 // merging inside the fused step: no host synchronisation; the step index and
 // an abort word come from device memory, scratch is reserved beforehand for
-// cells of up to nmax particles; words3 = {deleted, merged, cell counter}
+// cells of up to nmax particles; words3 = {deleted, merged, cell counters of the warp and block forms}
 int merge_fused_warps(mz_domain* d);
 void merge_fused_reserve(mz_domain* d, int64_t nmax, int64_t target, const mz_octree_params* prm);
 void launch_merge_fused(mz_domain* d, int s, int64_t threshold, int64_t target, const mz_octree_params* prm,
