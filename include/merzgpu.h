@@ -488,8 +488,9 @@ int mz_server_set_hbm_headroom(mz_server* server, int64_t bytes);
  * threshold (0-D) or, for 1-D, the launches value minus one (0 fused, 1 two
  * launches, 2 gathering and physics warps side by side).  A variable-weight plan
  * (equal_weight = 0) tries only the lanes per cell of its splitting NTC
- * (6 * trial_steps steps) and *big_cell_out receives 0.  No counterpart in
- * the reference. */
+ * (6 * trial_steps steps, without a graph), compares the splitting NTC's own
+ * launch times (the lanes change nothing else), and *big_cell_out receives 0.
+ * No counterpart in the reference. */
 int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
 
 /* ---------------------------------------------------------------- counters */

@@ -1269,6 +1269,20 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
         d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
         d->tuned_split = plan->dims == 0 ? 0 : k % nb;
     };
+    // a variable-weight plan's lanes change only its splitting NTC, while the
+    // merge's share of a step varies from step to step: its trials time the
+    // NTC launches alone (direct launches, each bracketed by events)
+    const bool kt_was = c->kernel_timing;
+    if (vw) {
+        p.use_graph = 0;
+        c->kernel_timing = true;
+    }
+    auto ntc_ms = [&]() {
+        c->resolve_timings();
+        for (const KernelTiming& t : c->timings)
+            if (t.name == "vw_ntc") return t.total_ms;
+        return 0.0;
+    };
     // two rounds, the second in reverse order, and a configuration's time is
     // the sum of its two: the step time drifts as the simulation evolves (the
     // collision-rate estimate adapts), and the reversal cancels a linear drift
@@ -1277,15 +1291,23 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
             const int k = round == 0 ? i : nconf - 1 - i;
             apply(k);
             p.step0 = step;
+            const double before = vw ? ntc_ms() : 0.0;
             MZ_CK(cudaEventRecord(e0, c->stream));
             launch_step(d, &p, trial_steps, nullptr, nullptr);
             MZ_CK(cudaEventRecord(e1, c->stream));
             MZ_CK(cudaEventSynchronize(e1));
             float ms = 0.0f;
             MZ_CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (vw) ms = (float)(ntc_ms() - before);
             step += (uint64_t)trial_steps;
             total[k] += ms;
         }
+    if (vw && !kt_was) {
+        // the trials' timings were the tuner's own
+        c->resolve_timings();
+        c->timings.clear();
+    }
+    c->kernel_timing = kt_was;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     apply((int)(std::min_element(total.begin(), total.end()) - total.begin()));
