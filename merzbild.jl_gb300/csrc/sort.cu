@@ -189,13 +189,17 @@ __global__ void k_scatter(DomainView d, int s, int64_t hw)
     }
 }
 
+constexpr size_t SORT_GATHER_SMEM = (size_t)8 * SORT_SMEM_KEYS * sizeof(int32_t);  // 64 KB per 256-thread block
+
 __global__ void __launch_bounds__(256) k_sort_gather(DomainView d, int s)
 {
+    extern __shared__ int32_t sortbuf[];  // SORT_SMEM_KEYS per warp
     const SpeciesView& S = d.sp[s];
     const int warps = (gridDim.x * blockDim.x) >> 5;
+    int32_t* mine = sortbuf + (size_t)(threadIdx.x >> 5) * SORT_SMEM_KEYS;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < d.n_cells; c += warps) {
         const Indexer p = S.ind[c];
-        sort_gather_segment(S, c, p.start1, p.n1);
+        sort_gather_segment(S, c, p.start1, p.n1, mine);
     }
 }
 
@@ -273,6 +277,16 @@ static int grid_for(mz_ctx* c, int64_t work, int threads, int per_sm = 8)
 void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index)
 {
     mz_ctx* c = d->ctx;
+    {
+        // the gather's per-warp sort buffers exceed the default shared-memory
+        // limit (never called under stream capture: the sort synchronises)
+        static bool raised[64] = {false};
+        if (c->device < 0 || c->device >= 64 || !raised[c->device]) {
+            MZ_CK(cudaFuncSetAttribute(k_sort_gather, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)SORT_GATHER_SMEM));
+            if (c->device >= 0 && c->device < 64) raised[c->device] = true;
+        }
+    }
     SpeciesHost& S = d->sp[s];
     DomainView v = make_view(d);
     const int64_t hw = S.hw;
@@ -289,7 +303,8 @@ void launch_sort(mz_domain* d, int s, const mz_grid1d* grid, int64_t* out_index)
     launch_scan_cells(d, S.counts, S.ind, S.fill, d->d_scalar, true, nullptr, 0, nullptr);
     if (hw > 0) {
         MZ_LAUNCH(c, "sort_scatter", k_scatter, grid_for(c, hw, 256), 256, 0, v, s, hw);
-        MZ_LAUNCH(c, "sort_gather", k_sort_gather, grid_for(c, d->n_cells * 32, 256, 16), 256, 0, v, s);
+        MZ_LAUNCH(c, "sort_gather", k_sort_gather, grid_for(c, d->n_cells * 32, 256, 16), 256, SORT_GATHER_SMEM, v,
+                  s);
     }
     MZ_CK(cudaMemcpyAsync(d->h_scalar, d->d_scalar, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     std::vector<int32_t> idx;

@@ -228,10 +228,25 @@ static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, in
     sort_gather_regs<32>(S, c, start, N, acc);
 }
 
+// Segments of 1,025 .. 2,048 particles in kernels with registers to spare
+// (BIG): 64 rows per lane, out of line like the 32-row form.
+static __device__ __noinline__ void sort_gather_regs_64(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
+                                                        Sums4& acc)
+{
+    sort_gather_regs<64>(S, c, start, N, acc);
+}
+
+// Other segments of more than 1,024 particles sort their source slots with
+// Batcher's network: in a per-warp shared-memory buffer of SORT_SMEM_KEYS
+// keys where the launch provides one, else in place in global memory.
+constexpr int SORT_SMEM_KEYS = 2048;
+
 // Sort the source slots of cell c's segment [start, start + N) and gather the
 // particles from buffer A into the same positions of buffer B (one warp).
 // Returns this lane's first-pass props sums of the gathered particles.
-__device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N)
+template <bool BIG = false>
+__device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
+                                                     int32_t* sortbuf = nullptr)
 {
     Sums4 acc{0.0, 0.0, 0.0, 0.0};
     if (N <= 0) return acc;
@@ -241,11 +256,18 @@ __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32
     else if (N <= 256) sort_gather_regs<8>(S, c, start, N, acc);
     else if (N <= 512) sort_gather_regs<16>(S, c, start, N, acc);
     else if (N <= 1024) sort_gather_regs_32(S, c, start, N, acc);
+    else if (BIG && N <= 2048) sort_gather_regs_64(S, c, start, N, acc);
     else {
-        warp_oddeven_sort(S.idx + start, N);
+        const bool shared = sortbuf && N <= SORT_SMEM_KEYS;
+        int32_t* keys = shared ? sortbuf : S.idx + start;
+        if (shared) {
+            for (int q = (threadIdx.x & 31); q < N; q += 32) sortbuf[q] = S.idx[start + q];
+            __syncwarp();
+        }
+        warp_oddeven_sort(keys, N);
         for (int q = (threadIdx.x & 31); q < N; q += 32) {
             const int64_t dst = (int64_t)start + q;
-            copy_particle(S.A, S.B, S.idx[dst], dst);
+            copy_particle(S.A, S.B, keys[q], dst);
             S.cellB[dst] = c;
             S.key[dst] = c;
             const PV r = S.B.wv[dst];
@@ -254,6 +276,7 @@ __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32
             acc.sy += r.vy * r.w;
             acc.sz += r.vz * r.w;
         }
+        __syncwarp();  // the buffer is reused by the warp's next segment
     }
     return acc;
 }

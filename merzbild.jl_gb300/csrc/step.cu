@@ -130,9 +130,9 @@ __device__ __forceinline__ void write_props(const StepArgs& a, int64_t ix, const
 // publish every gathered cell; MODE 2 warps take cells from their own
 // counter, wait for the cells' publication (acquire) and run NTC + convection
 // on the gathered buffer B.
-template <int G, int MODE, bool WS = false>
+template <int G, int MODE, bool WS = false, bool BIG = false>
 __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a, int32_t* cell_hist,
-                                          double2* stage = nullptr)
+                                          double2* stage = nullptr, int32_t* sortbuf = nullptr)
 {
     constexpr int CPW = 32 / G;
     const bool gather_on = MODE == 1 ? true : (MODE == 2 ? false : a.gather != 0);
@@ -180,7 +180,7 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                 for (int q = 0; q < nq; ++q) {
                     const Indexer p = S.ind[c0 + q];
                     const Sums4 t = (WS && MODE == 1) ? sort_gather_segment_staged(S, c0 + q, p.start1, p.n1, stage)
-                                                      : sort_gather_segment(S, c0 + q, p.start1, p.n1);
+                                                      : sort_gather_segment<BIG>(S, c0 + q, p.start1, p.n1, sortbuf);
                     if (props1) props_pass1_into_lane(t.n, t.sx, t.sy, t.sz, q, mn, msx, msy, msz);
                 }
                 __syncwarp();
@@ -390,6 +390,17 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
 __global__ void __launch_bounds__(256, 3) k_cell_gather(DomainView d, StepArgs a)
 {
     cell_body<32, 1>(d, a, nullptr);
+}
+
+// The same for the variable-weight step, whose cells often hold more than
+// 1,024 particles: two warps per block with registers for 64-row sorts
+// (segments up to 2,048) and a shared-memory buffer each for larger ones.
+constexpr int GB_THREADS = 64;
+constexpr size_t GB_SMEM = (size_t)(GB_THREADS / 32) * SORT_SMEM_KEYS * sizeof(int32_t);
+__global__ void __launch_bounds__(GB_THREADS) k_cell_gather_big(DomainView d, StepArgs a)
+{
+    extern __shared__ int32_t sortbuf[];
+    cell_body<32, 1, false, true>(d, a, nullptr, nullptr, sortbuf + (size_t)(threadIdx.x >> 5) * SORT_SMEM_KEYS);
 }
 
 template <int G>
@@ -1123,11 +1134,11 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
     const int ntc_threads = ntc_warps >= 8 * (int64_t)c->num_sms ? 256 : 32;
     const int nblocks = (int)std::max<int64_t>(
         1, std::min<int64_t>(div_up(ntc_warps * 32, ntc_threads), (int64_t)c->num_sms * 16 * (256 / ntc_threads)));
-    // the gather takes one cell per warp; with few cells, two-warp blocks
-    // spread them over every SM
-    const int gthreads = d->n_cells >= 8 * 3 * (int64_t)c->num_sms ? 256 : 64;
+    // the gather takes one cell per warp, in two-warp blocks (which also
+    // spread few cells over every SM) with their segments' sort buffers
+    const int gthreads = GB_THREADS;
     int per_sm = 0;
-    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_gather, gthreads, 0));
+    MZ_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_gather_big, gthreads, GB_SMEM));
     const int gblocks = (int)std::max<int64_t>(
         1, std::min<int64_t>(div_up(d->n_cells, gthreads / 32), (int64_t)c->num_sms * std::max(per_sm, 1)));
     VwDev* V = d->d_vw;
@@ -1187,7 +1198,7 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
             b.props = want_props ? 1 : 0;
             b.physics = 0;
             b.advance = 0;
-            MZ_LAUNCH(c, "step_cell_final", k_cell_gather, gblocks, gthreads, 0, v, b);
+            MZ_LAUNCH(c, "step_cell_final", k_cell_gather_big, gblocks, gthreads, GB_SMEM, v, b);
             S.cur ^= 1;
         };
         const int64_t todo = n_steps - done;
