@@ -564,6 +564,20 @@ constexpr size_t MB_SMEM = MB_OFF_OX + (size_t)MB_BINS * sizeof(PX);
 static_assert((size_t)MB_N * (sizeof(int32_t) + 2 * sizeof(double) + 1) <= (size_t)MB_N * sizeof(PX),
               "octree scratch must fit the position region");
 
+// FP32 value of a positive double by truncation of its mantissa (relative
+// error below 2^-23, never upward); ok = false outside the FP32 normal range
+__device__ __forceinline__ float f32_of_positive(double x, bool& ok)
+{
+    const long long bits = __double_as_longlong(x);
+    if (bits == 0) {
+        ok = true;
+        return 0.0f;
+    }
+    const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+    ok = bits > 0 && e >= -126 && e <= 127;
+    return __int_as_float(((e + 127) << 23) | (int)((bits >> 29) & 0x7FFFFF));
+}
+
 // compute_octant through integer keys: for doubles that are not NaN, x > m
 // exactly when key(x) > key(m) as signed integers (-0.0 taken as +0.0), and
 // integer compares keep the FP64 pipe free
@@ -618,6 +632,7 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
     PV* ov = reinterpret_cast<PV*>(smem + MB_OFF_OV);
     PX* ox = reinterpret_cast<PX*>(smem + MB_OFF_OX);
     __shared__ double s_red[NW][6];
+    __shared__ double s_wa[MB_BINS];  // bin weights for the choice of the bin to split (see below)
     __shared__ int s_nbins;
     __shared__ int s_pos[MB_BINS], s_kbig[MB_BINS];
     __shared__ int s_scan[NW][2];
@@ -691,17 +706,28 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
             b.refinable = (n > 2) && (a.prm.max_depth > 0);
             b.pad = 0;
             bins[0] = b;
+            s_wa[0] = 1e50;
         }
         int nbins = 1;
         int total = n >= 2 ? 2 : n;  // total_post_merge_np
         __syncwarp();
-        for (;;) {
+        // The heaviest refinable bin, first in bin order on ties.  A child's
+        // weight -- the sum of its particles' weights in particle order, the
+        // reference's rounding -- is a sequential FP64 chain; here a child
+        // first gets an FP32 sum (within 4e-6 relative of the exact one) and
+        // the choice is made on those when no other refinable bin comes
+        // within 1e-5 of the largest; otherwise the exact weights of the
+        // contenders decide.  Exact weights of the remaining bins follow the
+        // octree, in parallel.
+        auto heaviest = [&](bool exact, double floor_w, int& bid_out) {
             double bw = -1.0;
             int bid = -1;
             for (int b = lane; b < nbins; b += 32) {
                 const MergeBin& B = bins[b];
-                if (B.refinable && B.w > bw) {
-                    bw = B.w;
+                if (!B.refinable || s_wa[b] < floor_w) continue;
+                const double w = exact ? B.w : s_wa[b];
+                if (w > bw) {
+                    bw = w;
                     bid = b;
                 }
             }
@@ -714,7 +740,31 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                     bid = id2;
                 }
             }
+            bid_out = bid;
+            return bw;
+        };
+        for (;;) {
+            int bid = -1;
+            const double bwa = heaviest(false, -1.0, bid);
             if (bid < 0) break;
+            {
+                const double thr = bwa - 1e-5 * bwa;
+                bool near = false;
+                for (int b = lane; b < nbins; b += 32)
+                    near |= b != bid && bins[b].refinable && s_wa[b] >= thr;
+                if (__any_sync(0xFFFFFFFFu, near)) {
+                    for (int b = lane; b < nbins; b += 32) {
+                        MergeBin& B = bins[b];
+                        if (B.refinable && s_wa[b] >= thr && B.w < 0.0) {
+                            double w = 0.0;
+                            for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
+                            B.w = w;
+                        }
+                    }
+                    __syncwarp();
+                    heaviest(true, thr, bid);
+                }
+            }
             if (total + 14 > a.target) break;
 
             // split_bin! (:503-633)
@@ -773,8 +823,28 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                 for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
             }
             __syncwarp();
+            // the octants' weights in FP32: lane-strided partial sums over the
+            // sorted list (at most MB_N / 32 = 48 terms each), then a warp tree
+            float wf[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool fok = true;
+            for (int j = lane; j < nb; j += 32) {
+                bool ok;
+                const float f = f32_of_positive(tw[j], ok);
+                fok &= ok;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (j >= incl[k] - cnt[k] && j < incl[k]) wf[k] += f;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) wf[k] += __shfl_xor_sync(0xFFFFFFFFu, wf[k], o);
+            const bool approx = __all_sync(0xFFFFFFFFu, fok);
+            // weights outside the FP32 range: the exact sums now, in particle
+            // order as the reference sums them (octant k's particles sit in
+            // [incl[k-1], incl[k]) in reversed particle order)
             double wo = 0.0;
-            {
+            if (!approx) {
                 int lo = 0, hi = 0;
 #pragma unroll
                 for (int k = 0; k < 8; ++k)
@@ -790,6 +860,10 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                     if (cnt[k] == 0) continue;
                     const int id = kch == 0 ? bid : nbins + kch - 1;
                     const double wk = __shfl_sync(0xFFFFFFFFu, wo, k);
+                    float wfk = 0.f;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (q == k) wfk = wf[q];
                     if (lane == 0) {
                         MergeBin b;
                         for (int q = 0; q < 3; ++q) {
@@ -803,7 +877,8 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                             }
                         }
                         b.np = cnt[k];
-                        b.w = wk;
+                        b.w = approx ? -1.0 : wk;  // -1: the exact weight is still to be summed
+                        s_wa[id] = approx ? (double)wfk : wk;
                         b.depth = P.depth + 1;
                         b.start = startk;
                         b.end = startk + cnt[k] - 1;
@@ -827,6 +902,17 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
     }
     __syncthreads();
     const int nbins = s_nbins;
+    // the exact weights still missing: each bin's particles in particle order
+    // (its range holds them reversed), one thread per bin
+    for (int q = tid; q < nbins; q += MB_THREADS) {
+        MergeBin& B = bins[q];
+        if (B.w < 0.0) {
+            double w = 0.0;
+            for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
+            B.w = w;
+        }
+    }
+    __syncthreads();
     // the particles in list order (the octree scratch is dead: lx takes it)
     for (int i = tid; i < n; i += MB_THREADS) {
         const int q = pis[i];
