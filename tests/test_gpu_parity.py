@@ -99,6 +99,31 @@ def test_sort_random_bit_exact(ctx, orc, n_cells, n, seed):
     assert np.array_equal(dind[:, 0], oind[0, :, 0])
 
 
+def test_sort_large_segments_bit_exact(ctx, orc):
+    """Destination segments of up to 1,024 particles (register sort), of
+    1,025-2,048 (sorted in a shared-memory buffer) and above 2,048 (sorted in
+    place in global memory) end bit for bit like the oracle's sort."""
+    rng = np.random.default_rng(9)
+    L = 5e-4
+    counts = np.array([5, 1024, 1025, 1500, 2048, 2049, 3000])
+    n_cells, n = len(counts), int(counts.sum())
+    sp = species(["Ar"])
+    w, v, x, cell = random_particles(rng, n, n_cells, L=L)
+    dest = rng.permutation(np.repeat(np.arange(n_cells), counts))
+    x[:, 0] = (dest + rng.uniform(0.01, 0.99, n)) * (L / n_cells)
+    x[:, 1] = np.arange(n)
+    o = oracle_state(orc, n_cells, sp, mz.VHS, [(w, v, x, cell)])
+    dom = device_state(ctx, n_cells, sp, interactions(sp), [(w, v, x, cell)])
+    o.sort(0, L=L, nx=n_cells)
+    perm = dom.sort(0, mz.Grid1DUniform(L, n_cells), return_index=True)
+    orows, ocell = oracle_logical(o, 0)
+    drows, dcell = device_logical(dom, 0)
+    assert np.array_equal(np.bincount(dcell, minlength=n_cells), counts)
+    assert np.array_equal(orows, drows) and np.array_equal(ocell, dcell)
+    assert np.array_equal(perm, o.pv_get(0)["index"][:n] - 1)
+    dom.close()
+
+
 # ---------------------------------------------------------------- convection
 def test_convection_golden_on_device(ctx, golden):
     sc = scenario(golden, "convection_specular_4particles")

@@ -283,6 +283,31 @@ def test_two_launch_step_equals_fused(ctx, orc):
     assert_close_rows(a2["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T, two launches")
 
 
+def test_launch_forms_with_cells_above_1024_particles(ctx, orc):
+    """Cells of ~1,500 particles take the gathers' sorts for large segments
+    (in place in global memory in these kernels): the three launch forms give
+    the same particles and properties, equal to the oracle loop's."""
+    results = []
+    for launches in (1, 2, 3):
+        sp, grid, walls, dt, o, dom, seed = couette_setup(ctx, orc, nx=10, ppc=1500, seed=31)
+        n_before = device_logical(dom, 0)[1]
+        assert np.bincount(n_before, minlength=10).min() > 1024
+        inst, avg = mz.PhysProps(dom), mz.PhysProps(dom)
+        plan = couette_plan(grid, walls, dt, avg_start=2, n_avg=3)
+        plan.launches = launches
+        dom.step(plan, 4, inst, avg)
+        results.append((device_logical(dom, 0), inst.fetch(), avg.fetch()))
+        if launches == 1:
+            ref_avg = oracle_couette(orc, o, grid, walls, dt, seed, 4, 2)
+        dom.close()
+    (r1, i1, a1) = results[0]
+    for r2, i2, a2 in results[1:]:
+        assert np.array_equal(r1[1], r2[1]) and np.array_equal(r1[0], r2[0])
+        for k in ("np", "n", "v", "T"):
+            assert np.array_equal(i1[k], i2[k]) and np.array_equal(a1[k], a2[k]), k
+    assert_close_rows(a1["T"][:, 0:1], ref_avg[5].reshape(-1, 1), 1e-11, "averaged T")
+
+
 def test_two_species_couette_step_matches_reference_loop(ctx, orc):
     """An Ar + He mixture between the Couette walls: the fused and the
     two-launch 1-D step give the same particles, and both follow the
