@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MZ_ABI_VERSION 2
+#define MZ_ABI_VERSION 3
 #define MZ_MAX_SPECIES 4
 
 enum {
@@ -143,6 +143,8 @@ typedef struct {
     int64_t merge_threshold;
     int64_t merge_target;
     mz_octree_params octree;
+    int32_t split_lanes;  /* equal_weight = 0: lanes per cell of the splitting NTC, 8, 16 or 32; 0:
+                             the autotuner's choice, else 32.  Results do not depend on it */
 } mz_step_plan;
 
 /* ---------------------------------------------------------------- context */
@@ -487,9 +489,10 @@ int mz_server_set_hbm_headroom(mz_server* server, int64_t bytes);
  * mz_step calls whose plan leaves big_cell at 0.  *big_cell_out receives the
  * threshold (0-D) or, for 1-D, the launches value minus one (0 fused, 1 two
  * launches, 2 gathering and physics warps side by side).  A variable-weight plan
- * (equal_weight = 0) tries only the lanes per cell of its splitting NTC
- * (6 * trial_steps steps, without a graph), compares the splitting NTC's own
- * launch times (the lanes change nothing else), and *big_cell_out receives 0.
+ * (equal_weight = 0) tries only the lanes per cell of its splitting NTC (8,
+ * 16, 32; 6 * trial_steps steps, without a graph), compares the splitting
+ * NTC's own launch times (the lanes change nothing else), and *big_cell_out
+ * receives 0.
  * No counterpart in the reference. */
 int mz_step_autotune(mz_domain* dom, const mz_step_plan* plan, int64_t trial_steps, int32_t* lanes, int32_t* big_cell);
 

@@ -131,6 +131,7 @@ struct mz_domain_s {
     int64_t hitq_cap = 0;
     // fused-step mapping chosen by mz_step_autotune (0: the default rules)
     int32_t tuned_lanes = 0;    // lanes per cell in k_cell's NTC (8, 16, 32)
+    int32_t tuned_vw_lanes = 0; // lanes per cell of the variable-weight step's splitting NTC (8, 16, 32)
     int32_t tuned_big = 0;      // 0-D block-per-cell threshold (-1: never)
     int32_t tuned_split = 0;    // 1-D: 1 = gather + props and NTC + convection in two launches,
                                 // 2 = one launch with gathering and physics warps side by side

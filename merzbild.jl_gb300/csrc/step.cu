@@ -1126,7 +1126,8 @@ static void launch_step_vw(mz_domain* d, const mz_step_plan* plan, int64_t n_ste
     // a batch ends at its first split, so a cell's batches hold ~2-3
     // candidates and narrow groups let one FP64 instruction serve several
     // cells; with few cells, one-warp blocks spread the warps over every SM
-    const int G = d->tuned_lanes ? d->tuned_lanes : 8;
+    const int G = plan->split_lanes ? plan->split_lanes : (d->tuned_vw_lanes ? d->tuned_vw_lanes : 32);
+    MZ_REQUIRE(G == 8 || G == 16 || G == 32, "mz_step: split_lanes must be 0, 8, 16 or 32");
     using KNtc = void (*)(DomainView, int, double, const uint32_t*, const int*, const int32_t*, const int32_t*);
     const KNtc kntc = G == 8 ? k_vw_ntc<8> : (G == 16 ? k_vw_ntc<16> : k_vw_ntc<32>);
     const int cblocks = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(d->n_cells, 256), (int64_t)c->num_sms * 8));
@@ -1269,14 +1270,18 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     mz_step_plan p = *plan;
     p.big_cell = 0;
     p.launches = 0;
+    p.split_lanes = 0;
     std::vector<float> total(nconf, 0.0f);
     uint64_t step = plan->step0;
     cudaEvent_t e0, e1;
     MZ_CK(cudaEventCreate(&e0));
     MZ_CK(cudaEventCreate(&e1));
     auto apply = [&](int k) {
+        if (vw) {
+            d->tuned_vw_lanes = lanes_c[k / nb];
+            return;
+        }
         d->tuned_lanes = lanes_c[k / nb];
-        if (vw) return;
         d->tuned_big = plan->dims == 0 ? big_c[k % nb] : -1;
         d->tuned_split = plan->dims == 0 ? 0 : k % nb;
     };
@@ -1322,6 +1327,6 @@ void autotune_step(mz_domain* d, const mz_step_plan* plan, int64_t trial_steps, 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     apply((int)(std::min_element(total.begin(), total.end()) - total.begin()));
-    if (lanes_out) *lanes_out = d->tuned_lanes;
+    if (lanes_out) *lanes_out = vw ? d->tuned_vw_lanes : d->tuned_lanes;
     if (big_out) *big_out = vw ? 0 : (plan->dims == 0 ? d->tuned_big : d->tuned_split);
 }

@@ -116,6 +116,7 @@ struct MzStepPlan
     launches::Int32
     hit_queue_capacity::Int64
     merge_threshold::Int64; merge_target::Int64; octree::DeviceOctree
+    split_lanes::Int32
 end
 
 # ------------------------------------------------------------------ handles
@@ -457,7 +458,7 @@ function step!(dp::DeviceParticles, n_steps; grid::DeviceGrid1D=DeviceGrid1D(1.0
     w = walls === nothing ? DeviceWalls1D((0.0, 0.0), ntuple(_ -> 0.0, 6), (0.0, 0.0),
                                           ntuple(_ -> 0.0, 2 * MZ_MAX_SPECIES)) : walls
     plan = MzStepPlan(dims, 1, equal_weight ? 1 : 0, 1, avg_start, n_avg, Δt, dw_tol, step0, 1, 0, grid, w, 0, 0,
-                      merge_threshold, merge_target, octree)
+                      merge_threshold, merge_target, octree, 0)
     check(ccall((:mz_step, libmz), Cint, (Ptr{Cvoid}, Ref{MzStepPlan}, Int64, Ptr{Cvoid}, Ptr{Cvoid}),
                 dp.ptr, plan, n_steps, inst === nothing ? C_NULL : inst.ptr, avg === nothing ? C_NULL : avg.ptr),
           dp.ctx)

@@ -75,7 +75,7 @@ class StepPlan(C.Structure):
     _fields_ = [("dims", i32), ("collide", i32), ("equal_weight", i32), ("props", i32), ("avg_start", i64),
                 ("n_avg", i64), ("dt", d), ("dw_tol", d), ("step0", u64), ("use_graph", i32), ("big_cell", i32),
                 ("grid", Grid1D), ("walls", Walls1D), ("launches", i32), ("hit_queue_capacity", i64),
-                ("merge_threshold", i64), ("merge_target", i64), ("octree", OctreeParams)]
+                ("merge_threshold", i64), ("merge_target", i64), ("octree", OctreeParams), ("split_lanes", i32)]
 
 
 _SIGS = {

@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol(built):
     import merzgpu
 
     assert sorted(merzgpu.exported_symbols()) == syms  # the Python binding covers the whole ABI
-    assert merzgpu.lib().mz_version() == 2
+    assert merzgpu.lib().mz_version() == 3
 
 
 def test_julia_binding_calls_only_declared_symbols():

@@ -120,7 +120,8 @@ def test_splitting_and_merging_conserve_per_cell(ctx):
     assert merged > 0 and dom.counters()["splits"] > 0
 
 
-def _vw_plan(grid, walls, dt, octree, threshold, target, dims=1, step0=0, graph=True, avg_start=0, n_avg=1):
+def _vw_plan(grid, walls, dt, octree, threshold, target, dims=1, step0=0, graph=True, avg_start=0, n_avg=1,
+             split_lanes=0):
     """mz_step with equal_weight = 0: ntc! with splitting, merging of the cells
     above `threshold` down to `target`, (1-D) convection, sort, props."""
     p = mz._lib.StepPlan()
@@ -132,6 +133,7 @@ def _vw_plan(grid, walls, dt, octree, threshold, target, dims=1, step0=0, graph=
     if walls is not None:
         p.walls = walls.c_struct()
     p.merge_threshold, p.merge_target, p.octree = threshold, target, octree.params
+    p.split_lanes = split_lanes
     return p
 
 
@@ -204,29 +206,34 @@ def test_fused_varweight_step_equals_standalone_loop(ctx, orc, graph):
 
 
 def test_varweight_lanes_per_cell_change_no_result(ctx):
-    """8, 16 or 32 lanes per cell in the splitting NTC (chosen by
-    mz_step_autotune on real steps): the same particles after the same steps."""
+    """8, 16 or 32 lanes per cell in the splitting NTC, set by the plan or
+    chosen by mz_step_autotune on real steps: the same particles after the
+    same steps."""
     nx, ppc, steps, threshold, target, seed = 40, 150, 14, 170, 90, 55
     sp, inter, grid, walls, dt, smax, arrays = _varweight_state(nx, ppc, seed)
     octree = mz.OctreeN2Merge(max_Nbins=6000)
     runs = []
-    for tune in (True, False):
+    for lanes in ("tune", 8, 16, 32):
         dom = mz.Domain(ctx, nx, sp, 8 * nx * ppc, interactions=inter, seed=seed)
         dom.upload(0, *arrays)
         dom.set_cell_volumes(grid.V)
         dom.set_sigma_g_w_max(0, 0, smax)
         done = 0
-        if tune:
-            lanes, big = dom.autotune(_vw_plan(grid, walls, dt, octree, threshold, target), trial_steps=1)
-            assert lanes in (8, 16, 32) and big == 0
+        if lanes == "tune":
+            chosen, big = dom.autotune(_vw_plan(grid, walls, dt, octree, threshold, target), trial_steps=1)
+            assert chosen in (8, 16, 32) and big == 0
             done = 6
-        dom.step(_vw_plan(grid, walls, dt, octree, threshold, target, step0=done), steps - done)
+        dom.step(_vw_plan(grid, walls, dt, octree, threshold, target, step0=done,
+                          split_lanes=0 if lanes == "tune" else lanes), steps - done)
         runs.append(device_logical(dom, 0))
+        assert dom.counters()["splits"] > 0
         dom.close()
-    assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][0], runs[1][0])
+    for r in runs[1:]:
+        assert np.array_equal(runs[0][1], r[1]) and np.array_equal(runs[0][0], r[0])
 
 
-def test_fused_varweight_couette_at_the_benchmark_size_matches_oracle(ctx, orc):
+@pytest.mark.parametrize("split_lanes", [32, 8])
+def test_fused_varweight_couette_at_the_benchmark_size_matches_oracle(ctx, orc, split_lanes):
     """The variable-weight Couette configuration: 1,000 cells, 1,000 initial
     particles per cell with weights log-uniform over two decades, merging of
     cells above 1,200 particles down to 300; four fused steps against the
@@ -241,7 +248,7 @@ def test_fused_varweight_couette_at_the_benchmark_size_matches_oracle(ctx, orc):
     dom.set_cell_volumes(grid.V)
     dom.set_sigma_g_w_max(0, 0, smax)
     inst = mz.PhysProps(dom)
-    dom.step(_vw_plan(grid, walls, dt, octree, threshold, target), steps, inst)
+    dom.step(_vw_plan(grid, walls, dt, octree, threshold, target, split_lanes=split_lanes), steps, inst)
     o = oracle_state(orc, nx, sp, mz.VHS, [arrays], capacity=cap)
     o.cf_set_smax(0, 0, smax)
     oc = orc.Octree(orc.SPLIT_MID, mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit, 6000, 10)
