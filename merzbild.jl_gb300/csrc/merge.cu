@@ -70,18 +70,60 @@ struct MergeArgs {
     int32_t min_n;  // warp kernel: cells of at most min_n particles are left to the block kernel
 };
 
-__device__ __forceinline__ double warp_min(double v)
+// Integer order keys of doubles: for doubles that are not NaN, x > m exactly
+// when key(x) > key(m) as signed integers (-0.0 taken as +0.0).  Compares,
+// minima and maxima on keys run on the integer pipe; the FP64 pipe retires
+// one warp instruction per 64 cycles.
+__device__ __forceinline__ long long order_key(double x)
+{
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ __forceinline__ double of_order_key(long long k)
+{
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFll));
+}
+__device__ __forceinline__ long long warp_min_key(long long v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = min(v, (long long)__shfl_xor_sync(0xFFFFFFFFu, v, o));
     return v;
 }
-__device__ __forceinline__ double warp_max(double v)
+__device__ __forceinline__ long long warp_max_key(long long v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_xor_sync(0xFFFFFFFFu, v, o));
     return v;
 }
+// the minimum / maximum velocity keys over lane-strided particles
+struct KeyBounds {
+    long long lo[3], hi[3];
+    __device__ __forceinline__ KeyBounds()
+    {
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = order_key(9299792458.0);
+            hi[c] = order_key(-9299792458.0);
+        }
+    }
+    __device__ __forceinline__ void add(const PV& v)
+    {
+        const long long k[3] = {order_key(v.vx), order_key(v.vy), order_key(v.vz)};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = min(lo[c], k[c]);
+            hi[c] = max(hi[c], k[c]);
+        }
+    }
+    __device__ __forceinline__ void warp_reduce()
+    {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = warp_min_key(lo[c]);
+            hi[c] = warp_max_key(hi[c]);
+        }
+    }
+};
 
 // compute_octant (merging_octree_N2.jl:304-316), 0-based
 __device__ __forceinline__ int octant_of(const PV& v, const double* mid)
@@ -90,24 +132,18 @@ __device__ __forceinline__ int octant_of(const PV& v, const double* mid)
 }
 
 // bin_bounds_recompute! (:382-418): min / max of the velocities of list[bs, be]
+// (a zero bound may come out as +0.0 where the reference keeps -0.0: no
+// octant test or output depends on the sign of a zero bound)
 __device__ __forceinline__ void bounds_of(const Cols& A, const int32_t* pis, int bs, int be, double* mn, double* mx)
 {
     const int lane = threadIdx.x & 31;
-    double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
-    double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
-    for (int i = bs + lane; i <= be; i += 32) {
-        const PV v = A.wv[pis[i]];
-        lo[0] = fmin(lo[0], v.vx);
-        lo[1] = fmin(lo[1], v.vy);
-        lo[2] = fmin(lo[2], v.vz);
-        hi[0] = fmax(hi[0], v.vx);
-        hi[1] = fmax(hi[1], v.vy);
-        hi[2] = fmax(hi[2], v.vz);
-    }
+    KeyBounds kb;
+    for (int i = bs + lane; i <= be; i += 32) kb.add(A.wv[pis[i]]);
+    kb.warp_reduce();
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        mn[c] = warp_min(lo[c]);
-        mx[c] = warp_max(hi[c]);
+        mn[c] = of_order_key(kb.lo[c]);
+        mx[c] = of_order_key(kb.hi[c]);
     }
 }
 
@@ -578,15 +614,7 @@ __device__ __forceinline__ float f32_of_positive(double x, bool& ok)
     return __int_as_float(((e + 127) << 23) | (int)((bits >> 29) & 0x7FFFFF));
 }
 
-// compute_octant through integer keys: for doubles that are not NaN, x > m
-// exactly when key(x) > key(m) as signed integers (-0.0 taken as +0.0), and
-// integer compares keep the FP64 pipe free
-__device__ __forceinline__ long long order_key(double x)
-{
-    long long b = __double_as_longlong(x);
-    if (b == (long long)0x8000000000000000ull) b = 0;
-    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
-}
+// compute_octant through integer keys
 __device__ __forceinline__ int octant_of_keys(const PV& v, const long long* km)
 {
     return (order_key(v.vx) > km[0] ? 1 : 0) + (order_key(v.vy) > km[1] ? 2 : 0) + (order_key(v.vz) > km[2] ? 4 : 0);
@@ -596,21 +624,13 @@ __device__ __forceinline__ void bounds_of_list(const PV* cv, const int32_t* pis,
                                                double* mx)
 {
     const int lane = threadIdx.x & 31;
-    double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
-    double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
-    for (int i = bs + lane; i <= be; i += 32) {
-        const PV v = cv[pis[i]];
-        lo[0] = fmin(lo[0], v.vx);
-        lo[1] = fmin(lo[1], v.vy);
-        lo[2] = fmin(lo[2], v.vz);
-        hi[0] = fmax(hi[0], v.vx);
-        hi[1] = fmax(hi[1], v.vy);
-        hi[2] = fmax(hi[2], v.vz);
-    }
+    KeyBounds kb;
+    for (int i = bs + lane; i <= be; i += 32) kb.add(cv[pis[i]]);
+    kb.warp_reduce();
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        mn[c] = warp_min(lo[c]);
-        mx[c] = warp_max(hi[c]);
+        mn[c] = of_order_key(kb.lo[c]);
+        mx[c] = of_order_key(kb.hi[c]);
     }
 }
 
@@ -631,8 +651,7 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
     uint8_t* oct = reinterpret_cast<uint8_t*>(tw + MB_N);
     PV* ov = reinterpret_cast<PV*>(smem + MB_OFF_OV);
     PX* ox = reinterpret_cast<PX*>(smem + MB_OFF_OX);
-    __shared__ double s_red[NW][6];
-    __shared__ double s_wa[MB_BINS];  // bin weights for the choice of the bin to split (see below)
+    __shared__ long long s_wk[MB_BINS];  // bin weights for the choice of the bin to split (see below)
     __shared__ int s_nbins;
     __shared__ int s_pos[MB_BINS], s_kbig[MB_BINS];
     __shared__ int s_scan[NW][2];
@@ -652,35 +671,24 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
             mx[k] = 299792458.0;
         }
     } else {
-        double lo[3] = {9299792458.0, 9299792458.0, 9299792458.0};
-        double hi[3] = {-9299792458.0, -9299792458.0, -9299792458.0};
-        for (int i = tid; i < n; i += MB_THREADS) {
-            const PV v = cv[i];
-            lo[0] = fmin(lo[0], v.vx);
-            lo[1] = fmin(lo[1], v.vy);
-            lo[2] = fmin(lo[2], v.vz);
-            hi[0] = fmax(hi[0], v.vx);
-            hi[1] = fmax(hi[1], v.vy);
-            hi[2] = fmax(hi[2], v.vz);
-        }
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = warp_min(lo[k]);
-            hi[k] = warp_max(hi[k]);
-        }
+        KeyBounds kb;
+        for (int i = tid; i < n; i += MB_THREADS) kb.add(cv[i]);
+        kb.warp_reduce();
+        __shared__ long long s_kb[NW][6];
         if (lane == 0)
             for (int k = 0; k < 3; ++k) {
-                s_red[warp][k] = lo[k];
-                s_red[warp][3 + k] = hi[k];
+                s_kb[warp][k] = kb.lo[k];
+                s_kb[warp][3 + k] = kb.hi[k];
             }
         __syncthreads();
         for (int k = 0; k < 3; ++k) {
-            double l = s_red[0][k], h = s_red[0][3 + k];
+            long long l = s_kb[0][k], h = s_kb[0][3 + k];
             for (int w = 1; w < NW; ++w) {
-                l = fmin(l, s_red[w][k]);
-                h = fmax(h, s_red[w][3 + k]);
+                l = min(l, s_kb[w][k]);
+                h = max(h, s_kb[w][3 + k]);
             }
-            mn[k] = l;
-            mx[k] = h;
+            mn[k] = of_order_key(l);
+            mx[k] = of_order_key(h);
         }
         if (a.prm.init_bin_bounds == INIT_MINMAX_SYM)
             for (int k = 0; k < 3; ++k) {
@@ -706,7 +714,7 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
             b.refinable = (n > 2) && (a.prm.max_depth > 0);
             b.pad = 0;
             bins[0] = b;
-            s_wa[0] = 1e50;
+            s_wk[0] = b.refinable ? __double_as_longlong(1e50) : -1ll;
         }
         int nbins = 1;
         int total = n >= 2 ? 2 : n;  // total_post_merge_np
@@ -718,51 +726,70 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
         // the choice is made on those when no other refinable bin comes
         // within 1e-5 of the largest; otherwise the exact weights of the
         // contenders decide.  Exact weights of the remaining bins follow the
-        // octree, in parallel.
-        auto heaviest = [&](bool exact, double floor_w, int& bid_out) {
-            double bw = -1.0;
+        // octree, in parallel.  s_wk holds the approximate weight of a
+        // refinable bin as the bits of the double and -1 for the others:
+        // weights are not negative, and the bits of non-negative doubles
+        // order as their values, so the choice runs on integer compares (the
+        // FP64 pipe retires one warp instruction per 64 cycles).  One pass
+        // yields the largest weight, its bin and the runner-up weight.
+        for (;;) {
+            long long k1 = -1, k2 = -1;
             int bid = -1;
             for (int b = lane; b < nbins; b += 32) {
-                const MergeBin& B = bins[b];
-                if (!B.refinable || s_wa[b] < floor_w) continue;
-                const double w = exact ? B.w : s_wa[b];
-                if (w > bw) {
-                    bw = w;
+                const long long k = s_wk[b];
+                if (k > k1) {
+                    k2 = k1;
+                    k1 = k;
                     bid = b;
+                } else if (k > k2) {
+                    k2 = k;
                 }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const double w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
-                const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
-                if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
-                    bw = w2;
-                    bid = id2;
+                const long long o1 = __shfl_xor_sync(0xFFFFFFFFu, k1, o);
+                const long long o2 = __shfl_xor_sync(0xFFFFFFFFu, k2, o);
+                const int oid = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+                const bool take = oid >= 0 && (bid < 0 || o1 > k1 || (o1 == k1 && oid < bid));
+                const long long lose = take ? k1 : o1;
+                k2 = max(max(k2, o2), lose);
+                if (take) {
+                    k1 = o1;
+                    bid = oid;
                 }
             }
-            bid_out = bid;
-            return bw;
-        };
-        for (;;) {
-            int bid = -1;
-            const double bwa = heaviest(false, -1.0, bid);
             if (bid < 0) break;
-            {
-                const double thr = bwa - 1e-5 * bwa;
-                bool near = false;
-                for (int b = lane; b < nbins; b += 32)
-                    near |= b != bid && bins[b].refinable && s_wa[b] >= thr;
-                if (__any_sync(0xFFFFFFFFu, near)) {
-                    for (int b = lane; b < nbins; b += 32) {
-                        MergeBin& B = bins[b];
-                        if (B.refinable && s_wa[b] >= thr && B.w < 0.0) {
-                            double w = 0.0;
-                            for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
-                            B.w = w;
-                        }
+            const double b1 = __longlong_as_double(k1);
+            const long long kthr = __double_as_longlong(b1 - 1e-5 * b1);
+            if (k2 >= kthr) {
+                // the contenders' exact weights, then the heaviest of them
+                for (int b = lane; b < nbins; b += 32) {
+                    MergeBin& B = bins[b];
+                    if (s_wk[b] >= kthr && B.w < 0.0) {
+                        double w = 0.0;
+                        for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
+                        B.w = w;
                     }
-                    __syncwarp();
-                    heaviest(true, thr, bid);
+                }
+                __syncwarp();
+                long long bw = -1;
+                bid = -1;
+                for (int b = lane; b < nbins; b += 32) {
+                    if (s_wk[b] < kthr) continue;
+                    const long long w = __double_as_longlong(bins[b].w);
+                    if (w > bw) {
+                        bw = w;
+                        bid = b;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const long long w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
+                    const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+                    if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
+                        bw = w2;
+                        bid = id2;
+                    }
                 }
             }
             if (total + 14 > a.target) break;
@@ -854,44 +881,46 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                     }
                 for (int j = hi - 1; j >= lo; --j) wo += tw[j];
             }
-            {
-                int kch = 0, startk = bs;
-                for (int k = 0; k < 8; ++k) {
-                    if (cnt[k] == 0) continue;
-                    const int id = kch == 0 ? bid : nbins + kch - 1;
-                    const double wk = __shfl_sync(0xFFFFFFFFu, wo, k);
-                    float wfk = 0.f;
+            // the children: lane k writes octant k's bin; the first non-empty
+            // octant takes the parent's slot, the others are appended in
+            // octant order
+            int cl = 0, il = 0;
+            float wfl = 0.f;
 #pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (q == k) wfk = wf[q];
-                    if (lane == 0) {
-                        MergeBin b;
-                        for (int q = 0; q < 3; ++q) {
-                            const bool upper = (k >> q) & 1;
-                            if (a.prm.bin_bounds_compute == BOUNDS_INHERIT) {
-                                b.vmin[q] = upper ? mid[q] : P.vmin[q];
-                                b.vmax[q] = upper ? P.vmax[q] : mid[q];
-                            } else {
-                                b.vmin[q] = P.vmin[q];
-                                b.vmax[q] = P.vmax[q];
-                            }
-                        }
-                        b.np = cnt[k];
-                        b.w = approx ? -1.0 : wk;  // -1: the exact weight is still to be summed
-                        s_wa[id] = approx ? (double)wfk : wk;
-                        b.depth = P.depth + 1;
-                        b.start = startk;
-                        b.end = startk + cnt[k] - 1;
-                        b.refinable = (cnt[k] > 2) && (b.depth < a.prm.max_depth);
-                        b.pad = 0;
-                        bins[id] = b;
-                    }
-                    total += cnt[k] >= 2 ? 2 : cnt[k];
-                    startk += cnt[k];
-                    ++kch;
+            for (int k = 0; k < 8; ++k)
+                if (lane == k) {
+                    cl = cnt[k];
+                    il = incl[k];
+                    wfl = wf[k];
                 }
-                total -= 2;
+            const unsigned nonempty = __ballot_sync(0xFFFFFFFFu, cl > 0);
+            if (cl > 0) {
+                const int kch = __popc(nonempty & lanemask_lt());
+                const int id = kch == 0 ? bid : nbins + kch - 1;
+                MergeBin b;
+                for (int q = 0; q < 3; ++q) {
+                    const bool upper = (lane >> q) & 1;
+                    if (a.prm.bin_bounds_compute == BOUNDS_INHERIT) {
+                        b.vmin[q] = upper ? mid[q] : P.vmin[q];
+                        b.vmax[q] = upper ? P.vmax[q] : mid[q];
+                    } else {
+                        b.vmin[q] = P.vmin[q];
+                        b.vmax[q] = P.vmax[q];
+                    }
+                }
+                b.np = cl;
+                b.w = approx ? -1.0 : wo;  // -1: the exact weight is still to be summed
+                b.depth = P.depth + 1;
+                b.start = bs + il - cl;
+                b.end = bs + il - 1;
+                b.refinable = (cl > 2) && (b.depth < a.prm.max_depth);
+                b.pad = 0;
+                s_wk[id] = b.refinable ? __double_as_longlong(approx ? (double)wfl : wo) : -1ll;
+                bins[id] = b;
             }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) total += cnt[k] >= 2 ? 2 : cnt[k];
+            total -= 2;
             __syncwarp();
             for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
             nbins += nne - 1;
