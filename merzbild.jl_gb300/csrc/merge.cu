@@ -590,6 +590,7 @@ __global__ void __launch_bounds__(256) k_merge(DomainView d, MergeArgs a)
 // bin moments (one thread per bin, the wide bins one warp each) and the write-
 // back -- use every warp.  Same arithmetic in the same order as merge_cell.
 constexpr int MB_THREADS = 256, MB_N = 1536, MB_BINS = 384;
+constexpr int MB_SPLIT_BLOCK = 128;  // splits of at least this many particles run on every warp of the block
 constexpr size_t MB_OFF_PIS = (size_t)MB_BINS * sizeof(MergeBin);
 constexpr size_t MB_OFF_CV = MB_OFF_PIS + (size_t)MB_N * sizeof(int32_t);
 constexpr size_t MB_OFF_LV = MB_OFF_CV + (size_t)MB_N * sizeof(PV);
@@ -698,105 +699,132 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
             }
     }
 
-    // compute_octree! (:998-1039) by the first warp
-    if (warp == 0) {
-        if (lane == 0) {
-            MergeBin b;
-            b.w = 1e50;
-            for (int k = 0; k < 3; ++k) {
-                b.vmin[k] = mn[k];
-                b.vmax[k] = mx[k];
+    {
+        // compute_octree! (:998-1039).  The first warp chooses the bins to split
+        // and writes the children.  A split of MB_SPLIT_BLOCK or more particles
+        // runs its octant and counting-sort passes on every warp of the block,
+        // each on a contiguous chunk of the bin's list (the counting sort's order
+        // is the one-warp order: a warp's ranks start after the earlier chunks'),
+        // smaller splits on the first warp alone.
+        __shared__ int s_bid, s_nb;
+        __shared__ int s_wc[NW][8];
+        __shared__ float s_wf[NW][8];
+        __shared__ int s_fok[NW];
+        int nbins = 1;               // first warp
+        int total = n >= 2 ? 2 : n;  // total_post_merge_np, first warp
+        bool more = true;            // first warp: max_Nbins leaves room for a split
+        if (warp == 0) {
+            if (lane == 0) {
+                MergeBin b;
+                b.w = 1e50;
+                for (int k = 0; k < 3; ++k) {
+                    b.vmin[k] = mn[k];
+                    b.vmax[k] = mx[k];
+                }
+                b.np = n;
+                b.start = 0;
+                b.end = n - 1;
+                b.depth = 0;
+                b.refinable = (n > 2) && (a.prm.max_depth > 0);
+                b.pad = 0;
+                bins[0] = b;
+                s_wk[0] = b.refinable ? __double_as_longlong(1e50) : -1ll;
             }
-            b.np = n;
-            b.start = 0;
-            b.end = n - 1;
-            b.depth = 0;
-            b.refinable = (n > 2) && (a.prm.max_depth > 0);
-            b.pad = 0;
-            bins[0] = b;
-            s_wk[0] = b.refinable ? __double_as_longlong(1e50) : -1ll;
+            __syncwarp();
         }
-        int nbins = 1;
-        int total = n >= 2 ? 2 : n;  // total_post_merge_np
-        __syncwarp();
-        // The heaviest refinable bin, first in bin order on ties.  A child's
-        // weight -- the sum of its particles' weights in particle order, the
-        // reference's rounding -- is a sequential FP64 chain; here a child
-        // first gets an FP32 sum (within 4e-6 relative of the exact one) and
-        // the choice is made on those when no other refinable bin comes
-        // within 1e-5 of the largest; otherwise the exact weights of the
-        // contenders decide.  Exact weights of the remaining bins follow the
-        // octree, in parallel.  s_wk holds the approximate weight of a
-        // refinable bin as the bits of the double and -1 for the others:
-        // weights are not negative, and the bits of non-negative doubles
-        // order as their values, so the choice runs on integer compares (the
-        // FP64 pipe retires one warp instruction per 64 cycles).  One pass
-        // yields the largest weight, its bin and the runner-up weight.
         for (;;) {
-            long long k1 = -1, k2 = -1;
-            int bid = -1;
-            for (int b = lane; b < nbins; b += 32) {
-                const long long k = s_wk[b];
-                if (k > k1) {
-                    k2 = k1;
-                    k1 = k;
-                    bid = b;
-                } else if (k > k2) {
-                    k2 = k;
+            if (warp == 0) {
+                // The heaviest refinable bin, first in bin order on ties.  A
+                // child's weight -- the sum of its particles' weights in particle
+                // order, the reference's rounding -- is a sequential FP64 chain;
+                // here a child first gets an FP32 sum (within 4e-6 relative of the
+                // exact one) and the choice is made on those when no other
+                // refinable bin comes within 1e-5 of the largest; otherwise the
+                // exact weights of the contenders decide.  Exact weights of the
+                // remaining bins follow the octree, in parallel.  s_wk holds the
+                // approximate weight of a refinable bin as the bits of the double
+                // and -1 for the others: weights are not negative, and the bits of
+                // non-negative doubles order as their values, so the choice runs
+                // on integer compares (the FP64 pipe retires one warp instruction
+                // per 64 cycles).  One pass yields the largest weight, its bin and
+                // the runner-up weight.
+                int bid = -1;
+                if (more) {
+                    long long k1 = -1, k2 = -1;
+                    for (int b = lane; b < nbins; b += 32) {
+                        const long long k = s_wk[b];
+                        if (k > k1) {
+                            k2 = k1;
+                            k1 = k;
+                            bid = b;
+                        } else if (k > k2) {
+                            k2 = k;
+                        }
+                    }
+    #pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const long long o1 = __shfl_xor_sync(0xFFFFFFFFu, k1, o);
+                        const long long o2 = __shfl_xor_sync(0xFFFFFFFFu, k2, o);
+                        const int oid = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+                        const bool take = oid >= 0 && (bid < 0 || o1 > k1 || (o1 == k1 && oid < bid));
+                        const long long lose = take ? k1 : o1;
+                        k2 = max(max(k2, o2), lose);
+                        if (take) {
+                            k1 = o1;
+                            bid = oid;
+                        }
+                    }
+                    if (bid >= 0) {
+                        const double b1 = __longlong_as_double(k1);
+                        const long long kthr = __double_as_longlong(b1 - 1e-5 * b1);
+                        if (k2 >= kthr) {
+                            // the contenders' exact weights, then the heaviest of them
+                            for (int b = lane; b < nbins; b += 32) {
+                                MergeBin& B = bins[b];
+                                if (s_wk[b] >= kthr && B.w < 0.0) {
+                                    double w = 0.0;
+                                    for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
+                                    B.w = w;
+                                }
+                            }
+                            __syncwarp();
+                            long long bw = -1;
+                            bid = -1;
+                            for (int b = lane; b < nbins; b += 32) {
+                                if (s_wk[b] < kthr) continue;
+                                const long long w = __double_as_longlong(bins[b].w);
+                                if (w > bw) {
+                                    bw = w;
+                                    bid = b;
+                                }
+                            }
+    #pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) {
+                                const long long w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
+                                const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
+                                if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
+                                    bw = w2;
+                                    bid = id2;
+                                }
+                            }
+                        }
+                        if (total + 14 > a.target) bid = -1;
+                    }
+                }
+                if (lane == 0) {
+                    s_bid = bid;
+                    s_nb = bid >= 0 ? bins[bid].end - bins[bid].start + 1 : 0;
                 }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const long long o1 = __shfl_xor_sync(0xFFFFFFFFu, k1, o);
-                const long long o2 = __shfl_xor_sync(0xFFFFFFFFu, k2, o);
-                const int oid = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
-                const bool take = oid >= 0 && (bid < 0 || o1 > k1 || (o1 == k1 && oid < bid));
-                const long long lose = take ? k1 : o1;
-                k2 = max(max(k2, o2), lose);
-                if (take) {
-                    k1 = o1;
-                    bid = oid;
-                }
-            }
+            __syncthreads();
+            const int bid = s_bid, nb = s_nb;
             if (bid < 0) break;
-            const double b1 = __longlong_as_double(k1);
-            const long long kthr = __double_as_longlong(b1 - 1e-5 * b1);
-            if (k2 >= kthr) {
-                // the contenders' exact weights, then the heaviest of them
-                for (int b = lane; b < nbins; b += 32) {
-                    MergeBin& B = bins[b];
-                    if (s_wk[b] >= kthr && B.w < 0.0) {
-                        double w = 0.0;
-                        for (int j = B.end; j >= B.start; --j) w += cv[pis[j]].w;
-                        B.w = w;
-                    }
-                }
-                __syncwarp();
-                long long bw = -1;
-                bid = -1;
-                for (int b = lane; b < nbins; b += 32) {
-                    if (s_wk[b] < kthr) continue;
-                    const long long w = __double_as_longlong(bins[b].w);
-                    if (w > bw) {
-                        bw = w;
-                        bid = b;
-                    }
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const long long w2 = __shfl_xor_sync(0xFFFFFFFFu, bw, o);
-                    const int id2 = __shfl_xor_sync(0xFFFFFFFFu, bid, o);
-                    if (id2 >= 0 && (bid < 0 || w2 > bw || (w2 == bw && id2 < bid))) {
-                        bw = w2;
-                        bid = id2;
-                    }
-                }
-            }
-            if (total + 14 > a.target) break;
+            const bool wide = nb >= MB_SPLIT_BLOCK;
+            if (!wide && warp != 0) continue;  // the first warp splits alone
 
             // split_bin! (:503-633)
             const MergeBin P = bins[bid];
-            const int bs = P.start, be = P.end, nb = be - bs + 1;
+            const int bs = P.start, be = P.end;
             double vmin[3], vmax[3];
             for (int k = 0; k < 3; ++k) {
                 vmin[k] = P.vmin[k];
@@ -809,34 +837,83 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                 mid[k] = 0.5 * (vmin[k] + vmax[k]);
                 kmid[k] = order_key(mid[k]);
             }
+            // this warp's chunk of the list: all of it on the first warp alone
+            const int chunk = wide ? ((nb + MB_THREADS - 1) / MB_THREADS) * 32 : nb;
+            const int i0w = wide ? min(nb, warp * chunk) : 0;
+            const int i1w = min(nb, i0w + chunk);
+            // octants and counts; the octants' weights in FP32 on the way
+            // (lane-strided partial sums of at most MB_N / 32 = 48 terms, a warp
+            // tree, and the warps' sums added in warp order)
             int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int i = lane; i < nb; i += 32) {
+            float wf[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool fok = true;
+            for (int i = i0w + lane; i < i1w; i += 32) {
                 const PV v = cv[pis[bs + i]];
                 const int o = octant_of_keys(v, kmid);
                 oct[i] = (uint8_t)o;
                 wl[i] = v.w;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) cnt[k] += (o == k);
+                bool ok;
+                const float f = f32_of_positive(v.w, ok);
+                fok &= ok;
+    #pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    cnt[k] += (o == k);
+                    if (o == k) wf[k] += f;
+                }
             }
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cnt[k] = __reduce_add_sync(0xFFFFFFFFu, cnt[k]);
+    #pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                cnt[k] = __reduce_add_sync(0xFFFFFFFFu, cnt[k]);
+    #pragma unroll
+                for (int o = 16; o > 0; o >>= 1) wf[k] += __shfl_xor_sync(0xFFFFFFFFu, wf[k], o);
+            }
+            bool approx = __all_sync(0xFFFFFFFFu, fok);
+            int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (wide) {
+                if (lane == 0) {
+    #pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        s_wc[warp][k] = cnt[k];
+                        s_wf[warp][k] = wf[k];
+                    }
+                    s_fok[warp] = approx ? 1 : 0;
+                }
+                __syncthreads();
+                // the bin's counts, and this warp's ranks start after the earlier chunks'
+    #pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    int t = 0, before = 0;
+                    float f = 0.f;
+                    for (int w = 0; w < NW; ++w) {
+                        const int x = s_wc[w][k];
+                        t += x;
+                        before += w < warp ? x : 0;
+                        f += s_wf[w][k];
+                    }
+                    cnt[k] = t;
+                    seen[k] = before;
+                    wf[k] = f;
+                }
+                for (int w = 0; w < NW; ++w) approx &= s_fok[w] != 0;
+            }
             __syncwarp();
             int incl[8], run = 0;
             int nne = 0;
-#pragma unroll
+    #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 run += cnt[k];
                 incl[k] = run;
                 nne += cnt[k] > 0;
             }
-            int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int i0 = 0; i0 < nb; i0 += 32) {
+            // the counting sort: octant k's particles in [incl[k-1], incl[k]),
+            // in reversed list order
+            for (int i0 = i0w; i0 < i1w; i0 += 32) {
                 const int i = i0 + lane;
-                const bool in = i < nb;
+                const bool in = i < i1w;
                 const int o = in ? oct[i] : 8;
                 const unsigned peers = __match_any_sync(0xFFFFFFFFu, o);
                 int r = __popc(peers & lanemask_lt()), end_o = 0;
-#pragma unroll
+    #pragma unroll
                 for (int k = 0; k < 8; ++k)
                     if (o == k) {
                         r += seen[k];
@@ -846,34 +923,26 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                     tmp[end_o - 1 - r] = pis[bs + i];
                     tw[end_o - 1 - r] = wl[i];
                 }
-#pragma unroll
+    #pragma unroll
                 for (int k = 0; k < 8; ++k) seen[k] += __popc(__ballot_sync(0xFFFFFFFFu, in && o == k));
             }
-            __syncwarp();
-            // the octants' weights in FP32: lane-strided partial sums over the
-            // sorted list (at most MB_N / 32 = 48 terms each), then a warp tree
-            float wf[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            bool fok = true;
-            for (int j = lane; j < nb; j += 32) {
-                bool ok;
-                const float f = f32_of_positive(tw[j], ok);
-                fok &= ok;
-#pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    if (j >= incl[k] - cnt[k] && j < incl[k]) wf[k] += f;
+            if (wide) {
+                __syncthreads();
+                for (int i = tid; i < nb; i += MB_THREADS) pis[bs + i] = tmp[i];
+                __syncthreads();  // the first warp's next choice may read the list
+                if (warp != 0) continue;
+            } else {
+                __syncwarp();
+                for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
+                __syncwarp();
             }
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) wf[k] += __shfl_xor_sync(0xFFFFFFFFu, wf[k], o);
-            const bool approx = __all_sync(0xFFFFFFFFu, fok);
-            // weights outside the FP32 range: the exact sums now, in particle
-            // order as the reference sums them (octant k's particles sit in
-            // [incl[k-1], incl[k]) in reversed particle order)
+            // the first warp: weights outside the FP32 range are summed exactly
+            // now, in particle order as the reference sums them (octant k's
+            // particles sit in [incl[k-1], incl[k]) in reversed particle order)
             double wo = 0.0;
             if (!approx) {
                 int lo = 0, hi = 0;
-#pragma unroll
+    #pragma unroll
                 for (int k = 0; k < 8; ++k)
                     if (lane == k) {
                         lo = incl[k] - cnt[k];
@@ -886,7 +955,7 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
             // octant order
             int cl = 0, il = 0;
             float wfl = 0.f;
-#pragma unroll
+    #pragma unroll
             for (int k = 0; k < 8; ++k)
                 if (lane == k) {
                     cl = cnt[k];
@@ -918,18 +987,16 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                 s_wk[id] = b.refinable ? __double_as_longlong(approx ? (double)wfl : wo) : -1ll;
                 bins[id] = b;
             }
-#pragma unroll
+    #pragma unroll
             for (int k = 0; k < 8; ++k) total += cnt[k] >= 2 ? 2 : cnt[k];
             total -= 2;
-            __syncwarp();
-            for (int i = lane; i < nb; i += 32) pis[bs + i] = tmp[i];
             nbins += nne - 1;
+            more = nbins + 7 <= a.prm.max_Nbins;
             __syncwarp();
-            if (nbins + 7 > a.prm.max_Nbins) break;
         }
-        if (lane == 0) s_nbins = nbins;
+        if (tid == 0) s_nbins = nbins;
+        __syncthreads();
     }
-    __syncthreads();
     const int nbins = s_nbins;
     // the exact weights still missing: each bin's particles in particle order
     // (its range holds them reversed), one thread per bin

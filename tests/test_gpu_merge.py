@@ -144,6 +144,49 @@ CASES = [
 ]
 
 
+
+@pytest.mark.parametrize("weights", ["beyond_fp32", "equal"])
+def test_merge_bin_choice_on_exact_weights_vs_oracle(ctx, orc, weights):
+    """Bins chosen on exact weights: weights beyond the FP32 range (each
+    split sums its octants exactly at once) and equal weights (octants of
+    equal counts tie, so the contenders' exact sums decide), in cells of up
+    to 1,500 particles whose first splits run on every warp of the block."""
+    rng = np.random.default_rng(7 if weights == "equal" else 8)
+    n_cells = 24
+    (w, v, x, cells), L = _random_cells(rng, n_cells, 1500, 1.0)
+    if weights == "equal":
+        w = np.full(w.size, 1e12)
+    else:
+        w = 10.0 ** (35.0 + 10.0 * rng.random(w.size))
+    arrays = (w, v, x, cells)
+    init, bounds, max_bins, max_depth, target, threshold = (mz.OctreeInitBinMinMaxVel, mz.OctreeBinBoundsInherit,
+                                                            4096, 10, 60, 100)
+    sp = species(["Ar"])
+    o = oracle_state(orc, n_cells, sp, mz.VHS, [arrays])
+    dom = mz.Domain(ctx, n_cells, sp, w.size + 64, seed=77)
+    dom.upload(0, *arrays)
+    octree = mz.OctreeN2Merge(init_bin_bounds=init, bin_bounds_compute=bounds, max_Nbins=max_bins,
+                              max_depth=max_depth)
+    merged = dom.merge_octree(0, octree, target, threshold=threshold, step=5)
+    oc = orc.Octree(orc.SPLIT_MID, init, bounds, max_bins, max_depth)
+    counts = np.bincount(cells, minlength=n_cells)
+    expect = 0
+    for c in range(n_cells):
+        if counts[c] <= threshold:
+            continue
+        o.merge_octree(oc, 0, c + 1, target, seed=77, step=5)
+        expect += 1
+    assert merged == expect and expect > 5 and counts.max() > 1000
+    orows, ocells = oracle_logical(o, 0)
+    drows, dcells = device_logical(dom, 0)
+    assert np.array_equal(ocells, dcells)
+    assert_close_rows(orows, drows, RTOL, "merged cells")
+    oind, ont, _ = o.pia_get()
+    ind, nt = dom.indexer(0)
+    assert nt == ont[0] == dom.info(0)["n_total"]
+    assert np.array_equal(ind[:, 3], oind[0, :, 3]) and np.array_equal(ind[:, 6], oind[0, :, 6])
+
+
 @pytest.mark.parametrize("init,bounds,max_bins,max_depth,target,threshold,grid", CASES)
 def test_merge_cells_vs_oracle(ctx, orc, init, bounds, max_bins, max_depth, target, threshold, grid):
     """Cells of 0..1500 variable-weight particles merged in one launch against
