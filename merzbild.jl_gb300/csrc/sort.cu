@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) k_sort_gather(DomainView d, int s)
     int32_t* mine = sortbuf + (size_t)(threadIdx.x >> 5) * SORT_SMEM_KEYS;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < d.n_cells; c += warps) {
         const Indexer p = S.ind[c];
-        sort_gather_segment(S, c, p.start1, p.n1, mine);
+        sort_gather_segment<false, true>(S, c, p.start1, p.n1, mine);
     }
 }
 

@@ -48,6 +48,61 @@ __device__ __forceinline__ void warp_bitonic(int32_t (&v)[E])
     }
 }
 
+// The same network with its (k, j) stages in runtime loops: fully unrolled,
+// the 32- and 64-row sorts are more code than the instruction caches hold
+// (instruction fetch was the first stall of the gathers that run them).  A
+// stage within a row is one unrolled pass of shuffles; a stage across rows
+// (j >= 32) dispatches on the row distance to an unrolled pass.
+template <int JR, int E>
+__device__ __forceinline__ void bitonic_rows(int32_t (&v)[E], int k)
+{
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const int rp = r ^ JR;
+        if (rp > r) {
+            const bool asc = ((r * 32) & k) == 0;
+            const int32_t a = v[r], b = v[rp];
+            const bool sw = asc ? (a > b) : (a < b);
+            v[r] = sw ? b : a;
+            v[rp] = sw ? a : b;
+        }
+    }
+}
+template <int E>
+__device__ __forceinline__ void warp_bitonic_rolled(int32_t (&v)[E])
+{
+    static_assert(E == 32 || E == 64, "rolled network for 32 or 64 rows");
+    const int lane = threadIdx.x & 31;
+    constexpr int P = 32 * E;
+#pragma unroll 1
+    for (int k = 2; k <= P; k <<= 1) {
+#pragma unroll 1
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                switch (j >> 5) {
+                case 1: bitonic_rows<1>(v, k); break;
+                case 2: bitonic_rows<2>(v, k); break;
+                case 4: bitonic_rows<4>(v, k); break;
+                case 8: bitonic_rows<8>(v, k); break;
+                case 16: bitonic_rows<16>(v, k); break;
+                default:
+                    if constexpr (E == 64) bitonic_rows<32>(v, k);
+                    break;
+                }
+            } else {
+                const bool lower = (lane & j) == 0;
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    const int p = r * 32 + lane;
+                    const int32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[r], j);
+                    const bool asc = (p & k) == 0;
+                    v[r] = (lower == asc) ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+}
+
 // Batcher's odd-even merge sort of a[0, n) in global memory by one warp.
 // Every comparator moves the smaller key to the lower index, so lengths that
 // are not a power of two need no padding.
@@ -130,7 +185,7 @@ __device__ __forceinline__ void gather_records(const Cols& A, const Cols& B, con
     }
 }
 
-template <int E>
+template <int E, bool ROLLED = false>
 __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c, int32_t start, int32_t N, Sums4& acc)
 {
     const int lane = threadIdx.x & 31;
@@ -140,7 +195,8 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
         const int q = r * 32 + lane;
         v[r] = q < N ? S.idx[start + q] : INT_MAX;
     }
-    warp_bitonic<E>(v);
+    if constexpr (ROLLED && E >= 32) warp_bitonic_rolled<E>(v);
+    else warp_bitonic<E>(v);
     gather_records<E>(S.A, S.B, v, start, N, acc);
 #pragma unroll
     for (int r = 0; r < E; ++r) {
@@ -222,18 +278,20 @@ __device__ __forceinline__ void sort_gather_staged(const SpeciesView& S, int32_t
 
 // Segments above 512 particles take an out-of-line call, so the registers
 // their 32-row sort needs do not raise the register count of every caller.
+template <bool ROLLED>
 static __device__ __noinline__ void sort_gather_regs_32(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
                                                         Sums4& acc)
 {
-    sort_gather_regs<32>(S, c, start, N, acc);
+    sort_gather_regs<32, ROLLED>(S, c, start, N, acc);
 }
 
 // Segments of 1,025 .. 2,048 particles in kernels with registers to spare
 // (BIG): 64 rows per lane, out of line like the 32-row form.
+template <bool ROLLED>
 static __device__ __noinline__ void sort_gather_regs_64(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
                                                         Sums4& acc)
 {
-    sort_gather_regs<64>(S, c, start, N, acc);
+    sort_gather_regs<64, ROLLED>(S, c, start, N, acc);
 }
 
 // Other segments of more than 1,024 particles sort their source slots with
@@ -244,7 +302,10 @@ constexpr int SORT_SMEM_KEYS = 2048;
 // Sort the source slots of cell c's segment [start, start + N) and gather the
 // particles from buffer A into the same positions of buffer B (one warp).
 // Returns this lane's first-pass props sums of the gathered particles.
-template <bool BIG = false>
+// ROLLED: the 32- and 64-row sorts with the rolled network (kernels that
+// only gather; the fused step kernel keeps the unrolled one, whose call
+// needs fewer registers saved around it).
+template <bool BIG = false, bool ROLLED = false>
 __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32_t c, int32_t start, int32_t N,
                                                      int32_t* sortbuf = nullptr)
 {
@@ -255,8 +316,8 @@ __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32
     else if (N <= 128) sort_gather_regs<4>(S, c, start, N, acc);
     else if (N <= 256) sort_gather_regs<8>(S, c, start, N, acc);
     else if (N <= 512) sort_gather_regs<16>(S, c, start, N, acc);
-    else if (N <= 1024) sort_gather_regs_32(S, c, start, N, acc);
-    else if (BIG && N <= 2048) sort_gather_regs_64(S, c, start, N, acc);
+    else if (N <= 1024) sort_gather_regs_32<ROLLED>(S, c, start, N, acc);
+    else if (BIG && N <= 2048) sort_gather_regs_64<ROLLED>(S, c, start, N, acc);
     else {
         const bool shared = sortbuf && N <= SORT_SMEM_KEYS;
         int32_t* keys = shared ? sortbuf : S.idx + start;

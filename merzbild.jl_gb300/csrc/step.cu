@@ -180,7 +180,8 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                 for (int q = 0; q < nq; ++q) {
                     const Indexer p = S.ind[c0 + q];
                     const Sums4 t = (WS && MODE == 1) ? sort_gather_segment_staged(S, c0 + q, p.start1, p.n1, stage)
-                                                      : sort_gather_segment<BIG>(S, c0 + q, p.start1, p.n1, sortbuf);
+                                                      : sort_gather_segment<BIG, MODE == 1 && !WS>(S, c0 + q, p.start1,
+                                                                                            p.n1, sortbuf);
                     if (props1) props_pass1_into_lane(t.n, t.sx, t.sy, t.sz, q, mn, msx, msy, msz);
                 }
                 __syncwarp();
