@@ -71,7 +71,7 @@ __device__ __forceinline__ void bitonic_rows(int32_t (&v)[E], int k)
 template <int E>
 __device__ __forceinline__ void warp_bitonic_rolled(int32_t (&v)[E])
 {
-    static_assert(E == 32 || E == 64, "rolled network for 32 or 64 rows");
+    static_assert(E == 16 || E == 32 || E == 64, "rolled network for 16, 32 or 64 rows");
     const int lane = threadIdx.x & 31;
     constexpr int P = 32 * E;
 #pragma unroll 1
@@ -84,9 +84,11 @@ __device__ __forceinline__ void warp_bitonic_rolled(int32_t (&v)[E])
                 case 2: bitonic_rows<2>(v, k); break;
                 case 4: bitonic_rows<4>(v, k); break;
                 case 8: bitonic_rows<8>(v, k); break;
-                case 16: bitonic_rows<16>(v, k); break;
                 default:
-                    if constexpr (E == 64) bitonic_rows<32>(v, k);
+                    if constexpr (E >= 32) {
+                        if (j >> 5 == 16) bitonic_rows<16>(v, k);
+                        else if constexpr (E == 64) bitonic_rows<32>(v, k);
+                    }
                     break;
                 }
             } else {
@@ -195,7 +197,7 @@ __device__ __forceinline__ void sort_gather_regs(const SpeciesView& S, int32_t c
         const int q = r * 32 + lane;
         v[r] = q < N ? S.idx[start + q] : INT_MAX;
     }
-    if constexpr (ROLLED && E >= 32) warp_bitonic_rolled<E>(v);
+    if constexpr (ROLLED && E >= 16) warp_bitonic_rolled<E>(v);
     else warp_bitonic<E>(v);
     gather_records<E>(S.A, S.B, v, start, N, acc);
 #pragma unroll
@@ -315,7 +317,7 @@ __device__ __forceinline__ Sums4 sort_gather_segment(const SpeciesView& S, int32
     else if (N <= 64) sort_gather_regs<2>(S, c, start, N, acc);
     else if (N <= 128) sort_gather_regs<4>(S, c, start, N, acc);
     else if (N <= 256) sort_gather_regs<8>(S, c, start, N, acc);
-    else if (N <= 512) sort_gather_regs<16>(S, c, start, N, acc);
+    else if (N <= 512) sort_gather_regs<16, ROLLED>(S, c, start, N, acc);
     else if (N <= 1024) sort_gather_regs_32<ROLLED>(S, c, start, N, acc);
     else if (BIG && N <= 2048) sort_gather_regs_64<ROLLED>(S, c, start, N, acc);
     else {
