@@ -630,19 +630,27 @@ __global__ void __launch_bounds__(256, 4) k_step_scatter(DomainView d, int s, in
     if (n_dev) n = *n_dev;
     for (int64_t t0 = (int64_t)blockIdx.x * SCATTER_TILE; t0 < n; t0 += (int64_t)gridDim.x * SCATTER_TILE) {
         const int64_t t1 = min(n, t0 + (int64_t)SCATTER_TILE);
-        const int32_t cmid = S.cell[(t0 + t1 - 1) / 2];
-        const int kb = (cmid >= 0 ? cmid : S.key[(t0 + t1 - 1) / 2]) - SCATTER_WINDOW / 2;
-        for (int b = threadIdx.x; b < SCATTER_WINDOW; b += blockDim.x) hist[b] = 0;
-        __syncthreads();
+        // every load of the tile first, so that they are in flight together
+        // (and across the barrier below)
         int32_t key[PER], rank[PER];
 #pragma unroll
         for (int r = 0; r < PER; ++r) {
             const int64_t slot = t0 + threadIdx.x + 256 * r;
+            const bool in = slot < t1;
+            key[r] = in ? S.key[slot] : 0;
+            rank[r] = in && (!n_dev || S.cell[slot] >= 0) ? 0 : -1;
+        }
+        const int32_t cmid = S.cell[(t0 + t1 - 1) / 2];
+        const int kb = (cmid >= 0 ? cmid : S.key[(t0 + t1 - 1) / 2]) - SCATTER_WINDOW / 2;
+        for (int b = threadIdx.x; b < SCATTER_WINDOW; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const int64_t slot = t0 + threadIdx.x + 256 * r;
+            const bool live = rank[r] == 0;
             rank[r] = -1;
-            key[r] = 0;
-            if (slot < t1 && (!n_dev || S.cell[slot] >= 0)) {
-                const int32_t k = S.key[slot];
-                key[r] = k;
+            if (live) {
+                const int32_t k = key[r];
                 const int b = k - kb;
                 if ((unsigned)b < (unsigned)SCATTER_WINDOW) {
                     rank[r] = atomicAdd(&hist[b], 1);
