@@ -731,6 +731,9 @@ __device__ __forceinline__ CellMoments props_cells_finish(const Cols& P, const I
         const double ux = __shfl_sync(0xFFFFFFFFu, r.ux, q), uy = __shfl_sync(0xFFFFFFFFu, r.uy, q);
         const double uz = __shfl_sync(0xFFFFFFFFu, r.uz, q);
         double E = 0.0;
+        // unrolled so that several records' loads are in flight (the sums
+        // keep their order)
+#pragma unroll 4
         for (int j = lane; j < p.n1; j += 32) {
             const PV u = P.wv[p.start1 + j];
             const double dx = u.vx - ux, dy = u.vy - uy, dz = u.vz - uz;
