@@ -276,15 +276,27 @@ __device__ __forceinline__ void cell_body(const DomainView& d, const StepArgs& a
                 const uint32_t rid = cell_rid(d, cq), stp = cell_step(d, cq, step);
                 const Indexer p = S.ind[cq];
                 const int32_t n1 = p.n1, st1 = p.start1;
+                // each row's position and velocity are loaded one row ahead,
+                // before the current row's stores (other particles)
+                double x_next = 0.0, vx_next = 0.0;
+                if (lane < n1) {
+                    x_next = Q.pos[(int64_t)st1 + lane].x;
+                    vx_next = Q.wv[(int64_t)st1 + lane].vx;
+                }
                 for (int j0 = 0; j0 < n1; j0 += 32) {
                     const int j = j0 + lane;
                     const bool in = j < n1;
                     const int64_t qq = (int64_t)st1 + j;
+                    const double x_row = x_next, vx_row = vx_next;
+                    if (j + 32 < n1) {
+                        x_next = Q.pos[qq + 32].x;
+                        vx_next = Q.wv[qq + 32].vx;
+                    }
                     int32_t key = 0;
                     bool counted = false, hit = false;
                     if (in) {
-                        double x = Q.pos[qq].x;
-                        const double xn = fma(Q.wv[qq].vx, a.dt, x);
+                        double x = x_row;
+                        const double xn = fma(vx_row, a.dt, x);
                         if (move_free(a.W, xn, x)) {
                             Q.pos[qq].x = x;
                             key = cell_of(d, x, a.W.inv_dx);
