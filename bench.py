@@ -35,7 +35,7 @@ ALG_BYTES = 112  # per particle-step: every particle read once and written once 
 # DRAM bytes moved per particle by the two-launch step (gather + props, then
 # NTC + convection) and by the one-launch step, and the FP64 warp
 # instructions per particle of a whole step
-DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH = 256.7
+DRAM_BYTES_PER_PARTICLE_TWO_LAUNCH = 276.5
 DRAM_BYTES_PER_PARTICLE_FUSED = 386.6
 FORMS = ("one fused launch", "two launches", "gathering and physics warps side by side")
 FP64_WARP_INST_PER_PARTICLE = 0.814

@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(256, 2) k_cell(DomainView d, StepArgs a)
 // gathered into nearby cells soon after; with one cell in flight per warp the
 // lines in flight fit in L2 and are reused there (four cells per warp keep
 // twice the L2 in flight and miss).
-__global__ void __launch_bounds__(256, 4) k_cell_gather(DomainView d, StepArgs a)
+__global__ void __launch_bounds__(256, 3) k_cell_gather(DomainView d, StepArgs a)
 {
     cell_body<32, 1>(d, a, nullptr);
 }
