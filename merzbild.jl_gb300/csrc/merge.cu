@@ -705,8 +705,12 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
         // runs its octant and counting-sort passes on every warp of the block,
         // each on a contiguous chunk of the bin's list (the counting sort's order
         // is the one-warp order: a warp's ranks start after the earlier chunks'),
-        // smaller splits on the first warp alone.
-        __shared__ int s_bid, s_nb;
+        // smaller splits on the first warp alone.  The chosen bin and its
+        // particle count pass through s_bid / s_nb by iteration parity: the
+        // first warp writes a slot again only after every warp has passed the
+        // next barrier, that is after each warp has read it.
+        __shared__ int s_bid[2], s_nb[2];
+        int it = 0;
         __shared__ int s_wc[NW][8];
         __shared__ float s_wf[NW][8];
         __shared__ int s_fok[NW];
@@ -812,12 +816,13 @@ __device__ void merge_cell_block(const DomainView& d, const MergeArgs& a, int c,
                     }
                 }
                 if (lane == 0) {
-                    s_bid = bid;
-                    s_nb = bid >= 0 ? bins[bid].end - bins[bid].start + 1 : 0;
+                    s_bid[it & 1] = bid;
+                    s_nb[it & 1] = bid >= 0 ? bins[bid].end - bins[bid].start + 1 : 0;
                 }
             }
             __syncthreads();
-            const int bid = s_bid, nb = s_nb;
+            const int bid = s_bid[it & 1], nb = s_nb[it & 1];
+            ++it;
             if (bid < 0) break;
             const bool wide = nb >= MB_SPLIT_BLOCK;
             if (!wide && warp != 0) continue;  // the first warp splits alone
